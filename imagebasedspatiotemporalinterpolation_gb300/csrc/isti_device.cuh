@@ -1,0 +1,130 @@
+// Device-side arithmetic of the interpolation path.
+//
+// Every function restates one helper of the reference renderer in the same
+// floating-point operation order; the translation unit is compiled with
+// -fmad=false (no multiply-add contraction) and IEEE division/square root, so
+// each result is bit-identical to the host oracle's.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace isti
+{
+// src/renderer.cu:16-28
+constexpr float EPS_1_FULL_RES = 0.002f;
+constexpr float EPS_1_LOW_RES = EPS_1_FULL_RES * 4.0f;
+constexpr float EPS_2_FULL_RES = 0.001f;
+constexpr float EPS_2_LOW_RES = 0.004f;
+constexpr float EPS_3 = 0.01f;
+constexpr unsigned long long SPLAT_EMPTY = 0xfefefefefefefefeull; // cudaMemset(..., 0xfe) of every byte
+constexpr uint32_t SOFTSHADOW_BITS = 2u;
+constexpr uint32_t SOFTSHADOW_VAL_MASK = 3u;
+
+struct KeyInfo
+{
+    float depth;
+    uint32_t sx, sy; // source pixel
+};
+
+// encodeSplattingKey / decodeSplattingKey, src/renderer.cu:65-74
+__device__ __forceinline__ unsigned long long encode_key(float depth, uint32_t x, uint32_t y)
+{
+    return ((unsigned long long)__float_as_uint(depth) << 32) | (unsigned long long)((x << 16) | y);
+}
+
+__device__ __forceinline__ KeyInfo decode_key(unsigned long long key)
+{
+    KeyInfo k;
+    k.depth = __uint_as_float((uint32_t)(key >> 32));
+    k.sx = ((uint32_t)key) >> 16;
+    k.sy = (uint32_t)(key & 0xFFFFull);
+    return k;
+}
+
+// pixel2CS, include/util/helper_common.h:66-69: 2 * (p + 0.5) / res - 1
+__device__ __forceinline__ float2 pixel2cs(uint32_t px, uint32_t py, uint32_t w, uint32_t h)
+{
+    float ax = (float)px + 0.5f, ay = (float)py + 0.5f;
+    ax = 2.0f * ax;
+    ay = 2.0f * ay;
+    ax = __fdiv_rn(ax, (float)w);
+    ay = __fdiv_rn(ay, (float)h);
+    return make_float2(ax - 1.0f, ay - 1.0f);
+}
+
+// CS2pixel, include/util/helper_common.h:71-75: floor((cs + 1) * res * 0.5)
+// (float -> int conversion truncates and saturates, NaN -> 0)
+__device__ __forceinline__ int2 cs2pixel(float cx, float cy, uint32_t w, uint32_t h)
+{
+    float ax = cx + 1.0f, ay = cy + 1.0f;
+    ax = ax * (float)w;
+    ay = ay * (float)h;
+    ax = ax * 0.5f;
+    ay = ay * 0.5f;
+    return make_int2(__float2int_rz(floorf(ax)), __float2int_rz(floorf(ay)));
+}
+
+__device__ __forceinline__ bool in_range(int2 p, uint32_t w, uint32_t h)
+{
+    return p.x >= 0 && (uint32_t)p.x < w && p.y >= 0 && (uint32_t)p.y < h;
+}
+
+// glm-subset mat4 * vec4: (m0*x + m1*y) + (m2*z + m3*w), column-major m
+__device__ __forceinline__ float4 matvec(const float *m, float4 v)
+{
+    float4 r;
+    r.x = __fadd_rn(__fadd_rn(__fmul_rn(m[0], v.x), __fmul_rn(m[4], v.y)), __fadd_rn(__fmul_rn(m[8], v.z), __fmul_rn(m[12], v.w)));
+    r.y = __fadd_rn(__fadd_rn(__fmul_rn(m[1], v.x), __fmul_rn(m[5], v.y)), __fadd_rn(__fmul_rn(m[9], v.z), __fmul_rn(m[13], v.w)));
+    r.z = __fadd_rn(__fadd_rn(__fmul_rn(m[2], v.x), __fmul_rn(m[6], v.y)), __fadd_rn(__fmul_rn(m[10], v.z), __fmul_rn(m[14], v.w)));
+    r.w = __fadd_rn(__fadd_rn(__fmul_rn(m[3], v.x), __fmul_rn(m[7], v.y)), __fadd_rn(__fmul_rn(m[11], v.z), __fmul_rn(m[15], v.w)));
+    return r;
+}
+
+// w / w without a division: exactly 1 for finite non-zero w, NaN otherwise
+__device__ __forceinline__ float self_ratio(float w)
+{
+    return (isfinite(w) && w != 0.0f) ? 1.0f : __int_as_float(0x7fffffff);
+}
+
+// CS2WS / WS2CS, include/util/helper_common.h:77-87: (M v) / (M v).w
+__device__ __forceinline__ float4 project(const float *m, float4 v)
+{
+    const float4 p = matvec(m, v);
+    return make_float4(__fdiv_rn(p.x, p.w), __fdiv_rn(p.y, p.w), __fdiv_rn(p.z, p.w), self_ratio(p.w));
+}
+
+__device__ __forceinline__ float z_to_depth(float z) { return __fmul_rn(__fadd_rn(z, 1.0f), 0.5f); } // :89-91
+__device__ __forceinline__ float depth_to_z(float d) { return __fsub_rn(__fmul_rn(d, 2.0f), 1.0f); } // :93-95
+
+// lerp_color, include/util/helper_common.h:22-25: (a + t * (b - a)) / 255
+__device__ __forceinline__ float lerp_ch(uint32_t a, uint32_t b, float t)
+{
+    const float fa = (float)a, fb = (float)b;
+    return __fdiv_rn(__fadd_rn(fa, __fmul_rn(t, __fsub_rn(fb, fa))), 255.f);
+}
+
+// to_8bit, include/util/helper_common.h:27-30: min(255, max(0, int(f * 255)))
+__device__ __forceinline__ uint32_t to_8bit(float f)
+{
+    const int v = __float2int_rz(__fmul_rn(f, 255.f));
+    return (uint32_t)min(255, max(0, v));
+}
+
+// color_to_uchar4(lerp_color(a, b, t)), packed RGBA8 in a uint32 (R in bits 0-7)
+__device__ __forceinline__ uint32_t lerp_color_u8(uint32_t a, uint32_t b, float t)
+{
+    uint32_t r = 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++)
+        r |= to_8bit(lerp_ch((a >> (8 * c)) & 255u, (b >> (8 * c)) & 255u, t)) << (8 * c);
+    return r;
+}
+
+// float -> unsigned char of make_uchar4(float, ...): truncation, saturation, NaN -> 0
+__device__ __forceinline__ uint32_t cvt_u8(float f)
+{
+    return (uint32_t)min(255u, __float2uint_rz(f));
+}
+} // namespace isti

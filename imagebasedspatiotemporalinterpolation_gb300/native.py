@@ -1,0 +1,112 @@
+"""ctypes binding of the C ABI in include/isti.h (libisti.so).
+
+The library is the product's only compute path.  Loading fails loudly when it
+has not been built: there is no Python or CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import _build
+
+ISTI_OK = 0
+ISTI_ERR_INVALID_ARG = 1
+ISTI_ERR_OOM = 2
+ISTI_ERR_CUDA = 3
+ISTI_ERR_TIMEOUT = 4
+ISTI_ERR_UNSUPPORTED = 5
+
+MODE_OURS = 0
+MODE_BACKWARD_BIDIRECTIONAL = 1
+MODE_BACKWARD_UNIDIRECTIONAL = 2
+MODE_SPLATTING = 3
+MODE_TIMEWARP = 4
+
+MOTION_NONE = 0
+MOTION_F32X4 = 1
+MOTION_F16X3 = 2
+
+MAX_AUX_CAMS = 7
+
+Mat16 = C.c_float * 16
+
+
+class IstiView(C.Structure):
+    _fields_ = [
+        ("width", C.c_uint32), ("height", C.c_uint32),
+        ("color", C.c_void_p), ("z", C.c_void_p), ("motion", C.c_void_p),
+        ("motion_format", C.c_int32),
+        ("shadow_color_a", C.c_void_p), ("shadow_color_b", C.c_void_p), ("shadow_info", C.c_void_p),
+        ("viewproj", Mat16), ("inv_viewproj", Mat16),
+    ]
+
+
+class IstiFrameData(C.Structure):
+    _fields_ = [
+        ("fwd", IstiView), ("bwd", IstiView), ("num_aux", C.c_int32),
+        ("aux_curr", C.POINTER(IstiView)), ("aux_next", C.POINTER(IstiView)),
+        ("aux_priority", C.POINTER(C.c_int32)),
+    ]
+
+
+class IstiRenderInfo(C.Structure):
+    _fields_ = [
+        ("width", C.c_uint32), ("height", C.c_uint32), ("alpha", C.c_float),
+        ("viewproj", Mat16), ("inv_viewproj", Mat16),
+        ("frames_per_anchor", C.c_int32), ("shadow_frames_per_anchor", C.c_int32),
+        ("no_shadows", C.c_int32), ("mode", C.c_int32),
+    ]
+
+
+# Every function include/isti.h declares: name -> (restype, argtypes)
+SIGNATURES = {
+    "isti_abi_version": (C.c_int32, []),
+    "isti_last_error": (C.c_char_p, []),
+    "isti_status_string": (C.c_char_p, [C.c_int]),
+    "isti_renderer_create": (C.c_int, [C.POINTER(C.c_void_p)]),
+    "isti_renderer_destroy": (C.c_int, [C.c_void_p]),
+    "isti_render": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(IstiRenderInfo), C.POINTER(IstiFrameData), C.c_void_p]),
+    "isti_renderer_view_buffers": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                             C.POINTER(C.c_void_p), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+}
+
+
+class IstiError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"isti status {status}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def load(path: str | None = None) -> C.CDLL:
+    """Load libisti.so (built in-tree by __graft_entry__.build())."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or _build.cuda_lib_path()
+    if not os.path.exists(p):
+        raise RuntimeError(f"{p} is missing: build the CUDA extension first (python -c 'import __graft_entry__ as g; g.build()')")
+    lib = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(status: int) -> None:
+    if status != ISTI_OK:
+        lib = load()
+        raise IstiError(status, lib.isti_last_error().decode(errors="replace"))
+
+
+def mat16(m) -> Mat16:
+    """Row-major 4x4 (numpy math convention) -> column-major float[16]."""
+    import numpy as np
+    a = np.asarray(m, dtype=np.float32).reshape(4, 4)
+    return Mat16(*a.T.reshape(-1).tolist())

@@ -1,0 +1,149 @@
+/*
+ * isti — GB300-native per-frame image-based spatio-temporal interpolation.
+ *
+ * C ABI of the interpolation path of the reference renderer
+ * (DerThomy/ImageBasedSpatioTemporalInterpolation, src/renderer.cu).  The
+ * entry points below replace, one for one:
+ *
+ *   isti_renderer_create / _destroy  <- Renderer::Renderer() (include/renderer.h:54)
+ *                                        and its lazily allocated members
+ *                                        (src/renderer.cu:549-605); the reference
+ *                                        never frees them, this library does on destroy.
+ *   isti_render                      <- Renderer::render(ImageBuffer<uchar4,4>&,
+ *                                        const RenderInfo, const FrameData&)
+ *                                        (include/renderer.h:56, src/renderer.cu:607-694)
+ *   isti_frame_data / isti_view      <- FrameData / MotionZBufferImage / AuxCamData
+ *                                        (include/data.h:12-116)
+ *   isti_render_info                 <- RenderInfo / AdditionalRenderInfo
+ *                                        (include/renderer.h:18-35)
+ *   isti_renderer_view_buffers       <- read access to the private splat buffers and
+ *                                        flow fields (include/renderer.h:64-92), for
+ *                                        bit-exact checks
+ *
+ * Conventions
+ *  - Pixel data lives in device memory, dense row-major, (x, y) at y*width + x;
+ *    the structs themselves are host memory.  Reads outside an image return
+ *    zero, as the reference's border-mode textures do.
+ *  - Matrices are float[16], column-major (element row r, column c at [c*4+r]),
+ *    the glm layout.
+ *  - Work is enqueued on `stream` (a cudaStream_t, NULL = legacy default
+ *    stream); no call blocks the host.  A renderer owns per-frame
+ *    intermediates, so use one renderer per concurrently rendering stream.
+ *  - Errors are returned, never thrown; isti_last_error() describes the last
+ *    failure on the calling thread.
+ *  - Arithmetic is IEEE binary32 with every multiply and add rounded
+ *    separately (no contraction), so results are reproducible bit for bit.
+ */
+#ifndef ISTI_H
+#define ISTI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ISTI_ABI_VERSION 1
+#define ISTI_MAX_AUX_CAMS 7
+
+typedef enum isti_status
+{
+    ISTI_OK = 0,
+    ISTI_ERR_INVALID_ARG = 1,
+    ISTI_ERR_OOM = 2,
+    ISTI_ERR_CUDA = 3,
+    ISTI_ERR_TIMEOUT = 4,
+    ISTI_ERR_UNSUPPORTED = 5
+} isti_status;
+
+/* RenderMode, include/renderer.h:9-16 */
+typedef enum isti_render_mode
+{
+    ISTI_MODE_OURS = 0,
+    ISTI_MODE_BACKWARD_BIDIRECTIONAL = 1,
+    ISTI_MODE_BACKWARD_UNIDIRECTIONAL = 2,
+    ISTI_MODE_SPLATTING = 3,
+    ISTI_MODE_TIMEWARP = 4
+} isti_render_mode;
+
+/* Object-motion layout.  F32X4 is the reference's float4 image
+ * (include/data.h:56); F16X3 is the compact half-precision xyz form, widened
+ * exactly to float on load. */
+typedef enum isti_motion_format
+{
+    ISTI_MOTION_NONE = 0,
+    ISTI_MOTION_F32X4 = 1,
+    ISTI_MOTION_F16X3 = 2
+} isti_motion_format;
+
+/* One camera at one keyframe (MotionZBufferImage, include/data.h:12-62). */
+typedef struct isti_view
+{
+    uint32_t width, height;        /* 1..65535 */
+    const void *color;             /* RGBA8, 4-byte aligned */
+    const float *z;                /* NDC z in [-1, 1] */
+    const void *motion;            /* NDC delta to the other keyframe, this view's
+                                      viewproj; NULL = no object motion */
+    int32_t motion_format;         /* isti_motion_format */
+    const void *shadow_color_a;    /* RGBA8 or NULL (NULL disables soft shadows) */
+    const void *shadow_color_b;    /* RGBA8 or NULL */
+    const void *shadow_info;       /* RGBA8, RGB = 24-bit field of 2-bit levels;
+                                      required when shadow_color_a is given */
+    float viewproj[16];
+    float inv_viewproj[16];
+} isti_view;
+
+/* FrameData (include/data.h:79-116): fwd = earlier keyframe, bwd = later one;
+ * aux_curr[i] / aux_next[i] = aux camera i at those keyframes. */
+typedef struct isti_frame_data
+{
+    isti_view fwd, bwd;
+    int32_t num_aux;               /* 0..ISTI_MAX_AUX_CAMS */
+    const isti_view *aux_curr;
+    const isti_view *aux_next;
+    const int32_t *aux_priority;   /* NULL = all 0 */
+} isti_frame_data;
+
+/* RenderInfo + AdditionalRenderInfo (include/renderer.h:18-35). */
+typedef struct isti_render_info
+{
+    uint32_t width, height;        /* must equal the main keyframes' size */
+    float alpha;                   /* interpolation factor t */
+    float viewproj[16];            /* client camera */
+    float inv_viewproj[16];
+    int32_t frames_per_anchor;
+    int32_t shadow_frames_per_anchor; /* 0..16 */
+    int32_t no_shadows;
+    int32_t mode;                  /* isti_render_mode */
+} isti_render_info;
+
+typedef struct isti_renderer isti_renderer;
+
+int32_t isti_abi_version(void);
+const char *isti_last_error(void);
+const char *isti_status_string(isti_status s);
+
+isti_status isti_renderer_create(isti_renderer **out);
+isti_status isti_renderer_destroy(isti_renderer *r);
+
+/* Renders one interpolated client frame into out_rgba (device, width*height
+ * RGBA8).  Pixels without a valid result keep their previous content
+ * (temporal hole filling, src/renderer.cu:416-419,462-463), so the caller
+ * keeps the buffer alive across frames. */
+isti_status isti_render(isti_renderer *r, void *out_rgba, const isti_render_info *info, const isti_frame_data *frame,
+                        void *stream);
+
+/* Device pointers to the intermediates of the last isti_render call for view
+ * `view` (0 fwd, 1 bwd, 2+2i aux i curr, 3+2i aux i next): 64-bit splat keys
+ * (depth bits << 32 | x << 16 | y), f32x4 source->client flow and f32x4
+ * source->other-keyframe flow, each width*height elements.  A field that is
+ * not materialised is returned as NULL.  Valid until the next render or
+ * destroy. */
+isti_status isti_renderer_view_buffers(const isti_renderer *r, int32_t view, const uint64_t **splat, const float **cam_ff,
+                                       const float **full_ff, uint32_t *width, uint32_t *height);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
