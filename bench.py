@@ -1,0 +1,442 @@
+#!/usr/bin/env python
+"""Benchmark: interpolated Mpix/s of the per-frame interpolation path at 1080p.
+
+Workload (the configuration the headline metric is quoted on): 1920x1080
+main camera plus left/right aux cameras at +-0.3 m (6 source views per
+keyframe pair), soft shadows on, seeded procedural scene (64 spheres,
+|v| <= 0.5 m/s, 30 Hz keyframes), client at 120 Hz (frames_per_anchor 4,
+shadow_frames_per_anchor 4), plain method (mode 0: 3x3 window, 3 search
+iterations).
+
+One step = one keyframe interval = 3 interpolated 1080p client frames
+(t = 0.25, 0.5, 0.75) between a resident keyframe pair; steps cycle over
+``--pairs`` resident pairs.  Inputs are larger than L2: each frame touches
+~0.8 GB (6 source views of colour, z, f16 motion, shadow A/B/Info plus the
+renderer's keys and flow fields), and 6 keyframes x 3 cameras (~1.6 GB) stay
+resident.
+
+value: device-resident throughput (CUDA events on the rendering stream).
+e2e:   the same metric through the C ABI with host buffers: each step
+       uploads the newly arrived keyframe data from pinned host memory
+       (colour, z, motion and shadow images of the new keyframe for the 3
+       cameras, plus the earlier keyframe's forward motion and shadows) and
+       reads the 3 output frames back.
+
+--impl reference times the reference's per-frame algorithm on the host
+cores (the C oracle, OpenMP over all threads: the reference has no CPU
+implementation and its GPU code cannot be built on the GPU host), one 1080p
+frame per step.
+
+Multi-GPU: replicas only (every frame is independent); each rank renders its
+own seeded stream, no collective on the data path; time = max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W, H = 1920, 1080
+AUX = (-0.3, 0.3)
+TS = (1, 2, 3)            # b of t = b / 4
+FPA = SFPA = 4
+METRIC = "interp Mpix/s @1080p"
+WORKLOAD = "1080p interpolation, 3 cameras (main + aux +-0.3 m), soft shadows, t in {0.25,0.5,0.75}, plain search (mode 0)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--pairs", type=int, default=5)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel: str):
+    """dram bytes per launch for `kernel` from the committed ncu summaries
+    (line 'traffic_bytes_per_launch <kernel> <bytes>')."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for fn in sorted(os.listdir(d)):
+        if not fn.endswith((".md", ".txt")):
+            continue
+        for line in open(os.path.join(d, fn)):
+            parts = line.strip().strip("`").split()
+            if len(parts) == 3 and parts[0] == "traffic_bytes_per_launch" and parts[1] == kernel:
+                return float(parts[2])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        if self.path:
+            with open(self.path, "w") as f:
+                f.write(out)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+# ------------------------------------------------------------------ CPU (oracle port)
+
+def cpu_frames(seq, pairs):
+    out = []
+    for p in range(pairs):
+        fr = seq.frame(p)
+        for b in TS:
+            out.append((fr, seq.client(p, b)))
+    return out
+
+
+def time_cpu(frames, budget_s: float, max_frames: int):
+    """Times the oracle port (all OpenMP threads) frame by frame; returns (Mpix/s, frames, seconds)."""
+    import numpy as np
+
+    import oracle
+    n, t_total, i = 0, 0.0, 0
+    prev = np.zeros((H, W, 4), np.uint8)
+    while n < max_frames and (t_total < budget_s or n == 0):
+        fr, cl = frames[i % len(frames)]
+        call = oracle.prepared_call(fr, cl, prev)
+        t0 = time.perf_counter()
+        call()
+        t_total += time.perf_counter() - t0
+        n += 1
+        i += 1
+    return n * W * H / 1e6 / t_total, n, t_total
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+    from imagebasedspatiotemporalinterpolation_gb300.scene import Sequence
+
+    oracle.build()
+    seq = Sequence(W, H, 2, seed=args.seed, aux_offsets=AUX, shadows=True)
+    frames = cpu_frames(seq, 1)
+    time_cpu(frames, float("inf"), args.warmup)              # warm-up frames
+    mpix_s, n, secs = time_cpu(frames, float("inf"), args.steps)  # exactly K frames
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(mpix_s, 3), "unit": "Mpix/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs * 1e3 / n, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "step": "one 1080p interpolated frame (t cycling 0.25/0.5/0.75)"},
+        "cpu_baseline": {"value": round(mpix_s, 3), "unit": "Mpix/s", "cores": cores, "kind": "port",
+                         "sample": f"{n} frames of the workload, C oracle restating src/renderer.cu, OpenMP over {cores} threads"},
+        "e2e": {"value": round(mpix_s, 3), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ GPU (ours)
+
+def main_ours(args):
+    import numpy as np
+    import torch
+
+    from imagebasedspatiotemporalinterpolation_gb300 import _build
+    from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame, DeviceView, Renderer
+    from imagebasedspatiotemporalinterpolation_gb300.scene import Sequence
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    _build.build_all()
+    dev = torch.device("cuda", local)
+    P = args.pairs
+    seq = Sequence(W, H, P + 1, seed=args.seed + rank, aux_offsets=AUX, shadows=True)
+    n_cams = 1 + len(AUX)
+
+    # ---- resident keyframes: per keyframe k, camera c: colour, z, motions, shadows
+    def up(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+    res = {}
+    for k in range(P + 1):
+        for c in range(n_cams):
+            kf = seq.keyframe(k, c)
+            res[(k, c)] = dict(color=up(kf.color), z=up(kf.z), mf=up(kf.motion_fwd), mb=up(kf.motion_bwd),
+                               sf=[up(a) for a in kf.shadow_fwd], sb=[up(a) for a in kf.shadow_bwd],
+                               vp=kf.viewproj.astype(np.float32), ivp=np.linalg.inv(kf.viewproj).astype(np.float32))
+
+    def dview(d, forward):
+        sh = d["sf"] if forward else d["sb"]
+        return DeviceView(d["color"], d["z"], d["mf"] if forward else d["mb"], sh[0], sh[1], sh[2], d["vp"], d["ivp"])
+
+    frames = []
+    for p in range(P):
+        fr = DeviceFrame(dview(res[(p, 0)], True), dview(res[(p + 1, 0)], False))
+        for c in range(1, n_cams):
+            fr.aux_curr.append(dview(res[(p, c)], True))
+            fr.aux_next.append(dview(res[(p + 1, c)], False))
+            fr.aux_priority.append(3)
+        frames.append(fr)
+    from imagebasedspatiotemporalinterpolation_gb300.renderer import render_info
+    clients = [[render_info(seq.client(p, b)) for b in TS] for p in range(P)]
+    out = torch.zeros((H, W, 4), dtype=torch.uint8, device=dev)
+    r = Renderer()
+    stream = torch.cuda.current_stream(dev)
+
+    def step(s):
+        p = s % P
+        for ci in clients[p]:
+            r.render(out, ci, frames[p], stream)
+
+    for s in range(args.warmup):
+        step(s)
+    torch.cuda.synchronize()
+
+    # ---- timed region (device-resident inputs)
+    n_frames = args.steps * len(TS)
+    fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n_frames)]
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    r.timing()          # discard warm-up
+    r.enable_timing(True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t0.record(stream)
+    fi = 0
+    for s in range(args.steps):
+        p = s % P
+        for ci in clients[p]:
+            fev[fi][0].record(stream)
+            r.render(out, ci, frames[p], stream)
+            fev[fi][1].record(stream)
+            fi += 1
+    t1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    r.enable_timing(False)
+    ms = t0.elapsed_time(t1)
+    tim = r.timing()
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    frame_ms = sorted(a.elapsed_time(b) for a, b in fev)
+    total_mpix = world * n_frames * W * H / 1e6
+    value = total_mpix / (ms / 1e3)
+
+    # ---- e2e: host buffers through the C ABI, uploads + read-back inside the timed region
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, seq, res, clients, r, dev, world)
+
+    # ---- roofline of the dominant kernel
+    px = W * H
+    n_views = 2 * n_cams
+    alg = {"splat_kernel": n_views * (4 + 6) * px, "reproj_kernel": (n_views * (4 + 12) + 4) * px}
+    per_launch_ms = {"splat_kernel": tim["splat_ms"] / max(1, tim["frames"]), "reproj_kernel": tim["reproj_ms"] / max(1, tim["frames"])}
+    dom = max(per_launch_ms, key=per_launch_ms.get)
+    peak, peak_kind = peaks()
+    achieved = alg[dom] / (per_launch_ms[dom] / 1e3) / 1e9
+    traffic = profile_traffic(dom)
+    roof = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": traffic,
+            "algorithmic_bytes_per_launch": alg[dom]}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+        oracle.build()
+        host_seq = Sequence(W, H, 2, seed=args.seed, aux_offsets=AUX, shadows=True)
+        mpix_s, n, secs = time_cpu(cpu_frames(host_seq, 1), args.cpu_seconds, 30)
+        cpu = {"value": round(mpix_s, 3), "unit": "Mpix/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{n} frames ({secs:.1f} s) of the same workload, C oracle (OpenMP, all threads)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "width": W, "height": H, "source_views": n_views, "frames_per_step": len(TS),
+                       "resident_pairs": P, "mode": 0, "l2": "inputs larger than L2 (~0.8 GB touched per frame)",
+                       "parallelism": f"replicas x{world}"},
+            "p50_frame_ms": round(frame_ms[len(frame_ms) // 2], 4),
+            "p99_frame_ms": round(frame_ms[min(len(frame_ms) - 1, int(0.99 * len(frame_ms)))], 4),
+            "kernels_ms_per_frame": {"key_init": round(tim["init_ms"] / max(1, tim["frames"]), 4),
+                                     "splat_kernel": round(per_launch_ms["splat_kernel"], 4),
+                                     "reproj_kernel": round(per_launch_ms["reproj_kernel"], 4)},
+            "gpu_launches": tim["kernel_launches"],
+            "clocks": clk,
+            "e2e": e2e,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    r.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def run_e2e(args, seq, res, clients, r, dev, world):
+    """Streams keyframes from pinned host memory: per step, the new keyframe's
+    data goes up, 3 frames are rendered, the 3 frames come back."""
+    import numpy as np
+    import torch
+
+    from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame, DeviceView
+
+    P = args.pairs
+    n_cams = 1 + len(AUX)
+
+    def pin(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+
+    host = {}
+    for k in range(P + 1):
+        for c in range(n_cams):
+            kf = seq.keyframe(k, c)
+            host[(k, c)] = dict(color=pin(kf.color), z=pin(kf.z), mf=pin(kf.motion_fwd), mb=pin(kf.motion_bwd),
+                                sf=[pin(a) for a in kf.shadow_fwd], sb=[pin(a) for a in kf.shadow_bwd])
+    like = lambda t: torch.empty_like(t, device=dev)
+    h0 = host[(0, 0)]
+    slots = [[dict(color=like(h0["color"]), z=like(h0["z"])) for _ in range(n_cams)] for _ in range(2)]
+    per_step = [dict(mf=like(h0["mf"]), mb=like(h0["mb"]), sf=[like(a) for a in h0["sf"]], sb=[like(a) for a in h0["sb"]])
+                for _ in range(n_cams)]
+    outs_host = [torch.empty((H, W, 4), dtype=torch.uint8).pin_memory() for _ in TS]
+    out = torch.zeros((H, W, 4), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    h2d = d2h = 0
+
+    def step(s, count):
+        nonlocal h2d, d2h
+        p = s % P
+        k0, k1 = p, p + 1
+        for c in range(n_cams):
+            hk0, hk1 = host[(k0, c)], host[(k1, c)]
+            if s == 0:  # first step: the earlier keyframe is not resident yet
+                slots[k0 % 2][c]["color"].copy_(hk0["color"], non_blocking=True)
+                slots[k0 % 2][c]["z"].copy_(hk0["z"], non_blocking=True)
+            pairs = [(slots[k1 % 2][c]["color"], hk1["color"]), (slots[k1 % 2][c]["z"], hk1["z"]),
+                     (per_step[c]["mb"], hk1["mb"]), (per_step[c]["mf"], hk0["mf"])]
+            pairs += list(zip(per_step[c]["sb"], hk1["sb"])) + list(zip(per_step[c]["sf"], hk0["sf"]))
+            for d, h in pairs:
+                d.copy_(h, non_blocking=True)
+                if count:
+                    h2d += h.numel() * h.element_size()
+        views = []
+        for c in range(n_cams):
+            d0, d1 = res[(k0, c)], res[(k1, c)]
+            ps = per_step[c]
+            views.append((DeviceView(slots[k0 % 2][c]["color"], slots[k0 % 2][c]["z"], ps["mf"], *ps["sf"], d0["vp"], d0["ivp"]),
+                          DeviceView(slots[k1 % 2][c]["color"], slots[k1 % 2][c]["z"], ps["mb"], *ps["sb"], d1["vp"], d1["ivp"])))
+        fr = DeviceFrame(views[0][0], views[0][1], [v[0] for v in views[1:]], [v[1] for v in views[1:]], [3] * (n_cams - 1))
+        for i, ci in enumerate(clients[p]):
+            r.render(out, ci, fr, stream)
+            outs_host[i].copy_(out, non_blocking=True)
+            if count:
+                d2h += out.numel()
+
+    for s in range(args.warmup):
+        step(s, False)
+    torch.cuda.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for s in range(args.warmup, args.warmup + args.steps):
+        step(s, True)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1)
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = world * args.steps * len(TS) * W * H / 1e6 / (ms / 1e3)
+    return {"value": round(value, 2), "unit": "Mpix/s", "h2d_bytes_per_step": h2d // args.steps,
+            "d2h_bytes_per_step": d2h // args.steps, "ms_per_step": round(ms / args.steps, 4)}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return main_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

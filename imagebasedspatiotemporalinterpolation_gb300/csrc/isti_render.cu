@@ -20,6 +20,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 namespace isti
 {
@@ -425,6 +426,11 @@ struct isti_renderer
     size_t arena_bytes = 0;
     isti::FrameParams last{};
     bool has_frame = false;
+    // stage timing: 4 events per timed render (before init, after init, after splat, after reproj)
+    bool timing = false;
+    std::vector<cudaEvent_t> events;
+    size_t events_used = 0;
+    int32_t timed_launches = 0;
 };
 
 namespace
@@ -528,6 +534,8 @@ isti_status isti_renderer_destroy(isti_renderer *r)
     if (!r)
         return ISTI_OK;
     isti_status s = ISTI_OK;
+    for (cudaEvent_t ev : r->events)
+        cudaEventDestroy(ev);
     if (r->arena)
     {
         cudaError_t e = cudaFree(r->arena);
@@ -656,12 +664,33 @@ isti_status isti_render(isti_renderer *r, void *out_rgba, const isti_render_info
     p.linear = info->mode == ISTI_MODE_BACKWARD_BIDIRECTIONAL ? 1 : 0;
 
     cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
+    cudaEvent_t *ev = nullptr;
+    if (r->timing)
+    {
+        if (r->events_used + 4 > r->events.size())
+            for (int i = 0; i < 4; i++)
+            {
+                cudaEvent_t x;
+                e = cudaEventCreate(&x);
+                if (e != cudaSuccess)
+                    return cuda_fail(e, "cudaEventCreate");
+                r->events.push_back(x);
+            }
+        ev = &r->events[r->events_used];
+        r->events_used += 4;
+        r->timed_launches += 2;
+        cudaEventRecord(ev[0], stream);
+    }
     e = cudaMemsetAsync(base, 0xfe, key_bytes, stream);
     if (e != cudaSuccess)
         return cuda_fail(e, "cudaMemsetAsync");
+    if (ev)
+        cudaEventRecord(ev[1], stream);
     const dim3 blk(32, 8);
     const dim3 gs((max_w + 31) / 32, (max_h + 7) / 8, n_views);
     isti::splat_kernel<<<gs, blk, 0, stream>>>(p);
+    if (ev)
+        cudaEventRecord(ev[2], stream);
     const dim3 gr((info->width + 31) / 32, (info->height + 7) / 8);
     switch (info->mode)
     {
@@ -676,10 +705,45 @@ isti_status isti_render(isti_renderer *r, void *out_rgba, const isti_render_info
         isti::reproj_kernel<3, 5, true><<<gr, blk, 0, stream>>>(p);
         break;
     }
+    if (ev)
+        cudaEventRecord(ev[3], stream);
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return cuda_fail(e, "kernel launch");
     r->has_frame = true;
+    return ISTI_OK;
+}
+
+isti_status isti_renderer_enable_timing(isti_renderer *r, int32_t on)
+{
+    if (!r)
+        return fail(ISTI_ERR_INVALID_ARG, "renderer is NULL");
+    r->timing = on != 0;
+    return ISTI_OK;
+}
+
+isti_status isti_renderer_timing(isti_renderer *r, isti_timing *out)
+{
+    if (!r || !out)
+        return fail(ISTI_ERR_INVALID_ARG, "NULL argument");
+    std::memset(out, 0, sizeof *out);
+    for (size_t i = 0; i + 4 <= r->events_used; i += 4)
+    {
+        cudaError_t e = cudaEventSynchronize(r->events[i + 3]);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaEventSynchronize");
+        float a = 0.f, b = 0.f, c = 0.f;
+        cudaEventElapsedTime(&a, r->events[i], r->events[i + 1]);
+        cudaEventElapsedTime(&b, r->events[i + 1], r->events[i + 2]);
+        cudaEventElapsedTime(&c, r->events[i + 2], r->events[i + 3]);
+        out->init_ms += a;
+        out->splat_ms += b;
+        out->reproj_ms += c;
+        out->frames += 1;
+    }
+    out->kernel_launches = r->timed_launches;
+    r->events_used = 0;
+    r->timed_launches = 0;
     return ISTI_OK;
 }
 

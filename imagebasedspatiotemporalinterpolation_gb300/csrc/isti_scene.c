@@ -124,6 +124,7 @@ static double light_visibility(const isti_scene_desc *sc, d3 p, int self, double
 {
     const d3 L = v3(sc->light_dir[0], sc->light_dir[1], sc->light_dir[2]);
     const double theta = sc->light_radius_deg * (3.14159265358979323846 / 180.0);
+    const double sin_theta = sin(theta);
     double vis = 1.0;
     for (int i = 0; i < sc->n_spheres; i++)
     {
@@ -131,8 +132,17 @@ static double light_visibility(const isti_scene_desc *sc, d3 p, int self, double
             continue;
         const isti_sphere *s = &sc->spheres[i];
         const d3 dc = sub(sphere_centre(s, t), p);
-        const double dist = sqrt(dot(dc, dc));
-        if (dist <= s->r || dot(dc, L) <= 0.0)
+        const double proj = dot(dc, L);
+        if (proj <= 0.0)
+            continue;
+        const double d2 = dot(dc, dc);
+        /* sin(angle to L) > r/dist + sin(theta) implies the discs are apart */
+        const double perp2 = d2 - proj * proj;
+        const double reach = s->r + sqrt(d2) * sin_theta;
+        if (perp2 > reach * reach)
+            continue;
+        const double dist = sqrt(d2);
+        if (dist <= s->r)
             continue;
         const double beta = asin(s->r / dist);
         double ca = dot(dc, L) / dist;

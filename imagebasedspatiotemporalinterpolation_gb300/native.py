@@ -59,6 +59,11 @@ class IstiRenderInfo(C.Structure):
     ]
 
 
+class IstiTiming(C.Structure):
+    _fields_ = [("frames", C.c_int32), ("kernel_launches", C.c_int32), ("init_ms", C.c_float),
+                ("splat_ms", C.c_float), ("reproj_ms", C.c_float)]
+
+
 # Every function include/isti.h declares: name -> (restype, argtypes)
 SIGNATURES = {
     "isti_abi_version": (C.c_int32, []),
@@ -69,6 +74,8 @@ SIGNATURES = {
     "isti_render": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(IstiRenderInfo), C.POINTER(IstiFrameData), C.c_void_p]),
     "isti_renderer_view_buffers": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
                                              C.POINTER(C.c_void_p), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "isti_renderer_enable_timing": (C.c_int, [C.c_void_p, C.c_int32]),
+    "isti_renderer_timing": (C.c_int, [C.c_void_p, C.POINTER(IstiTiming)]),
 }
 
 

@@ -1,0 +1,198 @@
+"""Python mirror of the reference's renderer interface over the C ABI.
+
+  DeviceView   <- MotionZBufferImage (include/data.h:12-62), device-resident
+  DeviceFrame  <- FrameData (include/data.h:79-116), incl. swap()
+  Renderer     <- Renderer::render(ImageBuffer<uchar4,4>&, RenderInfo, FrameData&)
+                  (include/renderer.h:52-56)
+
+Device memory and streams come from PyTorch (plumbing only); every pixel is
+computed by libisti.so.  There is no CPU fallback: a missing library or a
+non-CUDA tensor raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import native
+from .native import IstiFrameData, IstiRenderInfo, IstiView, check, mat16
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _dptr(t) -> int | None:
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("isti buffers must be CUDA tensors")
+    if not t.is_contiguous():
+        raise ValueError("isti buffers must be contiguous")
+    return t.data_ptr()
+
+
+@dataclass
+class DeviceView:
+    """One camera at one keyframe in device memory."""
+    color: object                     # (H, W, 4) uint8
+    z: object                         # (H, W) float32
+    motion: object | None             # (H, W, 3) float16 or (H, W, 4) float32
+    shadow_a: object | None = None
+    shadow_b: object | None = None
+    shadow_info: object | None = None
+    viewproj: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32))
+    inv_viewproj: np.ndarray = field(default_factory=lambda: np.eye(4, dtype=np.float32))
+
+    @property
+    def width(self) -> int:
+        return int(self.z.shape[1])
+
+    @property
+    def height(self) -> int:
+        return int(self.z.shape[0])
+
+    @staticmethod
+    def from_host(v, device="cuda", motion_format: str = "f16x3", non_blocking: bool = False) -> "DeviceView":
+        torch = _torch()
+
+        def up(a, dtype=None):
+            if a is None:
+                return None
+            t = torch.from_numpy(np.ascontiguousarray(a if dtype is None else a.astype(dtype)))
+            return t.to(device, non_blocking=non_blocking)
+
+        if v.motion is None:
+            mot = None
+        elif motion_format == "f16x3":
+            mot = up(v.motion, np.float16)
+        elif motion_format == "f32x4":
+            mot = up(v.motion_f32x4())
+        else:
+            raise ValueError(f"unknown motion format {motion_format}")
+        return DeviceView(up(v.color), up(v.z, np.float32), mot, up(v.shadow_a), up(v.shadow_b), up(v.shadow_info),
+                          np.asarray(v.viewproj, np.float32), np.asarray(v.inv_viewproj, np.float32))
+
+    def to_c(self) -> IstiView:
+        if self.motion is None:
+            fmt = native.MOTION_NONE
+        elif self.motion.shape[-1] == 3:
+            fmt = native.MOTION_F16X3
+        else:
+            fmt = native.MOTION_F32X4
+        return IstiView(self.width, self.height, _dptr(self.color), _dptr(self.z), _dptr(self.motion), fmt,
+                        _dptr(self.shadow_a), _dptr(self.shadow_b), _dptr(self.shadow_info),
+                        mat16(self.viewproj), mat16(self.inv_viewproj))
+
+
+@dataclass
+class DeviceFrame:
+    """FrameData in device memory: fwd/bwd main keyframes plus aux cameras."""
+    fwd: DeviceView
+    bwd: DeviceView
+    aux_curr: list = field(default_factory=list)
+    aux_next: list = field(default_factory=list)
+    aux_priority: list = field(default_factory=list)
+    _c: object = None
+
+    @staticmethod
+    def from_host(frame, device="cuda", motion_format: str = "f16x3", non_blocking: bool = False) -> "DeviceFrame":
+        up = lambda v: DeviceView.from_host(v, device, motion_format, non_blocking)
+        return DeviceFrame(up(frame.fwd), up(frame.bwd), [up(v) for v in frame.aux_curr], [up(v) for v in frame.aux_next],
+                           list(frame.aux_priority))
+
+    def swap(self) -> None:
+        """FrameData::swap (include/data.h:110-115): the later keyframe becomes the earlier one."""
+        self.fwd, self.bwd = self.bwd, self.fwd
+        self.aux_curr, self.aux_next = self.aux_next, self.aux_curr
+        self._c = None
+
+    def views(self) -> list:
+        out = [self.fwd, self.bwd]
+        for a, b in zip(self.aux_curr, self.aux_next):
+            out += [a, b]
+        return out
+
+    def to_c(self):
+        """Marshalled isti_frame_data (cached until swap())."""
+        if self._c is None:
+            n = len(self.aux_curr)
+            curr = (IstiView * max(1, n))(*[v.to_c() for v in self.aux_curr])
+            nxt = (IstiView * max(1, n))(*[v.to_c() for v in self.aux_next])
+            prio = (C.c_int32 * max(1, n))(*(self.aux_priority or [0] * n))
+            fd = IstiFrameData(self.fwd.to_c(), self.bwd.to_c(), n, C.cast(curr, C.POINTER(IstiView)),
+                               C.cast(nxt, C.POINTER(IstiView)), C.cast(prio, C.POINTER(C.c_int32)))
+            self._c = (fd, curr, nxt, prio)
+        return self._c[0]
+
+
+def render_info(client) -> IstiRenderInfo:
+    """RenderInfo from a scene.Client-like object."""
+    return IstiRenderInfo(int(client.width), int(client.height), float(client.alpha), mat16(client.viewproj),
+                          mat16(client.inv_viewproj), int(client.frames_per_anchor),
+                          int(client.shadow_frames_per_anchor), int(bool(client.no_shadows)), int(client.mode))
+
+
+class _CudaArray:
+    """__cuda_array_interface__ view of a raw device pointer (read back only)."""
+
+    def __init__(self, ptr: int, shape: tuple, typestr: str):
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr, "data": (ptr, True), "version": 3,
+                                         "strides": None}
+
+
+class Renderer:
+    """Reference Renderer (include/renderer.h:52-93) on libisti.so."""
+
+    def __init__(self):
+        self._lib = native.load()
+        h = C.c_void_p()
+        check(self._lib.isti_renderer_create(C.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            check(self._lib.isti_renderer_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render(self, render_buffer, info, frame_data: DeviceFrame, stream=None) -> None:
+        """Render one interpolated client frame into render_buffer ((H, W, 4)
+        uint8 CUDA tensor).  Pixels without a valid result keep their content."""
+        torch = _torch()
+        ri = info if isinstance(info, IstiRenderInfo) else render_info(info)
+        if tuple(render_buffer.shape) != (ri.height, ri.width, 4) or render_buffer.dtype != torch.uint8:
+            raise ValueError("render_buffer must be a (H, W, 4) uint8 tensor of the render resolution")
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        check(self._lib.isti_render(self._h, _dptr(render_buffer), C.byref(ri), C.byref(frame_data.to_c()), C.c_void_p(s)))
+
+    def enable_timing(self, on: bool = True) -> None:
+        check(self._lib.isti_renderer_enable_timing(self._h, int(on)))
+
+    def timing(self) -> dict:
+        """Summed per-stage device time of the renders since the last call (waits for them)."""
+        t = native.IstiTiming()
+        check(self._lib.isti_renderer_timing(self._h, C.byref(t)))
+        return {"frames": t.frames, "kernel_launches": t.kernel_launches, "init_ms": t.init_ms,
+                "splat_ms": t.splat_ms, "reproj_ms": t.reproj_ms}
+
+    def view_buffers(self, view: int):
+        """(splat keys as int64 bit patterns (H, W), cam_ff f32 (H, W, 4), full_ff f32 (H, W, 4)) of the
+        last render, as copies."""
+        torch = _torch()
+        sp, cf, ff = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        w, h = C.c_uint32(), C.c_uint32()
+        check(self._lib.isti_renderer_view_buffers(self._h, view, C.byref(sp), C.byref(cf), C.byref(ff), C.byref(w), C.byref(h)))
+        H, W = h.value, w.value
+        out = []
+        for ptr, shape, ts in ((sp, (H, W), "<i8"), (cf, (H, W, 4), "<f4"), (ff, (H, W, 4), "<f4")):
+            out.append(None if not ptr.value else torch.as_tensor(_CudaArray(ptr.value, shape, ts), device="cuda").clone())
+        return tuple(out)

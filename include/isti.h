@@ -143,6 +143,22 @@ isti_status isti_render(isti_renderer *r, void *out_rgba, const isti_render_info
 isti_status isti_renderer_view_buffers(const isti_renderer *r, int32_t view, const uint64_t **splat, const float **cam_ff,
                                        const float **full_ff, uint32_t *width, uint32_t *height);
 
+/* Per-stage device time (no counterpart in the reference, which has no
+ * timers): when enabled, each render records CUDA events around the key
+ * initialisation, the splat launch and the reprojection launch on its stream. */
+typedef struct isti_timing
+{
+    int32_t frames;          /* renders timed since the previous query */
+    int32_t kernel_launches; /* launches of this library's kernels in those renders */
+    float init_ms;           /* summed device time of the splat-key initialisation */
+    float splat_ms;          /* summed device time of the splat kernel */
+    float reproj_ms;         /* summed device time of the reprojection kernel */
+} isti_timing;
+
+isti_status isti_renderer_enable_timing(isti_renderer *r, int32_t on);
+/* Waits for the recorded events, returns the sums and resets them. */
+isti_status isti_renderer_timing(isti_renderer *r, isti_timing *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -146,6 +146,22 @@ def run_oracle(frame, client, prev_out=None, nthreads: int = 0, with_intermediat
     return out, splats, cam, full
 
 
+def prepared_call(frame, client, prev_out=None, nthreads: int = 0):
+    """Marshals once and returns a zero-argument callable that runs only the C
+    oracle on these inputs (for timing the CPU baseline)."""
+    lib = _load(ORACLE_LIB, "oracle_render")
+    m = _Marshal(frame, client)
+    out = np.zeros((client.height, client.width, 4), np.uint8) if prev_out is None else np.array(prev_out, np.uint8, copy=True)
+
+    def call():
+        if lib.oracle_render(C.byref(m.frame), C.byref(m.info), C.c_void_p(out.ctypes.data), None, C.c_int(nthreads)) != 0:
+            raise ValueError("oracle_render rejected its arguments")
+        return out
+
+    call.keep = (m, out)
+    return call
+
+
 def run_reference(frame, client, prev_out=None):
     """The reference's own renderer.cu, executed on the CPU (oracle/_ref)."""
     lib = _load(REF_LIB, "isti_ref_render")

@@ -581,6 +581,10 @@ int oracle_render(const oracle_frame *frame, const oracle_render_info *s, uint8_
 {
     if (!frame || !s || !out_rgba || s->mode < 0 || s->mode > 3)
         return -1;
+    /* shadow levels sit at bits 2i of a 32-bit field: more than 16 sub-frames
+     * would shift past its width (undefined in the reference) */
+    if (s->shadow_frames_per_anchor < 0 || s->shadow_frames_per_anchor > 16)
+        return -1;
     if (!view_ok(&frame->fwd) || !view_ok(&frame->bwd) || frame->num_aux < 0)
         return -1;
     const u2 res = {s->width, s->height};
