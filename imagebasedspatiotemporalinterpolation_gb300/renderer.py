@@ -140,7 +140,7 @@ class _CudaArray:
     """__cuda_array_interface__ view of a raw device pointer (read back only)."""
 
     def __init__(self, ptr: int, shape: tuple, typestr: str):
-        self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr, "data": (ptr, True), "version": 3,
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr, "data": (ptr, False), "version": 3,
                                          "strides": None}
 
 
