@@ -18,6 +18,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -769,3 +770,173 @@ isti_status isti_renderer_view_buffers(const isti_renderer *r, int32_t view, con
 }
 
 } // extern "C"
+
+// ============================ rendering without allocation ============================
+//
+// isti_render_noalloc serves callers that may not allocate device memory while
+// they run (a host whose device budget is reserved up front by its own pool, a
+// real-time loop where cudaMalloc/cudaFree can synchronise the device).  Its
+// splat keys and flow fields live in g_noalloc_scratch below instead of a
+// renderer arena; the kernels are the ones isti_render launches.
+
+namespace
+{
+// Fixed scratch for isti_render_noalloc: ISTI_NOALLOC_SCRATCH_BYTES (64 MiB), loaded
+// with the module on every GPU that uses the library and kept until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[ISTI_NOALLOC_SCRATCH_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of g_noalloc_scratch on the current device.  In host code the
+// array's name only denotes a host-side shadow, so the address is looked up once
+// per device (with that device current) and cached.
+isti_status noalloc_scratch(int device, char **out)
+{
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES)
+        return fail(ISTI_ERR_UNSUPPORTED, "device ordinal beyond the no-allocation scratch table");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device])
+    {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_ptr[device] = p;
+    }
+    *out = static_cast<char *>(g_noalloc_ptr[device]);
+    return ISTI_OK;
+}
+} // namespace
+
+extern "C" isti_status isti_render_noalloc(void *out_rgba, const isti_render_info *info, const isti_frame_data *frame, void *stream_ptr)
+{
+    if (!out_rgba || !info || !frame)
+        return fail(ISTI_ERR_INVALID_ARG, "NULL argument");
+    if (reinterpret_cast<uintptr_t>(out_rgba) & 3u)
+        return fail(ISTI_ERR_INVALID_ARG, "out_rgba must be 4-byte aligned");
+    if (info->mode == ISTI_MODE_TIMEWARP)
+        return fail(ISTI_ERR_UNSUPPORTED, "timewarp mode is not implemented");
+    if (info->mode < 0 || info->mode > ISTI_MODE_TIMEWARP)
+        return fail(ISTI_ERR_INVALID_ARG, "unknown render mode");
+    if (info->shadow_frames_per_anchor < 0 || info->shadow_frames_per_anchor > 16)
+        return fail(ISTI_ERR_INVALID_ARG, "shadow_frames_per_anchor must be 0..16");
+    std::string why;
+    if (!view_ok(frame->fwd, why) || !view_ok(frame->bwd, why))
+        return fail(ISTI_ERR_INVALID_ARG, why);
+    if (frame->fwd.width != info->width || frame->fwd.height != info->height || frame->bwd.width != info->width ||
+        frame->bwd.height != info->height)
+        return fail(ISTI_ERR_INVALID_ARG, "render resolution must equal the main keyframes' resolution");
+    const int n_aux = frame->num_aux;
+    if (n_aux < 0 || n_aux > ISTI_MAX_AUX_CAMS)
+        return fail(ISTI_ERR_INVALID_ARG, "num_aux out of range");
+    if (n_aux > 0 && (!frame->aux_curr || !frame->aux_next))
+        return fail(ISTI_ERR_INVALID_ARG, "aux views are NULL");
+    for (int i = 0; i < n_aux; i++)
+    {
+        const isti_view &a = frame->aux_curr[i], &b = frame->aux_next[i];
+        if (!view_ok(a, why) || !view_ok(b, why))
+            return fail(ISTI_ERR_INVALID_ARG, why);
+        if (a.width != b.width || a.height != b.height)
+            return fail(ISTI_ERR_INVALID_ARG, "aux curr/next sizes differ");
+        if (a.width > info->width || a.height > info->height || (info->width - 1) / (info->width / a.width) >= a.width ||
+            (info->height - 1) / (info->height / a.height) >= a.height)
+            return fail(ISTI_ERR_INVALID_ARG, "aux resolution incompatible with the render resolution");
+    }
+
+    const int n_views = 2 + 2 * n_aux;
+    const isti_view *views[isti::MAX_VIEWS];
+    views[0] = &frame->fwd;
+    views[1] = &frame->bwd;
+    for (int i = 0; i < n_aux; i++)
+    {
+        views[2 + 2 * i] = &frame->aux_curr[i];
+        views[3 + 2 * i] = &frame->aux_next[i];
+    }
+    size_t key_bytes = 0, ff_bytes = 0, px[isti::MAX_VIEWS];
+    for (int k = 0; k < n_views; k++)
+    {
+        px[k] = (size_t)views[k]->width * views[k]->height;
+        key_bytes += align_up(px[k] * 8, 256);
+        ff_bytes += align_up(px[k] * 16, 256);
+    }
+    const size_t need = key_bytes + 2 * ff_bytes;
+    if (need > ISTI_NOALLOC_SCRATCH_BYTES)
+        return fail(ISTI_ERR_INVALID_ARG, "frame needs " + std::to_string(need) + " bytes of scratch; isti_render_noalloc holds at most " +
+                                              std::to_string((size_t)ISTI_NOALLOC_SCRATCH_BYTES) + " (use isti_render for larger frames)");
+
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaGetDevice");
+    char *base = nullptr;
+    isti_status st = noalloc_scratch(device, &base);
+    if (st != ISTI_OK)
+        return st;
+
+    isti::FrameParams p;
+    std::memset(&p, 0, sizeof p);
+    size_t off_key = 0, off_cam = key_bytes, off_full = key_bytes + ff_bytes;
+    const float alpha = info->alpha;
+    const float one_minus_alpha = 1.0f - alpha;
+    uint32_t max_w = 0, max_h = 0;
+    for (int k = 0; k < n_views; k++)
+    {
+        const bool fw = (k % 2) == 0;
+        const isti_view &v = *views[k];
+        const float *vp_to = (k < 2) ? (fw ? frame->bwd.viewproj : frame->fwd.viewproj)
+                                     : (fw ? frame->aux_next[(k - 2) / 2].viewproj : frame->aux_curr[(k - 2) / 2].viewproj);
+        const float *vp_main = fw ? frame->fwd.viewproj : frame->bwd.viewproj;
+        const int prio = (k < 2 || !frame->aux_priority) ? 0 : frame->aux_priority[(k - 2) / 2];
+        fill_view(p.v[k], v, fw ? 1 : 0, prio, fw ? alpha : one_minus_alpha, vp_to, vp_main);
+        p.v[k].splat = reinterpret_cast<unsigned long long *>(base + off_key);
+        p.v[k].cam_ff = reinterpret_cast<float4 *>(base + off_cam);
+        p.v[k].full_ff = reinterpret_cast<float4 *>(base + off_full);
+        off_key += align_up(px[k] * 8, 256);
+        off_cam += align_up(px[k] * 16, 256);
+        off_full += align_up(px[k] * 16, 256);
+        max_w = v.width > max_w ? v.width : max_w;
+        max_h = v.height > max_h ? v.height : max_h;
+    }
+    std::memcpy(p.cam_vp, info->viewproj, sizeof p.cam_vp);
+    p.out = static_cast<uint32_t *>(out_rgba);
+    p.out_w = info->width;
+    p.out_h = info->height;
+    p.alpha = alpha;
+    p.n_views = n_views;
+    p.n_aux = n_aux;
+    p.fpa = info->frames_per_anchor;
+    p.sfpa = info->shadow_frames_per_anchor;
+    p.no_shadows = info->no_shadows ? 1 : 0;
+    p.linear = info->mode == ISTI_MODE_BACKWARD_BIDIRECTIONAL ? 1 : 0;
+
+    // The array keeps the previous call's contents: every key starts as the
+    // reference's empty value (all bytes 0xfe); the flow fields are fully
+    // rewritten by the splat kernel before the reprojection reads them.
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
+    e = cudaMemsetAsync(base, 0xfe, key_bytes, stream);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaMemsetAsync");
+    const dim3 blk(32, 8);
+    const dim3 gs((max_w + 31) / 32, (max_h + 7) / 8, n_views);
+    isti::splat_kernel<<<gs, blk, 0, stream>>>(p);
+    const dim3 gr((info->width + 31) / 32, (info->height + 7) / 8);
+    switch (info->mode)
+    {
+    case ISTI_MODE_OURS:
+    case ISTI_MODE_BACKWARD_UNIDIRECTIONAL:
+        isti::reproj_kernel<1, 3, false><<<gr, blk, 0, stream>>>(p);
+        break;
+    case ISTI_MODE_SPLATTING:
+        isti::reproj_kernel<1, 0, false><<<gr, blk, 0, stream>>>(p);
+        break;
+    case ISTI_MODE_BACKWARD_BIDIRECTIONAL:
+        isti::reproj_kernel<3, 5, true><<<gr, blk, 0, stream>>>(p);
+        break;
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return cuda_fail(e, "kernel launch");
+    return ISTI_OK;
+}

@@ -76,7 +76,10 @@ SIGNATURES = {
                                              C.POINTER(C.c_void_p), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "isti_renderer_enable_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "isti_renderer_timing": (C.c_int, [C.c_void_p, C.POINTER(IstiTiming)]),
+    "isti_render_noalloc": (C.c_int, [C.c_void_p, C.POINTER(IstiRenderInfo), C.POINTER(IstiFrameData), C.c_void_p]),
 }
+
+NOALLOC_SCRATCH_BYTES = 64 << 20  # ISTI_NOALLOC_SCRATCH_BYTES
 
 
 class IstiError(RuntimeError):

@@ -196,3 +196,23 @@ class Renderer:
         for ptr, shape, ts in ((sp, (H, W), "<i8"), (cf, (H, W, 4), "<f4"), (ff, (H, W, 4), "<f4")):
             out.append(None if not ptr.value else torch.as_tensor(_CudaArray(ptr.value, shape, ts), device="cuda").clone())
         return tuple(out)
+
+
+def render_noalloc(render_buffer, info, frame_data: DeviceFrame, stream=None) -> None:
+    """isti_render_noalloc: render one frame without any device allocation.
+
+    For callers that cannot allocate device memory while they run (their
+    device budget is reserved up front by their own pool, or cudaMalloc's
+    possible device synchronisation would break a per-frame deadline).  The
+    scratch is a fixed 64 MiB array inside libisti.so, so frames are limited to
+    sum(width * height * 40 bytes) over the source views (640x360 with two aux
+    cameras fits).  The first call on a device looks up that array's address:
+    make it before any stream capture.  All calls share the array; do not let
+    calls overlap on the GPU."""
+    torch = _torch()
+    lib = native.load()
+    ri = info if isinstance(info, IstiRenderInfo) else render_info(info)
+    if tuple(render_buffer.shape) != (ri.height, ri.width, 4) or render_buffer.dtype != torch.uint8:
+        raise ValueError("render_buffer must be a (H, W, 4) uint8 tensor of the render resolution")
+    s = (stream or torch.cuda.current_stream()).cuda_stream
+    check(lib.isti_render_noalloc(_dptr(render_buffer), C.byref(ri), C.byref(frame_data.to_c()), C.c_void_p(s)))

@@ -159,6 +159,30 @@ isti_status isti_renderer_enable_timing(isti_renderer *r, int32_t on);
 /* Waits for the recorded events, returns the sums and resets them. */
 isti_status isti_renderer_timing(isti_renderer *r, isti_timing *out);
 
+/* Render without allocating (no counterpart in the reference, whose Renderer
+ * always allocates its own buffers).
+ *
+ * For callers that must not allocate device memory while they run: hosts
+ * whose device-memory budget is fully reserved up front by their own pool,
+ * and real-time loops (a compositor or serving thread with a per-frame
+ * deadline) where cudaMalloc/cudaFree may synchronise the device and take
+ * unbounded time.  Same inputs, output and semantics as isti_render, but no
+ * renderer handle: the splat keys and flow fields live in one fixed device
+ * array inside this library (ISTI_NOALLOC_SCRATCH_BYTES, held by every GPU
+ * that loads the library until the process exits).
+ *
+ *  - Limit: the sum over source views of width*height*40 bytes (each buffer
+ *    rounded up to 256 bytes) must fit in ISTI_NOALLOC_SCRATCH_BYTES, e.g.
+ *    640x360 with up to two aux cameras; larger frames are rejected with
+ *    ISTI_ERR_INVALID_ARG.
+ *  - The first call on a device looks up the array's device address; make
+ *    that first call before any stream capture.
+ *  - Every call uses the same array and re-initialises the keys itself; calls
+ *    whose work overlaps on the GPU (other streams, other threads) race on it,
+ *    so serialise them. */
+#define ISTI_NOALLOC_SCRATCH_BYTES (64u << 20)
+isti_status isti_render_noalloc(void *out_rgba, const isti_render_info *info, const isti_frame_data *frame, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
