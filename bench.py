@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-per-frame", action="store_true", help="skip the single-frame-call comparison")
     return ap.parse_args()
 
 
@@ -252,18 +253,18 @@ def main_ours(args):
     r = Renderer()
     stream = torch.cuda.current_stream(dev)
 
+    outs = [torch.zeros((H, W, 4), dtype=torch.uint8, device=dev) for _ in TS]
+
     def step(s):
         p = s % P
-        for ci in clients[p]:
-            r.render(out, ci, frames[p], stream)
+        r.render_batch(outs, clients[p], frames[p], chain=True, stream=stream)
 
     for s in range(args.warmup):
         step(s)
     torch.cuda.synchronize()
 
-    # ---- timed region (device-resident inputs)
-    n_frames = args.steps * len(TS)
-    fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n_frames)]
+    # ---- timed region (device-resident inputs): one batched call per keyframe interval
+    sev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(local)
     r.timing()          # discard warm-up
@@ -273,14 +274,10 @@ def main_ours(args):
     torch.cuda.synchronize()
     clocks.start()
     t0.record(stream)
-    fi = 0
     for s in range(args.steps):
-        p = s % P
-        for ci in clients[p]:
-            fev[fi][0].record(stream)
-            r.render(out, ci, frames[p], stream)
-            fev[fi][1].record(stream)
-            fi += 1
+        sev[s][0].record(stream)
+        step(s)
+        sev[s][1].record(stream)
     t1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -292,20 +289,45 @@ def main_ours(args):
         tt = torch.tensor([ms], device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         ms = float(tt.item())
-    frame_ms = sorted(a.elapsed_time(b) for a, b in fev)
-    total_mpix = world * n_frames * W * H / 1e6
-    value = total_mpix / (ms / 1e3)
+    step_ms = sorted(a.elapsed_time(b) for a, b in sev)
+    n_frames = args.steps * len(TS)
+    value = world * n_frames * W * H / 1e6 / (ms / 1e3)
+
+    # ---- the same frames through the single-frame call (isti_render), for comparison
+    per_frame = None
+    if not args.no_per_frame:
+        fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n_frames)]
+        torch.cuda.synchronize()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        fi = 0
+        for s in range(args.steps):
+            p = s % P
+            for ci in clients[p]:
+                fev[fi][0].record(stream)
+                r.render(out, ci, frames[p], stream)
+                fev[fi][1].record(stream)
+                fi += 1
+        a1.record(stream)
+        torch.cuda.synchronize()
+        frame_ms = sorted(a.elapsed_time(b) for a, b in fev)
+        per_frame = {"value": round(n_frames * W * H / 1e6 / (a0.elapsed_time(a1) / 1e3), 2), "unit": "Mpix/s",
+                     "p50_frame_ms": round(frame_ms[len(frame_ms) // 2], 4),
+                     "p99_frame_ms": round(frame_ms[min(len(frame_ms) - 1, int(0.99 * len(frame_ms)))], 4)}
 
     # ---- e2e: host buffers through the C ABI, uploads + read-back inside the timed region
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(args, seq, res, clients, r, dev, world)
 
-    # ---- roofline of the dominant kernel
+    # ---- roofline of the dominant kernel.  Algorithmic bytes of one batched call: every
+    # input byte of the 6 source views once (z + f16 motion for the splat launch; colour +
+    # shadow A/B/Info for the reprojection launch) and the 3 output frames once.
     px = W * H
     n_views = 2 * n_cams
-    alg = {"splat_kernel": n_views * (4 + 6) * px, "reproj_kernel": (n_views * (4 + 12) + 4) * px}
-    per_launch_ms = {"splat_kernel": tim["splat_ms"] / max(1, tim["frames"]), "reproj_kernel": tim["reproj_ms"] / max(1, tim["frames"])}
+    calls = max(1, tim["kernel_launches"] // 2)
+    alg = {"splat_kernel": n_views * (4 + 6) * px, "reproj_kernel": n_views * (4 + 12) * px + len(TS) * 4 * px}
+    per_launch_ms = {"splat_kernel": tim["splat_ms"] / calls, "reproj_kernel": tim["reproj_ms"] / calls}
     dom = max(per_launch_ms, key=per_launch_ms.get)
     peak, peak_kind = peaks()
     achieved = alg[dom] / (per_launch_ms[dom] / 1e3) / 1e9
@@ -331,11 +353,12 @@ def main_ours(args):
             "config": {"workload": WORKLOAD, "width": W, "height": H, "source_views": n_views, "frames_per_step": len(TS),
                        "resident_pairs": P, "mode": 0, "l2": "inputs larger than L2 (~0.8 GB touched per frame)",
                        "parallelism": f"replicas x{world}"},
-            "p50_frame_ms": round(frame_ms[len(frame_ms) // 2], 4),
-            "p99_frame_ms": round(frame_ms[min(len(frame_ms) - 1, int(0.99 * len(frame_ms)))], 4),
-            "kernels_ms_per_frame": {"key_init": round(tim["init_ms"] / max(1, tim["frames"]), 4),
-                                     "splat_kernel": round(per_launch_ms["splat_kernel"], 4),
-                                     "reproj_kernel": round(per_launch_ms["reproj_kernel"], 4)},
+            "p50_step_ms": round(step_ms[len(step_ms) // 2], 4),
+            "p99_step_ms": round(step_ms[min(len(step_ms) - 1, int(0.99 * len(step_ms)))], 4),
+            "kernels_ms_per_call": {"key_init": round(tim["init_ms"] / calls, 4),
+                                    "splat_kernel": round(per_launch_ms["splat_kernel"], 4),
+                                    "reproj_kernel": round(per_launch_ms["reproj_kernel"], 4)},
+            "per_frame_api": per_frame,
             "gpu_launches": tim["kernel_launches"],
             "clocks": clk,
             "e2e": e2e,
@@ -375,7 +398,7 @@ def run_e2e(args, seq, res, clients, r, dev, world):
     per_step = [dict(mf=like(h0["mf"]), mb=like(h0["mb"]), sf=[like(a) for a in h0["sf"]], sb=[like(a) for a in h0["sb"]])
                 for _ in range(n_cams)]
     outs_host = [torch.empty((H, W, 4), dtype=torch.uint8).pin_memory() for _ in TS]
-    out = torch.zeros((H, W, 4), dtype=torch.uint8, device=dev)
+    outs_dev = [torch.zeros((H, W, 4), dtype=torch.uint8, device=dev) for _ in TS]
     stream = torch.cuda.current_stream(dev)
     h2d = d2h = 0
 
@@ -402,11 +425,11 @@ def run_e2e(args, seq, res, clients, r, dev, world):
             views.append((DeviceView(slots[k0 % 2][c]["color"], slots[k0 % 2][c]["z"], ps["mf"], *ps["sf"], d0["vp"], d0["ivp"]),
                           DeviceView(slots[k1 % 2][c]["color"], slots[k1 % 2][c]["z"], ps["mb"], *ps["sb"], d1["vp"], d1["ivp"])))
         fr = DeviceFrame(views[0][0], views[0][1], [v[0] for v in views[1:]], [v[1] for v in views[1:]], [3] * (n_cams - 1))
-        for i, ci in enumerate(clients[p]):
-            r.render(out, ci, fr, stream)
-            outs_host[i].copy_(out, non_blocking=True)
+        r.render_batch(outs_dev, clients[p], fr, chain=True, stream=stream)
+        for i, o in enumerate(outs_dev):
+            outs_host[i].copy_(o, non_blocking=True)
             if count:
-                d2h += out.numel()
+                d2h += o.numel()
 
     for s in range(args.warmup):
         step(s, False)

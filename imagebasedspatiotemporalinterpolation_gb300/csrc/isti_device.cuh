@@ -112,14 +112,42 @@ __device__ __forceinline__ uint32_t to_8bit(float f)
     return (uint32_t)min(255, max(0, v));
 }
 
+// to_8bit(v / 255) for v = a + t * (b - a).  The round trip RN(RN(v / 255) * 255)
+// stays within 256 * 2^-23 = 2^-15 of v for 0 <= v < 256 and returns every integer
+// 0..255 unchanged, so its truncation is floor(v) unless v lies within 2^-12 of an
+// integer without being one; only that case (and v outside [0, 256), NaN) takes
+// the division.
+__device__ __forceinline__ uint32_t to_8bit_255ths(float v)
+{
+    const float fl = floorf(v);
+    const float fr = __fsub_rn(v, fl);
+    if (v >= 0.0f && v < 256.0f && (fr == 0.0f || (fr > 0x1p-12f && fr < 1.0f - 0x1p-12f)))
+        return (uint32_t)fl;
+    return to_8bit(__fdiv_rn(v, 255.f));
+}
+
 // color_to_uchar4(lerp_color(a, b, t)), packed RGBA8 in a uint32 (R in bits 0-7)
 __device__ __forceinline__ uint32_t lerp_color_u8(uint32_t a, uint32_t b, float t)
 {
     uint32_t r = 0;
 #pragma unroll
     for (int c = 0; c < 4; c++)
-        r |= to_8bit(lerp_ch((a >> (8 * c)) & 255u, (b >> (8 * c)) & 255u, t)) << (8 * c);
+    {
+        const float fa = (float)((a >> (8 * c)) & 255u), fb = (float)((b >> (8 * c)) & 255u);
+        r |= to_8bit_255ths(__fadd_rn(fa, __fmul_rn(t, __fsub_rn(fb, fa)))) << (8 * c);
+    }
     return r;
+}
+
+// sqrtf(s) < e, IEEE-exact: the square root is only taken within 0.01 % of e^2
+__device__ __forceinline__ bool sqrt_less(float s, float e)
+{
+    const float e2 = e * e;
+    if (s < e2 * 0.9999f)
+        return true;
+    if (s > e2 * 1.0001f)
+        return false;
+    return __fsqrt_rn(s) < e;
 }
 
 // float -> unsigned char of make_uchar4(float, ...): truncation, saturation, NaN -> 0

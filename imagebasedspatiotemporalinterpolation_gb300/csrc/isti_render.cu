@@ -3,14 +3,32 @@
 //
 // Reference: src/renderer.cu (DerThomy/ImageBasedSpatioTemporalInterpolation).
 //
+// A launch pair renders a batch of 1..ISTI_MAX_BATCH_FRAMES client frames of
+// one keyframe pair (isti_render is a batch of one).
+//
 // Layout in HBM (renderer-owned arena, one allocation):
-//   [splat keys of every view, u64 per pixel][cam flow f32x4 per pixel, every view][full flow f32x4, every view]
-// The key block is contiguous so one memset initialises all views.
+//   [splat keys, u64/px: frame-major, every view][cam flow f32x4/px: frame-major, every view]
+//   [full flow f32x4/px, every view][pixel->clip tables, (w + h) f32 per view]
+// The key block is contiguous so one memset initialises all frames and views.
 // Pixel inputs are caller-owned device images (include/isti.h).
 //
-// Launches per frame: 1 memset + 1 splat launch (all 2 + 2 * n_aux source
-// views, blockIdx.z = view) + 1 reprojection launch (one thread per output
-// pixel).  Nothing blocks the host.
+// Launches per batch: 1 memset + 1 splat launch (blockIdx.z = source view;
+// one extra z-slice fills the pixel->clip tables) + 1 reprojection launch.
+// Nothing blocks the host.
+//
+// Splat: per source pixel, the keyframe part (world positions, flow to the
+// other keyframe, visibility in the main view) is computed once, then the
+// client-camera projection, flow store and 64-bit atomicMin per frame.
+//
+// Reprojection: a block covers 32 output pixels of one row with one warp per
+// source view (view = threadIdx.y) and loops over the frames.  Each warp runs
+// window initialisation + iterative search + reprojection error for its view
+// (one direction of one camera); then one warp chooses the direction per
+// camera, the winning camera, and computes the colour (second chance, soft
+// shadows) only for the result that is written.  The reference computes the
+// colour of every camera's result (src/renderer.cu:378-396,436); only the
+// written one is observable and colour never feeds a choice, so the output is
+// identical.
 #include "isti.h"
 #include "isti_device.cuh"
 
@@ -26,36 +44,47 @@
 namespace isti
 {
 constexpr int MAX_VIEWS = 2 + 2 * ISTI_MAX_AUX_CAMS;
+constexpr int MAX_FRAMES = ISTI_MAX_BATCH_FRAMES;
+constexpr float FLT_MAX_F = 3.402823466e+38f;
 
 struct DevView
 {
-    const uint32_t *color;  // RGBA8 packed, R in bits 0-7
+    const uint32_t *color; // RGBA8 packed, R in bits 0-7
     const float *z;
     const void *motion;
     const uint32_t *sha, *shb, *shi;
-    unsigned long long *splat;
-    float4 *cam_ff;
+    unsigned long long *splat; // frame 0; frame k at + k * FrameParams::key_stride
+    float4 *cam_ff;            // frame 0; frame k at + k * FrameParams::cam_stride
     float4 *full_ff;
+    float *lut;                // pixel2CS tables: x at [0, w), y at [w, w + h)
     uint32_t w, h;
+    uint32_t sx, sy;           // output pixels per view pixel (aux_idx = idx / s, src/renderer.cu:433)
     int32_t motion_fmt;
     int32_t forward;
     int32_t priority;
-    float weight;
-    float err_sx, err_sy;   // res / min(res.x, res.y), computeReprojError scale (src/renderer.cu:213)
-    float inv_vp[16];       // this view's inverse viewproj
-    float vp_to[16];        // the other keyframe's viewproj (same camera)
-    float vp_main[16];      // main camera viewproj at this keyframe (visible_in_main test)
+    float err_sx, err_sy;      // res / min(res.x, res.y), computeReprojError scale (src/renderer.cu:213)
+    float inv_vp[16];          // this view's inverse viewproj
+    float vp_to[16];           // the other keyframe's viewproj (same camera)
+    float vp_main[16];         // main camera viewproj at this keyframe (visible_in_main test)
+};
+
+// Per-frame settings (RenderInfo / AdditionalRenderInfo, include/renderer.h:18-35)
+struct FrameCfg
+{
+    float alpha;
+    int32_t fpa, sfpa, no_shadows;
 };
 
 struct FrameParams
 {
     DevView v[MAX_VIEWS];
-    float cam_vp[16];
-    uint32_t *out;
+    float cam_vp[MAX_FRAMES][16];
+    uint32_t *out[MAX_FRAMES];
+    FrameCfg f[MAX_FRAMES];
+    size_t key_stride; // elements between frames in the key block
+    size_t cam_stride; // elements between frames in the cam-flow block
     uint32_t out_w, out_h;
-    float alpha;
-    int32_t n_views, n_aux;
-    int32_t fpa, sfpa, no_shadows, linear;
+    int32_t n_views, n_aux, n_frames, linear, chain;
 };
 
 // ---- border-addressed loads: zero outside the image (cudaAddressModeBorder) ----
@@ -85,10 +114,32 @@ __device__ __forceinline__ float4 load_motion(const DevView &v, size_t idx)
     return make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
+// pixel2CS of pixel (x, y) of view v from its tables; direct formula outside the image
+__device__ __forceinline__ float2 view_pixel2cs(const DevView &v, uint32_t x, uint32_t y)
+{
+    if (x < v.w && y < v.h)
+        return make_float2(__ldg(v.lut + x), __ldg(v.lut + v.w + y));
+    return pixel2cs(x, y, v.w, v.h);
+}
+
 // ---- computeFlowFields_sortedSplatting_kernel, src/renderer.cu:76-146 ----
+// blockIdx.z < n_views: one source view; blockIdx.z == n_views: pixel->clip tables.
 
 __global__ void __launch_bounds__(256) splat_kernel(const __grid_constant__ FrameParams p)
 {
+    if ((int)blockIdx.z == p.n_views)
+    {
+        const uint32_t t = ((blockIdx.y * gridDim.x + blockIdx.x) * blockDim.y + threadIdx.y) * blockDim.x + threadIdx.x;
+        for (int k = 0; k < p.n_views; k++)
+        {
+            const DevView &v = p.v[k];
+            if (t < v.w)
+                v.lut[t] = pixel2cs(t, 0, v.w, 1).x;
+            if (t < v.h)
+                v.lut[v.w + t] = pixel2cs(0, t, 1, v.h).y;
+        }
+        return;
+    }
     const DevView &v = p.v[blockIdx.z];
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -96,6 +147,7 @@ __global__ void __launch_bounds__(256) splat_kernel(const __grid_constant__ Fram
         return;
     const size_t idx = (size_t)y * v.w + x;
 
+    // keyframe part, independent of the client camera
     const float z_from = __ldg(v.z + idx);
     const float4 om = load_motion(v, idx);
     const float2 pcs = pixel2cs(x, y, v.w, v.h);
@@ -109,95 +161,39 @@ __global__ void __launch_bounds__(256) splat_kernel(const __grid_constant__ Fram
     const bool visible = cm.x > -lim && cm.x < lim && cm.y > -lim && cm.y < lim && cm.z > -lim && cm.z < lim;
     const float vis = visible ? 1.0f : 0.0f;
 
-    const float wg = v.weight;
-    const float4 scaled = make_float4(__fadd_rn(ws_from.x, __fmul_rn(wg, __fsub_rn(ws_to.x, ws_from.x))),
-                                      __fadd_rn(ws_from.y, __fmul_rn(wg, __fsub_rn(ws_to.y, ws_from.y))),
-                                      __fadd_rn(ws_from.z, __fmul_rn(wg, __fsub_rn(ws_to.z, ws_from.z))),
-                                      __fadd_rn(ws_from.w, __fmul_rn(wg, __fsub_rn(ws_to.w, ws_from.w))));
     const float4 cs_to = project(v.vp_to, ws_to);
     const float fmx = __fsub_rn(cs_to.x, cs_from.x), fmy = __fsub_rn(cs_to.y, cs_from.y), fmz = __fsub_rn(cs_to.z, cs_from.z);
     v.full_ff[idx] = make_float4(fmx, fmy, fmz, vis);
+    const float4 d_ws = make_float4(__fsub_rn(ws_to.x, ws_from.x), __fsub_rn(ws_to.y, ws_from.y), __fsub_rn(ws_to.z, ws_from.z),
+                                    __fsub_rn(ws_to.w, ws_from.w));
+    const unsigned long long key_src = encode_key(z_to_depth(z_from), x, y);
 
-    float depth = z_to_depth(z_from);
-    uint32_t tx = x, ty = y;
-    if (!p.linear)
+    // client-camera part, per frame
+    for (int k = 0; k < p.n_frames; k++)
     {
-        const float4 pc = project(p.cam_vp, scaled);
-        v.cam_ff[idx] = make_float4(__fsub_rn(pc.x, cs_from.x), __fsub_rn(pc.y, cs_from.y), __fsub_rn(pc.z, cs_from.z), vis);
-        const float depth_cam = z_to_depth(pc.z);
-        const int2 pix = cs2pixel(pc.x, pc.y, v.w, v.h);
-        if (!in_range(pix, v.w, v.h) || depth_cam < 0.0f)
-            return;
-        depth = depth_cam;
-        tx = (uint32_t)pix.x;
-        ty = (uint32_t)pix.y;
-    }
-    else
-    {
-        v.cam_ff[idx] = make_float4(__fmul_rn(fmx, wg), __fmul_rn(fmy, wg), __fmul_rn(fmz, wg), vis);
-    }
-    atomicMin(v.splat + (size_t)ty * v.w + tx, encode_key(depth, x, y));
-}
-
-// ---- bidirectional reprojection, src/renderer.cu:148-465 ----
-
-struct Result
-{
-    bool valid;
-    bool vis;
-    int32_t priority;
-    float error;
-    float depth;
-    uint32_t color;
-};
-
-// initializeSearchFromSplatting<W>, src/renderer.cu:148-175
-template <int W>
-__device__ __forceinline__ KeyInfo init_search(uint32_t ix, uint32_t iy, const DevView &v)
-{
-    const unsigned long long *sp = v.splat;
-    KeyInfo lowest = decode_key(__ldg(sp + (size_t)iy * v.w + ix));
-#pragma unroll
-    for (int yo = -W; yo <= W; yo++)
-#pragma unroll
-        for (int xo = -W; xo <= W; xo++)
+        const float wg = v.forward ? p.f[k].alpha : __fsub_rn(1.0f, p.f[k].alpha);
+        unsigned long long *keys = v.splat + k * p.key_stride;
+        float4 *cam = v.cam_ff + k * p.cam_stride;
+        if (!p.linear)
         {
-            const int2 n = make_int2((int)ix + xo, (int)iy + yo);
-            if (!in_range(n, v.w, v.h))
-                continue;
-            const KeyInfo cur = decode_key(__ldg(sp + (size_t)n.y * v.w + n.x));
-            if (cur.depth > 0.0f && (!isfinite(lowest.depth) || lowest.depth < 0.0f || cur.depth < lowest.depth))
-                lowest = cur;
+            const float4 scaled = make_float4(__fadd_rn(ws_from.x, __fmul_rn(wg, d_ws.x)), __fadd_rn(ws_from.y, __fmul_rn(wg, d_ws.y)),
+                                              __fadd_rn(ws_from.z, __fmul_rn(wg, d_ws.z)), __fadd_rn(ws_from.w, __fmul_rn(wg, d_ws.w)));
+            const float4 pc = project(p.cam_vp[k], scaled);
+            cam[idx] = make_float4(__fsub_rn(pc.x, cs_from.x), __fsub_rn(pc.y, cs_from.y), __fsub_rn(pc.z, cs_from.z), vis);
+            const float depth_cam = z_to_depth(pc.z);
+            const int2 pix = cs2pixel(pc.x, pc.y, v.w, v.h);
+            if (in_range(pix, v.w, v.h) && !(depth_cam < 0.0f))
+                atomicMin(keys + (size_t)pix.y * v.w + pix.x, encode_key(depth_cam, x, y));
         }
-    return lowest;
-}
-
-// iterativeSearch<N>, src/renderer.cu:177-202
-template <int N>
-__device__ __forceinline__ void iterative_search(uint32_t &sx, uint32_t &sy, float2 q, const DevView &v)
-{
-#pragma unroll
-    for (int i = 0; i < N; i++)
-    {
-        const float4 m = ld_f4(v.cam_ff, sx, sy, v.w, v.h);
-        const int2 t = cs2pixel(__fsub_rn(q.x, m.x), __fsub_rn(q.y, m.y), v.w, v.h);
-        if (!in_range(t, v.w, v.h))
-            continue;
-        sx = (uint32_t)t.x;
-        sy = (uint32_t)t.y;
+        else
+        {
+            cam[idx] = make_float4(__fmul_rn(fmx, wg), __fmul_rn(fmy, wg), __fmul_rn(fmz, wg), vis);
+            atomicMin(keys + idx, key_src);
+        }
     }
 }
 
-// computeReprojError, src/renderer.cu:204-215
-__device__ __forceinline__ float reproj_error(uint32_t sx, uint32_t sy, const DevView &v, float2 pcs, float4 m)
-{
-    const float2 pf = pixel2cs(sx, sy, v.w, v.h);
-    float ex = __fsub_rn(__fadd_rn(pf.x, m.x), pcs.x);
-    float ey = __fsub_rn(__fadd_rn(pf.y, m.y), pcs.y);
-    ex = __fmul_rn(ex, v.err_sx);
-    ey = __fmul_rn(ey, v.err_sy);
-    return __fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)));
-}
+// ---- colour: colorFromShadow / secondChanceAndBlend_kernel, src/renderer.cu:217-327 ----
 
 // colorFromShadow (level-index form), src/renderer.cu:217-268
 __device__ uint32_t color_from_shadow_idx(uint32_t sidx, int32_t sfpa, const DevView &v, uint32_t px, uint32_t py)
@@ -237,173 +233,178 @@ __device__ uint32_t color_from_shadow_idx(uint32_t sidx, int32_t sfpa, const Dev
     return main_color;
 }
 
-// colorFromShadow (two sub-frame form), src/renderer.cu:270-295
-__device__ uint32_t color_from_shadow(uint32_t sfx, uint32_t sfy, float sft, const FrameParams &p, const DevView &v, uint32_t px,
-                                      uint32_t py)
-{
-    if (p.no_shadows || sfx >= (uint32_t)p.sfpa || sfy == 0 || v.sha == nullptr)
-        return ld_c(v.color, px, py, v.w, v.h);
-    const int32_t sfpa = p.sfpa;
-    const uint32_t vx = (uint32_t)(v.forward ? (int32_t)sfx : sfpa - (int32_t)sfx);
-    const uint32_t vy = (uint32_t)(v.forward ? (int32_t)sfy : sfpa - (int32_t)sfy);
-    if (vx == vy || vy >= (uint32_t)sfpa)
-        return color_from_shadow_idx(vx, sfpa, v, px, py);
-    if (vx >= (uint32_t)sfpa)
-        return color_from_shadow_idx(vy, sfpa, v, px, py);
-    const uint32_t a = color_from_shadow_idx(vx, sfpa, v, px, py);
-    const uint32_t b = color_from_shadow_idx(vy, sfpa, v, px, py);
-    return lerp_color_u8(a, b, sft);
-}
-
 struct ShadowFrames
 {
     uint32_t frame_idx, sfx, sfy;
     float sft;
 };
 
-// secondChanceAndBlend_kernel<EPS_2>, src/renderer.cu:297-327
-__device__ uint32_t second_chance(float weight, const ShadowFrames &sf, uint32_t sx, uint32_t sy, const FrameParams &p, const DevView &from,
-                                  const DevView &to, float eps2)
+// frame_idx / shadow sub-frames, src/renderer.cu:359-364
+__device__ __forceinline__ ShadowFrames shadow_frames(const FrameCfg &c)
 {
-    const float4 m_ft = ld_f4(from.full_ff, sx, sy, from.w, from.h);
-    const float2 spcs = pixel2cs(sx, sy, from.w, from.h);
-    const float sz = ld_f(from.z, sx, sy, from.w, from.h);
-    const float pcx = __fadd_rn(spcs.x, m_ft.x), pcy = __fadd_rn(spcs.y, m_ft.y), pcz = __fadd_rn(sz, m_ft.z);
-    const int2 pp = cs2pixel(pcx, pcy, to.w, to.h);
-
-    uint32_t out = color_from_shadow(sf.sfx, sf.sfy, sf.sft, p, from, sx, sy);
-    if (sf.frame_idx >= (uint32_t)p.fpa)
-        return out;
-    if (in_range(pp, to.w, to.h))
-    {
-        const float az = ld_f(to.z, pp.x, pp.y, to.w, to.h);
-        const float4 m_tf = ld_f4(to.full_ff, pp.x, pp.y, to.w, to.h);
-        const float dx = __fsub_rn(m_ft.x, -m_tf.x), dy = __fsub_rn(m_ft.y, -m_tf.y), dz = __fsub_rn(m_ft.z, -m_tf.z);
-        const float dist = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
-        if (dist < EPS_3 && fabsf(__fsub_rn(az, pcz)) < eps2)
-            out = lerp_color_u8(color_from_shadow(sf.sfx, sf.sfy, sf.sft, p, to, pp.x, pp.y), out, weight);
-    }
-    return out;
-}
-
-// bidirectionalReprojection<SW, SI, ALWAYS_VALID, EPS_1, EPS_2>, src/renderer.cu:329-398
-template <int SW, int SI, bool ALWAYS_VALID>
-__device__ __forceinline__ Result bidir(uint32_t ix, uint32_t iy, float2 q_full, float2 pcs, const ShadowFrames &sf, const FrameParams &p,
-                                        const DevView &fwd, const DevView &bwd, float eps1, float eps2)
-{
-    float fwd_e = 3.402823466e+38f; // FLT_MAX
-    bool fwd_vis = false;
-    KeyInfo fi = init_search<SW>(ix, iy, fwd);
-    if (fi.depth > 0.0f && p.alpha < 1.0f)
-    {
-        iterative_search<SI>(fi.sx, fi.sy, q_full, fwd);
-        const float4 m = ld_f4(fwd.cam_ff, fi.sx, fi.sy, fwd.w, fwd.h);
-        fi.depth = z_to_depth(__fadd_rn(ld_f(fwd.z, fi.sx, fi.sy, fwd.w, fwd.h), m.z));
-        fwd_e = reproj_error(fi.sx, fi.sy, fwd, pcs, m);
-        fwd_vis = m.w > 0.0f;
-    }
-    float bwd_e = 3.402823466e+38f;
-    bool bwd_vis = false;
-    KeyInfo bi = init_search<SW>(ix, iy, bwd);
-    if (bi.depth > 0.0f)
-    {
-        iterative_search<SI>(bi.sx, bi.sy, q_full, bwd);
-        const float4 m = ld_f4(bwd.cam_ff, bi.sx, bi.sy, bwd.w, bwd.h);
-        bi.depth = z_to_depth(__fadd_rn(ld_f(bwd.z, bi.sx, bi.sy, bwd.w, bwd.h), m.z));
-        bwd_e = reproj_error(bi.sx, bi.sy, bwd, pcs, m);
-        bwd_vis = m.w > 0.0f;
-    }
-
-    Result r;
-    r.valid = false;
-    r.vis = false;
-    r.priority = 0;
-    r.error = 0.0f; // indeterminate in the reference for the always-valid blend
-    r.depth = 0.0f;
-    r.color = 0u;
-    if (fwd_e < eps1 || bwd_e < eps1)
-    {
-        const bool both = fwd_e < eps1 && bwd_e < eps1;
-        const bool similar = fabsf(__fsub_rn(depth_to_z(fi.depth), depth_to_z(bi.depth))) < eps2;
-        const bool choose_fwd = (both && !similar && fi.depth < bi.depth) || ((!both || similar) && fwd_e < bwd_e);
-        r.valid = true;
-        if (choose_fwd)
-        {
-            r.vis = fwd_vis || (both && similar && bwd_vis);
-            r.priority = fwd.priority;
-            r.error = fwd_e;
-            r.depth = fi.depth;
-            r.color = second_chance(__fsub_rn(1.0f, p.alpha), sf, fi.sx, fi.sy, p, fwd, bwd, eps2);
-        }
-        else
-        {
-            r.vis = bwd_vis || (both && similar && fwd_vis);
-            r.priority = bwd.priority;
-            r.error = bwd_e;
-            r.depth = bi.depth;
-            r.color = second_chance(p.alpha, sf, bi.sx, bi.sy, p, bwd, fwd, eps2);
-        }
-    }
-    else if (ALWAYS_VALID)
-    {
-        r.valid = true;
-        const uint32_t cf = second_chance(__fsub_rn(1.0f, p.alpha), sf, fi.sx, fi.sy, p, fwd, bwd, eps2);
-        const uint32_t cb = second_chance(p.alpha, sf, bi.sx, bi.sy, p, bwd, fwd, eps2);
-        r.color = lerp_color_u8(cf, cb, 0.5f);
-    }
-    return r;
-}
-
-// bidirectionalReprojection_kernel<SW, SI, MAIN_ALWAYS_VALID>, src/renderer.cu:400-465
-template <int SW, int SI, bool MAV>
-__global__ void __launch_bounds__(256) reproj_kernel(const __grid_constant__ FrameParams p)
-{
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= p.out_w || y >= p.out_h)
-        return;
-
-    // frame_idx / shadow sub-frames, src/renderer.cu:359-364
     ShadowFrames sf;
-    const float fa = __fmul_rn((float)p.fpa, p.alpha);
-    const float sa = __fmul_rn((float)p.sfpa, p.alpha);
+    const float fa = __fmul_rn((float)c.fpa, c.alpha);
+    const float sa = __fmul_rn((float)c.sfpa, c.alpha);
     sf.frame_idx = __float2uint_rn(fa);
     sf.sfx = __float2uint_rd(__fadd_rn(sa, 1e-9f));
     sf.sfy = __float2uint_ru(__fsub_rn(sa, 1e-9f));
     sf.sft = __fsub_rn(sa, (float)sf.sfx);
+    return sf;
+}
 
-    const float2 pcs = pixel2cs(x, y, p.out_w, p.out_h);
-    uint32_t *o = p.out + (size_t)y * p.out_w + x;
-    const Result m = bidir<SW, SI, MAV>(x, y, pcs, pcs, sf, p, p.v[0], p.v[1], EPS_1_FULL_RES, EPS_2_FULL_RES);
-    if (m.valid)
-        *o = m.color;
-    if (p.n_aux <= 0)
-        return;
+// colorFromShadow (two sub-frame form), src/renderer.cu:270-295
+__device__ uint32_t color_from_shadow(const ShadowFrames &sf, const FrameCfg &c, const DevView &v, uint32_t px, uint32_t py)
+{
+    if (c.no_shadows || sf.sfx >= (uint32_t)c.sfpa || sf.sfy == 0 || v.sha == nullptr)
+        return ld_c(v.color, px, py, v.w, v.h);
+    const int32_t sfpa = c.sfpa;
+    const uint32_t vx = (uint32_t)(v.forward ? (int32_t)sf.sfx : sfpa - (int32_t)sf.sfx);
+    const uint32_t vy = (uint32_t)(v.forward ? (int32_t)sf.sfy : sfpa - (int32_t)sf.sfy);
+    if (vx == vy || vy >= (uint32_t)sfpa)
+        return color_from_shadow_idx(vx, sfpa, v, px, py);
+    if (vx >= (uint32_t)sfpa)
+        return color_from_shadow_idx(vy, sfpa, v, px, py);
+    const uint32_t a = color_from_shadow_idx(vx, sfpa, v, px, py);
+    const uint32_t b = color_from_shadow_idx(vy, sfpa, v, px, py);
+    return lerp_color_u8(a, b, sf.sft);
+}
 
-    Result best;
+// secondChanceAndBlend_kernel<EPS_2>, src/renderer.cu:297-327
+__device__ uint32_t second_chance(float weight, const ShadowFrames &sf, const FrameCfg &c, uint32_t sx, uint32_t sy, const DevView &from,
+                                  const DevView &to, float eps2)
+{
+    const float4 m_ft = ld_f4(from.full_ff, sx, sy, from.w, from.h);
+    const float2 spcs = view_pixel2cs(from, sx, sy);
+    const float sz = ld_f(from.z, sx, sy, from.w, from.h);
+    const float pcx = __fadd_rn(spcs.x, m_ft.x), pcy = __fadd_rn(spcs.y, m_ft.y), pcz = __fadd_rn(sz, m_ft.z);
+    const int2 pp = cs2pixel(pcx, pcy, to.w, to.h);
+
+    uint32_t out = color_from_shadow(sf, c, from, sx, sy);
+    if (sf.frame_idx >= (uint32_t)c.fpa)
+        return out;
+    if (in_range(pp, to.w, to.h))
+    {
+        const size_t pi = (size_t)pp.y * to.w + pp.x;
+        const float az = __ldg(to.z + pi);
+        const float4 m_tf = __ldg(to.full_ff + pi);
+        const float dx = __fsub_rn(m_ft.x, -m_tf.x), dy = __fsub_rn(m_ft.y, -m_tf.y), dz = __fsub_rn(m_ft.z, -m_tf.z);
+        if (sqrt_less(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)), EPS_3) &&
+            fabsf(__fsub_rn(az, pcz)) < eps2)
+            out = lerp_color_u8(color_from_shadow(sf, c, to, pp.x, pp.y), out, weight);
+    }
+    return out;
+}
+
+// ---- bidirectional reprojection, src/renderer.cu:148-465 ----
+
+// One direction of one camera for one output pixel: window init + search + error.
+struct DirRes
+{
+    float error;  // FLT_MAX when not searched
+    float depth;  // searched depth, else the window-initialisation depth
+    uint32_t src; // source pixel, x << 16 | y
+    uint32_t vis; // visible_in_main
+};
+
+// Result of bidirectionalReprojection for one camera (src/renderer.cu:366-397), without its colour.
+struct CamRes
+{
+    bool valid;
+    bool vis;
+    bool blend;      // always-valid 50/50 blend of both directions
+    int32_t priority;
+    float error;     // indeterminate in the reference for the blend; 0 here
+    float depth;
+    int32_t dir;     // 0 forward keyframe, 1 backward keyframe
+    uint32_t src;
+};
+
+template <int SW>
+struct Tile
+{
+    static constexpr int W = 32 + 2 * SW;
+    static constexpr int H = 2 * SW + 1;
+};
+
+__device__ __forceinline__ CamRes cam_result(const DirRes &f, const DirRes &b, const DevView &vf, const DevView &vb, float eps1, float eps2,
+                                             bool always_valid)
+{
+    CamRes r;
+    r.valid = false;
+    r.vis = false;
+    r.blend = false;
+    r.priority = 0;
+    r.error = 0.0f;
+    r.depth = 0.0f;
+    r.dir = 0;
+    r.src = 0;
+    if (f.error < eps1 || b.error < eps1)
+    {
+        const bool both = f.error < eps1 && b.error < eps1;
+        const bool similar = fabsf(__fsub_rn(depth_to_z(f.depth), depth_to_z(b.depth))) < eps2;
+        const bool choose_fwd = (both && !similar && f.depth < b.depth) || ((!both || similar) && f.error < b.error);
+        r.valid = true;
+        if (choose_fwd)
+        {
+            r.vis = f.vis || (both && similar && b.vis);
+            r.priority = vf.priority;
+            r.error = f.error;
+            r.depth = f.depth;
+            r.dir = 0;
+            r.src = f.src;
+        }
+        else
+        {
+            r.vis = b.vis || (both && similar && f.vis);
+            r.priority = vb.priority;
+            r.error = b.error;
+            r.depth = b.depth;
+            r.dir = 1;
+            r.src = b.src;
+        }
+    }
+    else if (always_valid)
+    {
+        r.valid = true;
+        r.blend = true;
+    }
+    return r;
+}
+
+// Chooses among the cameras of one output pixel and returns the colour to
+// write (valid = false: keep the previous output), src/renderer.cu:400-465.
+template <bool MAV>
+__device__ __forceinline__ bool resolve_pixel(const DirRes *res, int lane, const FrameParams &p, const FrameCfg &c, uint32_t &color)
+{
+    const CamRes m = cam_result(res[lane], res[32 + lane], p.v[0], p.v[1], EPS_1_FULL_RES, EPS_2_FULL_RES, MAV);
+    CamRes best;
     best.valid = false;
     best.vis = false;
     best.priority = 0;
     best.error = 0.0f;
     best.depth = 0.0f;
-    best.color = 0u;
-    for (int i = 0; i < p.n_aux; i++)
+    int best_cam = 0;
+    const int n_cams = p.n_views / 2;
+    for (int cam = 1; cam < n_cams; cam++)
     {
-        const DevView &vf = p.v[2 + 2 * i];
-        const DevView &vb = p.v[3 + 2 * i];
-        const uint32_t ax = x / (p.out_w / vf.w), ay = y / (p.out_h / vf.h);
-        const float2 apcs = pixel2cs(ax, ay, vf.w, vf.h);
-        const Result r = bidir<SW, SI, false>(ax, ay, pcs, apcs, sf, p, vf, vb, EPS_1_LOW_RES, EPS_2_LOW_RES);
-        if (!best.valid)
-            best = r;
-        else if (r.valid)
+        const CamRes r = cam_result(res[(2 * cam) * 32 + lane], res[(2 * cam + 1) * 32 + lane], p.v[2 * cam], p.v[2 * cam + 1], EPS_1_LOW_RES,
+                                    EPS_2_LOW_RES, false);
+        bool take = !best.valid;
+        if (best.valid && r.valid)
         {
             const bool similar = fabsf(__fsub_rn(depth_to_z(best.depth), depth_to_z(r.depth))) < EPS_2_LOW_RES;
-            const bool choose_new = (!similar && r.depth < best.depth) || (similar && r.priority >= best.priority && r.error < best.error);
-            if (choose_new)
-                best = r;
+            take = (!similar && r.depth < best.depth) || (similar && r.priority >= best.priority && r.error < best.error);
+        }
+        if (take)
+        {
+            best = r;
+            best_cam = cam;
         }
     }
+    int cam = -1;
+    CamRes fin = m;
+    if (m.valid)
+        cam = 0;
     if (best.valid)
     {
         bool choose_aux = !m.valid;
@@ -413,8 +414,156 @@ __global__ void __launch_bounds__(256) reproj_kernel(const __grid_constant__ Fra
             choose_aux = !similar && best.depth < m.depth;
         }
         if (choose_aux)
-            *o = best.color;
+        {
+            cam = best_cam;
+            fin = best;
+        }
     }
+    if (cam < 0)
+        return false; // temporal hole filling: keep the previous output (src/renderer.cu:416-419,462-463)
+
+    const ShadowFrames sf = shadow_frames(c);
+    const DevView &vf = p.v[2 * cam], &vb = p.v[2 * cam + 1];
+    const float eps2 = cam == 0 ? EPS_2_FULL_RES : EPS_2_LOW_RES;
+    const float oma = __fsub_rn(1.0f, c.alpha);
+    if (fin.blend)
+    {
+        const DirRes &f = res[lane], &b = res[32 + lane];
+        const uint32_t cf = second_chance(oma, sf, c, f.src >> 16, f.src & 0xFFFFu, vf, vb, eps2);
+        const uint32_t cb = second_chance(c.alpha, sf, c, b.src >> 16, b.src & 0xFFFFu, vb, vf, eps2);
+        color = lerp_color_u8(cf, cb, 0.5f);
+    }
+    else if (fin.dir == 0)
+        color = second_chance(oma, sf, c, fin.src >> 16, fin.src & 0xFFFFu, vf, vb, eps2);
+    else
+        color = second_chance(c.alpha, sf, c, fin.src >> 16, fin.src & 0xFFFFu, vb, vf, eps2);
+    return true;
+}
+
+// bidirectionalReprojection_kernel<SW, SI, MAIN_ALWAYS_VALID>, src/renderer.cu:400-465
+// block = (32, n_views): 32 output pixels of row blockIdx.y, one warp per source view,
+// looping over the frames of the batch.
+template <int SW, int SI, bool MAV>
+__global__ void __launch_bounds__(32 * MAX_VIEWS) reproj_kernel(const __grid_constant__ FrameParams p)
+{
+    using T = Tile<SW>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int nv = p.n_views;
+    DirRes *res2 = reinterpret_cast<DirRes *>(smem);                    // [2][nv][32], double-buffered over frames
+    uint32_t *chain = reinterpret_cast<uint32_t *>(res2 + 2 * nv * 32); // [32] running output when chaining
+    unsigned long long *tiles = reinterpret_cast<unsigned long long *>(chain + 32);
+
+    const int lane = threadIdx.x, vw = threadIdx.y;
+    const uint32_t x0 = blockIdx.x * 32, x = x0 + lane, y = blockIdx.y;
+    const DevView &v = p.v[vw];
+    const uint32_t ix = v.sx == 1 ? x : x / v.sx, iy = v.sy == 1 ? y : y / v.sy, tx0 = v.sx == 1 ? x0 : x0 / v.sx;
+    const bool fwd = (vw & 1) == 0;
+    unsigned long long *tile = tiles + vw * (T::H * T::W);
+    const int cx = (int)(ix - tx0) + SW;
+    const float qx = __ldg(p.v[0].lut + min(x, p.out_w - 1)), qy = __ldg(p.v[0].lut + p.v[0].w + y); // pixel2CS(idx, res)
+    const float pcx = __ldg(v.lut + min(ix, v.w - 1)), pcy = __ldg(v.lut + v.w + iy);              // pixel2CS in this view
+
+    for (int k = 0; k < p.n_frames; k++)
+    {
+        const unsigned long long *keys = v.splat + k * p.key_stride;
+        const float4 *cam = v.cam_ff + k * p.cam_stride;
+        // splat keys around this warp's pixels (initializeSearchFromSplatting<SW>, src/renderer.cu:148-175);
+        // a key outside the view reads as 0 (depth +0.0), which the window never selects, exactly like the
+        // reference's skipped out-of-range neighbours
+#pragma unroll
+        for (int r = 0; r < T::H; r++)
+        {
+            const int gy = (int)iy - SW + r;
+            const bool row_ok = gy >= 0 && gy < (int)v.h;
+            for (int c = lane; c < T::W; c += 32)
+            {
+                const int gx = (int)tx0 - SW + c;
+                tile[r * T::W + c] = (row_ok && gx >= 0 && gx < (int)v.w) ? __ldg(keys + (size_t)gy * v.w + gx) : 0ull;
+            }
+        }
+        __syncwarp();
+
+        DirRes d;
+        d.error = FLT_MAX_F;
+        d.depth = 0.0f;
+        d.src = 0;
+        d.vis = 0;
+        if (x < p.out_w)
+        {
+            KeyInfo lowest = decode_key(tile[SW * T::W + cx]);
+#pragma unroll
+            for (int yo = -SW; yo <= SW; yo++)
+#pragma unroll
+                for (int xo = -SW; xo <= SW; xo++)
+                {
+                    const KeyInfo cur = decode_key(tile[(SW + yo) * T::W + cx + xo]);
+                    if (cur.depth > 0.0f && (!isfinite(lowest.depth) || lowest.depth < 0.0f || cur.depth < lowest.depth))
+                        lowest = cur;
+                }
+            uint32_t ssx = lowest.sx, ssy = lowest.sy;
+            d.depth = lowest.depth;
+            if (lowest.depth > 0.0f && (!fwd || p.f[k].alpha < 1.0f))
+            {
+                // iterativeSearch<SI>, src/renderer.cu:177-202.  The start is a splatted source pixel
+                // and every accepted step is in range, so no border handling is needed.
+#pragma unroll
+                for (int i = 0; i < SI; i++)
+                {
+                    const float4 m = __ldg(cam + (size_t)ssy * v.w + ssx);
+                    const int2 t = cs2pixel(__fsub_rn(qx, m.x), __fsub_rn(qy, m.y), v.w, v.h);
+                    if (in_range(t, v.w, v.h))
+                    {
+                        ssx = (uint32_t)t.x;
+                        ssy = (uint32_t)t.y;
+                    }
+                }
+                const size_t si = (size_t)ssy * v.w + ssx;
+                const float4 m = __ldg(cam + si);
+                d.depth = z_to_depth(__fadd_rn(__ldg(v.z + si), m.z));
+                // computeReprojError, src/renderer.cu:204-215
+                const float pfx = __ldg(v.lut + ssx), pfy = __ldg(v.lut + v.w + ssy);
+                float ex = __fsub_rn(__fadd_rn(pfx, m.x), pcx);
+                float ey = __fsub_rn(__fadd_rn(pfy, m.y), pcy);
+                ex = __fmul_rn(ex, v.err_sx);
+                ey = __fmul_rn(ey, v.err_sy);
+                d.error = __fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)));
+                d.vis = m.w > 0.0f;
+            }
+            d.src = (ssx << 16) | ssy;
+        }
+        DirRes *res = res2 + (k & 1) * nv * 32;
+        res[vw * 32 + lane] = d;
+        __syncthreads();
+        // The choice and colour of frame k run on warp k % nv while the other warps go
+        // on with frame k + 1 (double-buffered results).  The barrier of the next frame
+        // orders the running output of the chain from frame k to frame k + 1.
+        if (vw == k % nv && x < p.out_w)
+        {
+            uint32_t color = 0;
+            const bool valid = resolve_pixel<MAV>(res, lane, p, p.f[k], color);
+            uint32_t *o = p.out[k] + (size_t)y * p.out_w + x;
+            if (!p.chain)
+            {
+                if (valid)
+                    *o = color;
+            }
+            else
+            {
+                uint32_t run = k == 0 ? *o : chain[lane];
+                if (valid)
+                    run = color;
+                if (k > 0 || valid)
+                    *o = run;
+                chain[lane] = run;
+            }
+        }
+    }
+}
+
+template <int SW>
+constexpr size_t reproj_smem(int n_views)
+{
+    return (size_t)n_views * (2 * 32 * sizeof(DirRes) + Tile<SW>::H * Tile<SW>::W * sizeof(unsigned long long)) + 32 * sizeof(uint32_t);
 }
 } // namespace isti
 
@@ -427,9 +576,10 @@ struct isti_renderer
     size_t arena_bytes = 0;
     isti::FrameParams last{};
     bool has_frame = false;
-    // stage timing: 4 events per timed render (before init, after init, after splat, after reproj)
+    // stage timing: 4 events per timed call (before init, after init, after splat, after reproj)
     bool timing = false;
     std::vector<cudaEvent_t> events;
+    std::vector<int32_t> event_frames;
     size_t events_used = 0;
     int32_t timed_launches = 0;
 };
@@ -470,26 +620,260 @@ bool view_ok(const isti_view &v, std::string &why)
     return true;
 }
 
-void fill_view(isti::DevView &d, const isti_view &v, int forward, int priority, float weight, const float *vp_to, const float *vp_main)
+// Checks a batch (the reference's implicit contract, made explicit) and
+// returns its source views in kernel order.
+isti_status validate(int n_frames, void *const *outs, const isti_render_info *infos, const isti_frame_data *frame, const isti_view **views,
+                     int &n_views)
 {
-    d.color = static_cast<const uint32_t *>(v.color);
-    d.z = v.z;
-    d.motion = v.motion_format == ISTI_MOTION_NONE ? nullptr : v.motion;
-    d.motion_fmt = v.motion_format;
-    d.sha = static_cast<const uint32_t *>(v.shadow_color_a);
-    d.shb = static_cast<const uint32_t *>(v.shadow_color_b);
-    d.shi = static_cast<const uint32_t *>(v.shadow_info);
-    d.w = v.width;
-    d.h = v.height;
-    d.forward = forward;
-    d.priority = priority;
-    d.weight = weight;
-    const uint32_t mn = v.width < v.height ? v.width : v.height;
-    d.err_sx = (float)v.width / (float)mn;
-    d.err_sy = (float)v.height / (float)mn;
-    std::memcpy(d.inv_vp, v.inv_viewproj, sizeof d.inv_vp);
-    std::memcpy(d.vp_to, vp_to, sizeof d.vp_to);
-    std::memcpy(d.vp_main, vp_main, sizeof d.vp_main);
+    if (n_frames < 1 || n_frames > ISTI_MAX_BATCH_FRAMES)
+        return fail(ISTI_ERR_INVALID_ARG, "n_frames must be 1..ISTI_MAX_BATCH_FRAMES");
+    const isti_render_info *info = &infos[0];
+    for (int k = 0; k < n_frames; k++)
+    {
+        const isti_render_info &f = infos[k];
+        if (!outs[k])
+            return fail(ISTI_ERR_INVALID_ARG, "NULL output buffer");
+        if (reinterpret_cast<uintptr_t>(outs[k]) & 3u)
+            return fail(ISTI_ERR_INVALID_ARG, "output buffers must be 4-byte aligned");
+        if (f.mode == ISTI_MODE_TIMEWARP)
+            return fail(ISTI_ERR_UNSUPPORTED, "timewarp mode is not implemented");
+        if (f.mode < 0 || f.mode > ISTI_MODE_TIMEWARP)
+            return fail(ISTI_ERR_INVALID_ARG, "unknown render mode");
+        if (f.shadow_frames_per_anchor < 0 || f.shadow_frames_per_anchor > 16)
+            return fail(ISTI_ERR_INVALID_ARG, "shadow_frames_per_anchor must be 0..16");
+        if (f.width != info->width || f.height != info->height || f.mode != info->mode)
+            return fail(ISTI_ERR_INVALID_ARG, "all frames of a batch need the same resolution and mode");
+    }
+    std::string why;
+    if (!view_ok(frame->fwd, why) || !view_ok(frame->bwd, why))
+        return fail(ISTI_ERR_INVALID_ARG, why);
+    if (frame->fwd.width != info->width || frame->fwd.height != info->height || frame->bwd.width != info->width ||
+        frame->bwd.height != info->height)
+        return fail(ISTI_ERR_INVALID_ARG, "render resolution must equal the main keyframes' resolution");
+    const int n_aux = frame->num_aux;
+    if (n_aux < 0 || n_aux > ISTI_MAX_AUX_CAMS)
+        return fail(ISTI_ERR_INVALID_ARG, "num_aux out of range");
+    if (n_aux > 0 && (!frame->aux_curr || !frame->aux_next))
+        return fail(ISTI_ERR_INVALID_ARG, "aux views are NULL");
+    for (int i = 0; i < n_aux; i++)
+    {
+        const isti_view &a = frame->aux_curr[i], &b = frame->aux_next[i];
+        if (!view_ok(a, why) || !view_ok(b, why))
+            return fail(ISTI_ERR_INVALID_ARG, why);
+        if (a.width != b.width || a.height != b.height)
+            return fail(ISTI_ERR_INVALID_ARG, "aux curr/next sizes differ");
+        // aux_idx = idx / (res / aux_res) must stay inside the aux image (src/renderer.cu:425,433)
+        if (a.width > info->width || a.height > info->height || (info->width - 1) / (info->width / a.width) >= a.width ||
+            (info->height - 1) / (info->height / a.height) >= a.height)
+            return fail(ISTI_ERR_INVALID_ARG, "aux resolution incompatible with the render resolution");
+    }
+    n_views = 2 + 2 * n_aux;
+    views[0] = &frame->fwd;
+    views[1] = &frame->bwd;
+    for (int i = 0; i < n_aux; i++)
+    {
+        views[2 + 2 * i] = &frame->aux_curr[i];
+        views[3 + 2 * i] = &frame->aux_next[i];
+    }
+    return ISTI_OK;
+}
+
+struct Layout
+{
+    size_t key_frame_bytes, cam_frame_bytes; // one frame, every view
+    size_t key_bytes, cam_bytes, ff_bytes, lut_bytes, total;
+};
+
+Layout layout_of(const isti_view *const *views, int n_views, int n_frames)
+{
+    Layout l{};
+    for (int k = 0; k < n_views; k++)
+    {
+        const size_t px = (size_t)views[k]->width * views[k]->height;
+        l.key_frame_bytes += align_up(px * 8, 256);
+        l.cam_frame_bytes += align_up(px * 16, 256);
+        l.lut_bytes += align_up((size_t)(views[k]->width + views[k]->height) * 4, 256);
+    }
+    l.ff_bytes = l.cam_frame_bytes;
+    l.key_bytes = l.key_frame_bytes * n_frames;
+    l.cam_bytes = l.cam_frame_bytes * n_frames;
+    l.total = l.key_bytes + l.cam_bytes + l.ff_bytes + l.lut_bytes;
+    return l;
+}
+
+// Fills the kernel parameters for one batch whose intermediates live at `base`.
+void fill_params(isti::FrameParams &p, int n_frames, void *const *outs, const isti_render_info *infos, const isti_frame_data *frame,
+                 const isti_view *const *views, int n_views, const Layout &l, char *base, bool chain)
+{
+    std::memset(&p, 0, sizeof p);
+    const isti_render_info &info = infos[0];
+    size_t off_key = 0, off_cam = l.key_bytes, off_full = l.key_bytes + l.cam_bytes, off_lut = l.key_bytes + l.cam_bytes + l.ff_bytes;
+    for (int k = 0; k < n_views; k++)
+    {
+        const bool fw = (k % 2) == 0;
+        const isti_view &v = *views[k];
+        isti::DevView &d = p.v[k];
+        d.color = static_cast<const uint32_t *>(v.color);
+        d.z = v.z;
+        d.motion = v.motion_format == ISTI_MOTION_NONE ? nullptr : v.motion;
+        d.motion_fmt = v.motion_format;
+        d.sha = static_cast<const uint32_t *>(v.shadow_color_a);
+        d.shb = static_cast<const uint32_t *>(v.shadow_color_b);
+        d.shi = static_cast<const uint32_t *>(v.shadow_info);
+        d.w = v.width;
+        d.h = v.height;
+        d.sx = k < 2 ? 1u : info.width / v.width;
+        d.sy = k < 2 ? 1u : info.height / v.height;
+        d.forward = fw ? 1 : 0;
+        d.priority = (k < 2 || !frame->aux_priority) ? 0 : frame->aux_priority[(k - 2) / 2];
+        const uint32_t mn = v.width < v.height ? v.width : v.height;
+        d.err_sx = (float)v.width / (float)mn;
+        d.err_sy = (float)v.height / (float)mn;
+        const float *vp_to = (k < 2) ? (fw ? frame->bwd.viewproj : frame->fwd.viewproj)
+                                     : (fw ? frame->aux_next[(k - 2) / 2].viewproj : frame->aux_curr[(k - 2) / 2].viewproj);
+        const float *vp_main = fw ? frame->fwd.viewproj : frame->bwd.viewproj;
+        std::memcpy(d.inv_vp, v.inv_viewproj, sizeof d.inv_vp);
+        std::memcpy(d.vp_to, vp_to, sizeof d.vp_to);
+        std::memcpy(d.vp_main, vp_main, sizeof d.vp_main);
+        const size_t px = (size_t)v.width * v.height;
+        d.splat = reinterpret_cast<unsigned long long *>(base + off_key);
+        d.cam_ff = reinterpret_cast<float4 *>(base + off_cam);
+        d.full_ff = reinterpret_cast<float4 *>(base + off_full);
+        d.lut = reinterpret_cast<float *>(base + off_lut);
+        off_key += align_up(px * 8, 256);
+        off_cam += align_up(px * 16, 256);
+        off_full += align_up(px * 16, 256);
+        off_lut += align_up((size_t)(v.width + v.height) * 4, 256);
+    }
+    for (int k = 0; k < n_frames; k++)
+    {
+        std::memcpy(p.cam_vp[k], infos[k].viewproj, sizeof p.cam_vp[k]);
+        p.out[k] = static_cast<uint32_t *>(outs[k]);
+        p.f[k].alpha = infos[k].alpha;
+        p.f[k].fpa = infos[k].frames_per_anchor;
+        p.f[k].sfpa = infos[k].shadow_frames_per_anchor;
+        p.f[k].no_shadows = infos[k].no_shadows ? 1 : 0;
+    }
+    p.key_stride = l.key_frame_bytes / sizeof(unsigned long long);
+    p.cam_stride = l.cam_frame_bytes / sizeof(float4);
+    p.out_w = info.width;
+    p.out_h = info.height;
+    p.n_views = n_views;
+    p.n_aux = frame->num_aux;
+    p.n_frames = n_frames;
+    p.linear = info.mode == ISTI_MODE_BACKWARD_BIDIRECTIONAL ? 1 : 0;
+    p.chain = chain ? 1 : 0;
+}
+
+// Enqueues the splat and reprojection kernels of one batch.
+cudaError_t launch_batch(const isti::FrameParams &p, int mode, cudaStream_t stream, cudaEvent_t after_splat)
+{
+    uint32_t max_w = 0, max_h = 0;
+    for (int k = 0; k < p.n_views; k++)
+    {
+        max_w = p.v[k].w > max_w ? p.v[k].w : max_w;
+        max_h = p.v[k].h > max_h ? p.v[k].h : max_h;
+    }
+    const dim3 blk(32, 8);
+    const dim3 gs((max_w + 31) / 32, (max_h + 7) / 8, p.n_views + 1);
+    isti::splat_kernel<<<gs, blk, 0, stream>>>(p);
+    if (after_splat)
+        cudaEventRecord(after_splat, stream);
+    const dim3 gr((p.out_w + 31) / 32, p.out_h);
+    const dim3 br(32, p.n_views);
+    switch (mode)
+    {
+    case ISTI_MODE_OURS:
+    case ISTI_MODE_BACKWARD_UNIDIRECTIONAL:
+        isti::reproj_kernel<1, 3, false><<<gr, br, isti::reproj_smem<1>(p.n_views), stream>>>(p);
+        break;
+    case ISTI_MODE_SPLATTING:
+        isti::reproj_kernel<1, 0, false><<<gr, br, isti::reproj_smem<1>(p.n_views), stream>>>(p);
+        break;
+    case ISTI_MODE_BACKWARD_BIDIRECTIONAL:
+    {
+        const size_t smem = isti::reproj_smem<3>(p.n_views); // above 48 KiB from 7 aux cameras on
+        if (smem > 48 * 1024)
+        {
+            cudaError_t e = cudaFuncSetAttribute(isti::reproj_kernel<3, 5, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess)
+                return e;
+        }
+        isti::reproj_kernel<3, 5, true><<<gr, br, smem, stream>>>(p);
+        break;
+    }
+    }
+    return cudaGetLastError();
+}
+
+isti_status render_batch(isti_renderer *r, int n_frames, void *const *outs, const isti_render_info *infos, const isti_frame_data *frame,
+                         bool chain, cudaStream_t stream)
+{
+    const isti_view *views[isti::MAX_VIEWS];
+    int n_views = 0;
+    isti_status st = validate(n_frames, outs, infos, frame, views, n_views);
+    if (st != ISTI_OK)
+        return st;
+    const Layout l = layout_of(views, n_views, n_frames);
+
+    int cur = 0;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaGetDevice");
+    if (cur != r->device)
+        return fail(ISTI_ERR_INVALID_ARG, "renderer was created on another device");
+    if (l.total > r->arena_bytes)
+    {
+        if (r->arena)
+        {
+            e = cudaFree(r->arena);
+            r->arena = nullptr;
+            r->arena_bytes = 0;
+            if (e != cudaSuccess)
+                return cuda_fail(e, "cudaFree");
+        }
+        e = cudaMalloc(&r->arena, l.total);
+        if (e != cudaSuccess)
+        {
+            r->arena = nullptr;
+            return e == cudaErrorMemoryAllocation ? fail(ISTI_ERR_OOM, "cudaMalloc of the renderer arena failed") : cuda_fail(e, "cudaMalloc");
+        }
+        r->arena_bytes = l.total;
+    }
+    char *base = static_cast<char *>(r->arena);
+    fill_params(r->last, n_frames, outs, infos, frame, views, n_views, l, base, chain);
+
+    cudaEvent_t *ev = nullptr;
+    if (r->timing)
+    {
+        if (r->events_used + 4 > r->events.size())
+            for (int i = 0; i < 4; i++)
+            {
+                cudaEvent_t x;
+                e = cudaEventCreate(&x);
+                if (e != cudaSuccess)
+                    return cuda_fail(e, "cudaEventCreate");
+                r->events.push_back(x);
+            }
+        r->event_frames.resize(r->events.size() / 4);
+        r->event_frames[r->events_used / 4] = n_frames;
+        ev = &r->events[r->events_used];
+        r->events_used += 4;
+        r->timed_launches += 2;
+        cudaEventRecord(ev[0], stream);
+    }
+    e = cudaMemsetAsync(base, 0xfe, l.key_bytes, stream);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaMemsetAsync");
+    if (ev)
+        cudaEventRecord(ev[1], stream);
+    e = launch_batch(r->last, infos[0].mode, stream, ev ? ev[2] : nullptr);
+    if (ev)
+        cudaEventRecord(ev[3], stream);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "kernel launch");
+    r->has_frame = true;
+    return ISTI_OK;
 }
 } // namespace
 
@@ -547,172 +931,20 @@ isti_status isti_renderer_destroy(isti_renderer *r)
     return s;
 }
 
-isti_status isti_render(isti_renderer *r, void *out_rgba, const isti_render_info *info, const isti_frame_data *frame, void *stream_ptr)
+isti_status isti_render(isti_renderer *r, void *out_rgba, const isti_render_info *info, const isti_frame_data *frame, void *stream)
 {
     if (!r || !out_rgba || !info || !frame)
         return fail(ISTI_ERR_INVALID_ARG, "NULL argument");
-    if (reinterpret_cast<uintptr_t>(out_rgba) & 3u)
-        return fail(ISTI_ERR_INVALID_ARG, "out_rgba must be 4-byte aligned");
-    if (info->mode == ISTI_MODE_TIMEWARP)
-        return fail(ISTI_ERR_UNSUPPORTED, "timewarp mode is not implemented");
-    if (info->mode < 0 || info->mode > ISTI_MODE_TIMEWARP)
-        return fail(ISTI_ERR_INVALID_ARG, "unknown render mode");
-    if (info->shadow_frames_per_anchor < 0 || info->shadow_frames_per_anchor > 16)
-        return fail(ISTI_ERR_INVALID_ARG, "shadow_frames_per_anchor must be 0..16");
-    std::string why;
-    if (!view_ok(frame->fwd, why) || !view_ok(frame->bwd, why))
-        return fail(ISTI_ERR_INVALID_ARG, why);
-    if (frame->fwd.width != info->width || frame->fwd.height != info->height || frame->bwd.width != info->width ||
-        frame->bwd.height != info->height)
-        return fail(ISTI_ERR_INVALID_ARG, "render resolution must equal the main keyframes' resolution");
-    const int n_aux = frame->num_aux;
-    if (n_aux < 0 || n_aux > ISTI_MAX_AUX_CAMS)
-        return fail(ISTI_ERR_INVALID_ARG, "num_aux out of range");
-    if (n_aux > 0 && (!frame->aux_curr || !frame->aux_next))
-        return fail(ISTI_ERR_INVALID_ARG, "aux views are NULL");
-    for (int i = 0; i < n_aux; i++)
-    {
-        const isti_view &a = frame->aux_curr[i], &b = frame->aux_next[i];
-        if (!view_ok(a, why) || !view_ok(b, why))
-            return fail(ISTI_ERR_INVALID_ARG, why);
-        if (a.width != b.width || a.height != b.height)
-            return fail(ISTI_ERR_INVALID_ARG, "aux curr/next sizes differ");
-        // aux_idx = idx / (res / aux_res) must stay inside the aux image (src/renderer.cu:425,433)
-        if (a.width > info->width || a.height > info->height || (info->width - 1) / (info->width / a.width) >= a.width ||
-            (info->height - 1) / (info->height / a.height) >= a.height)
-            return fail(ISTI_ERR_INVALID_ARG, "aux resolution incompatible with the render resolution");
-    }
+    void *outs[1] = {out_rgba};
+    return render_batch(r, 1, outs, info, frame, false, static_cast<cudaStream_t>(stream));
+}
 
-    const int n_views = 2 + 2 * n_aux;
-    const isti_view *views[isti::MAX_VIEWS];
-    views[0] = &frame->fwd;
-    views[1] = &frame->bwd;
-    for (int i = 0; i < n_aux; i++)
-    {
-        views[2 + 2 * i] = &frame->aux_curr[i];
-        views[3 + 2 * i] = &frame->aux_next[i];
-    }
-    size_t key_bytes = 0, ff_bytes = 0;
-    size_t px[isti::MAX_VIEWS];
-    for (int k = 0; k < n_views; k++)
-    {
-        px[k] = (size_t)views[k]->width * views[k]->height;
-        key_bytes += align_up(px[k] * 8, 256);
-        ff_bytes += align_up(px[k] * 16, 256);
-    }
-    const size_t need = key_bytes + 2 * ff_bytes;
-
-    int cur = 0;
-    cudaError_t e = cudaGetDevice(&cur);
-    if (e != cudaSuccess)
-        return cuda_fail(e, "cudaGetDevice");
-    if (cur != r->device)
-        return fail(ISTI_ERR_INVALID_ARG, "renderer was created on another device");
-    if (need > r->arena_bytes)
-    {
-        if (r->arena)
-        {
-            e = cudaFree(r->arena);
-            r->arena = nullptr;
-            r->arena_bytes = 0;
-            if (e != cudaSuccess)
-                return cuda_fail(e, "cudaFree");
-        }
-        e = cudaMalloc(&r->arena, need);
-        if (e != cudaSuccess)
-        {
-            r->arena = nullptr;
-            return e == cudaErrorMemoryAllocation ? fail(ISTI_ERR_OOM, "cudaMalloc of the renderer arena failed") : cuda_fail(e, "cudaMalloc");
-        }
-        r->arena_bytes = need;
-    }
-
-    isti::FrameParams &p = r->last;
-    std::memset(&p, 0, sizeof p);
-    char *base = static_cast<char *>(r->arena);
-    size_t off_key = 0, off_cam = key_bytes, off_full = key_bytes + ff_bytes;
-    const float alpha = info->alpha;
-    const float one_minus_alpha = 1.0f - alpha;
-    uint32_t max_w = 0, max_h = 0;
-    for (int k = 0; k < n_views; k++)
-    {
-        const bool fw = (k % 2) == 0;
-        const isti_view &v = *views[k];
-        const float *vp_to = (k < 2) ? (fw ? frame->bwd.viewproj : frame->fwd.viewproj)
-                                     : (fw ? frame->aux_next[(k - 2) / 2].viewproj : frame->aux_curr[(k - 2) / 2].viewproj);
-        const float *vp_main = fw ? frame->fwd.viewproj : frame->bwd.viewproj;
-        const int prio = (k < 2 || !frame->aux_priority) ? 0 : frame->aux_priority[(k - 2) / 2];
-        fill_view(p.v[k], v, fw ? 1 : 0, prio, fw ? alpha : one_minus_alpha, vp_to, vp_main);
-        p.v[k].splat = reinterpret_cast<unsigned long long *>(base + off_key);
-        p.v[k].cam_ff = reinterpret_cast<float4 *>(base + off_cam);
-        p.v[k].full_ff = reinterpret_cast<float4 *>(base + off_full);
-        off_key += align_up(px[k] * 8, 256);
-        off_cam += align_up(px[k] * 16, 256);
-        off_full += align_up(px[k] * 16, 256);
-        max_w = v.width > max_w ? v.width : max_w;
-        max_h = v.height > max_h ? v.height : max_h;
-    }
-    std::memcpy(p.cam_vp, info->viewproj, sizeof p.cam_vp);
-    p.out = static_cast<uint32_t *>(out_rgba);
-    p.out_w = info->width;
-    p.out_h = info->height;
-    p.alpha = alpha;
-    p.n_views = n_views;
-    p.n_aux = n_aux;
-    p.fpa = info->frames_per_anchor;
-    p.sfpa = info->shadow_frames_per_anchor;
-    p.no_shadows = info->no_shadows ? 1 : 0;
-    p.linear = info->mode == ISTI_MODE_BACKWARD_BIDIRECTIONAL ? 1 : 0;
-
-    cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
-    cudaEvent_t *ev = nullptr;
-    if (r->timing)
-    {
-        if (r->events_used + 4 > r->events.size())
-            for (int i = 0; i < 4; i++)
-            {
-                cudaEvent_t x;
-                e = cudaEventCreate(&x);
-                if (e != cudaSuccess)
-                    return cuda_fail(e, "cudaEventCreate");
-                r->events.push_back(x);
-            }
-        ev = &r->events[r->events_used];
-        r->events_used += 4;
-        r->timed_launches += 2;
-        cudaEventRecord(ev[0], stream);
-    }
-    e = cudaMemsetAsync(base, 0xfe, key_bytes, stream);
-    if (e != cudaSuccess)
-        return cuda_fail(e, "cudaMemsetAsync");
-    if (ev)
-        cudaEventRecord(ev[1], stream);
-    const dim3 blk(32, 8);
-    const dim3 gs((max_w + 31) / 32, (max_h + 7) / 8, n_views);
-    isti::splat_kernel<<<gs, blk, 0, stream>>>(p);
-    if (ev)
-        cudaEventRecord(ev[2], stream);
-    const dim3 gr((info->width + 31) / 32, (info->height + 7) / 8);
-    switch (info->mode)
-    {
-    case ISTI_MODE_OURS:
-    case ISTI_MODE_BACKWARD_UNIDIRECTIONAL:
-        isti::reproj_kernel<1, 3, false><<<gr, blk, 0, stream>>>(p);
-        break;
-    case ISTI_MODE_SPLATTING:
-        isti::reproj_kernel<1, 0, false><<<gr, blk, 0, stream>>>(p);
-        break;
-    case ISTI_MODE_BACKWARD_BIDIRECTIONAL:
-        isti::reproj_kernel<3, 5, true><<<gr, blk, 0, stream>>>(p);
-        break;
-    }
-    if (ev)
-        cudaEventRecord(ev[3], stream);
-    e = cudaGetLastError();
-    if (e != cudaSuccess)
-        return cuda_fail(e, "kernel launch");
-    r->has_frame = true;
-    return ISTI_OK;
+isti_status isti_render_batch(isti_renderer *r, int32_t n_frames, void *const *out_rgba, const isti_render_info *infos,
+                              const isti_frame_data *frame, int32_t chain_outputs, void *stream)
+{
+    if (!r || !out_rgba || !infos || !frame)
+        return fail(ISTI_ERR_INVALID_ARG, "NULL argument");
+    return render_batch(r, n_frames, out_rgba, infos, frame, chain_outputs != 0, static_cast<cudaStream_t>(stream));
 }
 
 isti_status isti_renderer_enable_timing(isti_renderer *r, int32_t on)
@@ -740,7 +972,7 @@ isti_status isti_renderer_timing(isti_renderer *r, isti_timing *out)
         out->init_ms += a;
         out->splat_ms += b;
         out->reproj_ms += c;
-        out->frames += 1;
+        out->frames += r->event_frames[i / 4];
     }
     out->kernel_launches = r->timed_launches;
     r->events_used = 0;
@@ -753,13 +985,15 @@ isti_status isti_renderer_view_buffers(const isti_renderer *r, int32_t view, con
 {
     if (!r || !r->has_frame)
         return fail(ISTI_ERR_INVALID_ARG, "no frame rendered yet");
-    if (view < 0 || view >= r->last.n_views)
+    const int nv = r->last.n_views;
+    if (view < 0 || view >= nv * r->last.n_frames)
         return fail(ISTI_ERR_INVALID_ARG, "view index out of range");
-    const isti::DevView &d = r->last.v[view];
+    const int k = view / nv;
+    const isti::DevView &d = r->last.v[view % nv];
     if (splat)
-        *splat = reinterpret_cast<const uint64_t *>(d.splat);
+        *splat = reinterpret_cast<const uint64_t *>(d.splat + k * r->last.key_stride);
     if (cam_ff)
-        *cam_ff = reinterpret_cast<const float *>(d.cam_ff);
+        *cam_ff = reinterpret_cast<const float *>(d.cam_ff + k * r->last.cam_stride);
     if (full_ff)
         *full_ff = reinterpret_cast<const float *>(d.full_ff);
     if (width)
@@ -776,8 +1010,8 @@ isti_status isti_renderer_view_buffers(const isti_renderer *r, int32_t view, con
 // isti_render_noalloc serves callers that may not allocate device memory while
 // they run (a host whose device budget is reserved up front by its own pool, a
 // real-time loop where cudaMalloc/cudaFree can synchronise the device).  Its
-// splat keys and flow fields live in g_noalloc_scratch below instead of a
-// renderer arena; the kernels are the ones isti_render launches.
+// intermediates live in g_noalloc_scratch below instead of a renderer arena;
+// the kernels are the ones isti_render launches.
 
 namespace
 {
@@ -814,128 +1048,34 @@ extern "C" isti_status isti_render_noalloc(void *out_rgba, const isti_render_inf
 {
     if (!out_rgba || !info || !frame)
         return fail(ISTI_ERR_INVALID_ARG, "NULL argument");
-    if (reinterpret_cast<uintptr_t>(out_rgba) & 3u)
-        return fail(ISTI_ERR_INVALID_ARG, "out_rgba must be 4-byte aligned");
-    if (info->mode == ISTI_MODE_TIMEWARP)
-        return fail(ISTI_ERR_UNSUPPORTED, "timewarp mode is not implemented");
-    if (info->mode < 0 || info->mode > ISTI_MODE_TIMEWARP)
-        return fail(ISTI_ERR_INVALID_ARG, "unknown render mode");
-    if (info->shadow_frames_per_anchor < 0 || info->shadow_frames_per_anchor > 16)
-        return fail(ISTI_ERR_INVALID_ARG, "shadow_frames_per_anchor must be 0..16");
-    std::string why;
-    if (!view_ok(frame->fwd, why) || !view_ok(frame->bwd, why))
-        return fail(ISTI_ERR_INVALID_ARG, why);
-    if (frame->fwd.width != info->width || frame->fwd.height != info->height || frame->bwd.width != info->width ||
-        frame->bwd.height != info->height)
-        return fail(ISTI_ERR_INVALID_ARG, "render resolution must equal the main keyframes' resolution");
-    const int n_aux = frame->num_aux;
-    if (n_aux < 0 || n_aux > ISTI_MAX_AUX_CAMS)
-        return fail(ISTI_ERR_INVALID_ARG, "num_aux out of range");
-    if (n_aux > 0 && (!frame->aux_curr || !frame->aux_next))
-        return fail(ISTI_ERR_INVALID_ARG, "aux views are NULL");
-    for (int i = 0; i < n_aux; i++)
-    {
-        const isti_view &a = frame->aux_curr[i], &b = frame->aux_next[i];
-        if (!view_ok(a, why) || !view_ok(b, why))
-            return fail(ISTI_ERR_INVALID_ARG, why);
-        if (a.width != b.width || a.height != b.height)
-            return fail(ISTI_ERR_INVALID_ARG, "aux curr/next sizes differ");
-        if (a.width > info->width || a.height > info->height || (info->width - 1) / (info->width / a.width) >= a.width ||
-            (info->height - 1) / (info->height / a.height) >= a.height)
-            return fail(ISTI_ERR_INVALID_ARG, "aux resolution incompatible with the render resolution");
-    }
-
-    const int n_views = 2 + 2 * n_aux;
+    void *outs[1] = {out_rgba};
     const isti_view *views[isti::MAX_VIEWS];
-    views[0] = &frame->fwd;
-    views[1] = &frame->bwd;
-    for (int i = 0; i < n_aux; i++)
-    {
-        views[2 + 2 * i] = &frame->aux_curr[i];
-        views[3 + 2 * i] = &frame->aux_next[i];
-    }
-    size_t key_bytes = 0, ff_bytes = 0, px[isti::MAX_VIEWS];
-    for (int k = 0; k < n_views; k++)
-    {
-        px[k] = (size_t)views[k]->width * views[k]->height;
-        key_bytes += align_up(px[k] * 8, 256);
-        ff_bytes += align_up(px[k] * 16, 256);
-    }
-    const size_t need = key_bytes + 2 * ff_bytes;
-    if (need > ISTI_NOALLOC_SCRATCH_BYTES)
-        return fail(ISTI_ERR_INVALID_ARG, "frame needs " + std::to_string(need) + " bytes of scratch; isti_render_noalloc holds at most " +
+    int n_views = 0;
+    isti_status st = validate(1, outs, info, frame, views, n_views);
+    if (st != ISTI_OK)
+        return st;
+    const Layout l = layout_of(views, n_views, 1);
+    if (l.total > ISTI_NOALLOC_SCRATCH_BYTES)
+        return fail(ISTI_ERR_INVALID_ARG, "frame needs " + std::to_string(l.total) + " bytes of scratch; isti_render_noalloc holds at most " +
                                               std::to_string((size_t)ISTI_NOALLOC_SCRATCH_BYTES) + " (use isti_render for larger frames)");
-
     int device = 0;
     cudaError_t e = cudaGetDevice(&device);
     if (e != cudaSuccess)
         return cuda_fail(e, "cudaGetDevice");
     char *base = nullptr;
-    isti_status st = noalloc_scratch(device, &base);
+    st = noalloc_scratch(device, &base);
     if (st != ISTI_OK)
         return st;
-
     isti::FrameParams p;
-    std::memset(&p, 0, sizeof p);
-    size_t off_key = 0, off_cam = key_bytes, off_full = key_bytes + ff_bytes;
-    const float alpha = info->alpha;
-    const float one_minus_alpha = 1.0f - alpha;
-    uint32_t max_w = 0, max_h = 0;
-    for (int k = 0; k < n_views; k++)
-    {
-        const bool fw = (k % 2) == 0;
-        const isti_view &v = *views[k];
-        const float *vp_to = (k < 2) ? (fw ? frame->bwd.viewproj : frame->fwd.viewproj)
-                                     : (fw ? frame->aux_next[(k - 2) / 2].viewproj : frame->aux_curr[(k - 2) / 2].viewproj);
-        const float *vp_main = fw ? frame->fwd.viewproj : frame->bwd.viewproj;
-        const int prio = (k < 2 || !frame->aux_priority) ? 0 : frame->aux_priority[(k - 2) / 2];
-        fill_view(p.v[k], v, fw ? 1 : 0, prio, fw ? alpha : one_minus_alpha, vp_to, vp_main);
-        p.v[k].splat = reinterpret_cast<unsigned long long *>(base + off_key);
-        p.v[k].cam_ff = reinterpret_cast<float4 *>(base + off_cam);
-        p.v[k].full_ff = reinterpret_cast<float4 *>(base + off_full);
-        off_key += align_up(px[k] * 8, 256);
-        off_cam += align_up(px[k] * 16, 256);
-        off_full += align_up(px[k] * 16, 256);
-        max_w = v.width > max_w ? v.width : max_w;
-        max_h = v.height > max_h ? v.height : max_h;
-    }
-    std::memcpy(p.cam_vp, info->viewproj, sizeof p.cam_vp);
-    p.out = static_cast<uint32_t *>(out_rgba);
-    p.out_w = info->width;
-    p.out_h = info->height;
-    p.alpha = alpha;
-    p.n_views = n_views;
-    p.n_aux = n_aux;
-    p.fpa = info->frames_per_anchor;
-    p.sfpa = info->shadow_frames_per_anchor;
-    p.no_shadows = info->no_shadows ? 1 : 0;
-    p.linear = info->mode == ISTI_MODE_BACKWARD_BIDIRECTIONAL ? 1 : 0;
-
+    fill_params(p, 1, outs, info, frame, views, n_views, l, base, false);
     // The array keeps the previous call's contents: every key starts as the
-    // reference's empty value (all bytes 0xfe); the flow fields are fully
-    // rewritten by the splat kernel before the reprojection reads them.
+    // reference's empty value (all bytes 0xfe); flow fields and tables are fully
+    // rewritten by the splat launch before the reprojection reads them.
     cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
-    e = cudaMemsetAsync(base, 0xfe, key_bytes, stream);
+    e = cudaMemsetAsync(base, 0xfe, l.key_bytes, stream);
     if (e != cudaSuccess)
         return cuda_fail(e, "cudaMemsetAsync");
-    const dim3 blk(32, 8);
-    const dim3 gs((max_w + 31) / 32, (max_h + 7) / 8, n_views);
-    isti::splat_kernel<<<gs, blk, 0, stream>>>(p);
-    const dim3 gr((info->width + 31) / 32, (info->height + 7) / 8);
-    switch (info->mode)
-    {
-    case ISTI_MODE_OURS:
-    case ISTI_MODE_BACKWARD_UNIDIRECTIONAL:
-        isti::reproj_kernel<1, 3, false><<<gr, blk, 0, stream>>>(p);
-        break;
-    case ISTI_MODE_SPLATTING:
-        isti::reproj_kernel<1, 0, false><<<gr, blk, 0, stream>>>(p);
-        break;
-    case ISTI_MODE_BACKWARD_BIDIRECTIONAL:
-        isti::reproj_kernel<3, 5, true><<<gr, blk, 0, stream>>>(p);
-        break;
-    }
-    e = cudaGetLastError();
+    e = launch_batch(p, info->mode, stream, nullptr);
     if (e != cudaSuccess)
         return cuda_fail(e, "kernel launch");
     return ISTI_OK;

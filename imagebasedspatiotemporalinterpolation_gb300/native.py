@@ -77,7 +77,11 @@ SIGNATURES = {
     "isti_renderer_enable_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "isti_renderer_timing": (C.c_int, [C.c_void_p, C.POINTER(IstiTiming)]),
     "isti_render_noalloc": (C.c_int, [C.c_void_p, C.POINTER(IstiRenderInfo), C.POINTER(IstiFrameData), C.c_void_p]),
+    "isti_render_batch": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(IstiRenderInfo),
+                                    C.POINTER(IstiFrameData), C.c_int32, C.c_void_p]),
 }
+
+MAX_BATCH_FRAMES = 8  # ISTI_MAX_BATCH_FRAMES
 
 NOALLOC_SCRATCH_BYTES = 64 << 20  # ISTI_NOALLOC_SCRATCH_BYTES
 

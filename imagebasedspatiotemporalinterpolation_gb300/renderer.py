@@ -174,6 +174,23 @@ class Renderer:
         s = (stream or torch.cuda.current_stream()).cuda_stream
         check(self._lib.isti_render(self._h, _dptr(render_buffer), C.byref(ri), C.byref(frame_data.to_c()), C.c_void_p(s)))
 
+    def render_batch(self, render_buffers, infos, frame_data: DeviceFrame, chain: bool = True, stream=None) -> None:
+        """Render len(infos) client frames of one keyframe pair in one launch pair
+        (isti_render_batch).  With chain=True the result equals rendering the
+        frames in order into one persistent buffer that starts as
+        render_buffers[0] and is copied to render_buffers[k] after frame k."""
+        torch = _torch()
+        n = len(infos)
+        if n != len(render_buffers) or not 1 <= n <= native.MAX_BATCH_FRAMES:
+            raise ValueError(f"need 1..{native.MAX_BATCH_FRAMES} frames and one buffer per frame")
+        ris = (IstiRenderInfo * n)(*[i if isinstance(i, IstiRenderInfo) else render_info(i) for i in infos])
+        for b in render_buffers:
+            if tuple(b.shape) != (ris[0].height, ris[0].width, 4) or b.dtype != torch.uint8:
+                raise ValueError("render buffers must be (H, W, 4) uint8 tensors of the render resolution")
+        outs = (C.c_void_p * n)(*[_dptr(b) for b in render_buffers])
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        check(self._lib.isti_render_batch(self._h, n, outs, ris, C.byref(frame_data.to_c()), int(chain), C.c_void_p(s)))
+
     def enable_timing(self, on: bool = True) -> None:
         check(self._lib.isti_renderer_enable_timing(self._h, int(on)))
 

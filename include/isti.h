@@ -134,12 +134,30 @@ isti_status isti_renderer_destroy(isti_renderer *r);
 isti_status isti_render(isti_renderer *r, void *out_rgba, const isti_render_info *info, const isti_frame_data *frame,
                         void *stream);
 
-/* Device pointers to the intermediates of the last isti_render call for view
- * `view` (0 fwd, 1 bwd, 2+2i aux i curr, 3+2i aux i next): 64-bit splat keys
+/* Renders n_frames client frames of one keyframe pair (several t values or
+ * eyes) with one splat launch and one reprojection launch (no counterpart in
+ * the reference, which renders frame by frame, src/main.cu:152-190).  Frame k
+ * uses infos[k] (same width, height and mode for all k) and writes
+ * out_rgba[k].  The result equals n_frames isti_render calls in order:
+ *  - chain_outputs == 0: each out_rgba[k] is updated in place like a
+ *    separate isti_render call on that buffer;
+ *  - chain_outputs != 0: as if all frames went into one persistent buffer
+ *    that starts as out_rgba[0]'s content and is copied to out_rgba[k] after
+ *    frame k (out_rgba[k], k >= 1, is fully overwritten).
+ * The work that does not depend on the client camera (world positions,
+ * keyframe-to-keyframe flow) is done once for all frames.
+ * 1 <= n_frames <= ISTI_MAX_BATCH_FRAMES. */
+#define ISTI_MAX_BATCH_FRAMES 8
+isti_status isti_render_batch(isti_renderer *r, int32_t n_frames, void *const *out_rgba, const isti_render_info *infos,
+                              const isti_frame_data *frame, int32_t chain_outputs, void *stream);
+
+/* Device pointers to the intermediates of the last render call for view
+ * `view` (0 fwd, 1 bwd, 2+2i aux i curr, 3+2i aux i next; after a batch,
+ * frame k's views follow at k * (2 + 2 * num_aux)): 64-bit splat keys
  * (depth bits << 32 | x << 16 | y), f32x4 source->client flow and f32x4
- * source->other-keyframe flow, each width*height elements.  A field that is
- * not materialised is returned as NULL.  Valid until the next render or
- * destroy. */
+ * source->other-keyframe flow (shared by the frames of a batch), each
+ * width*height elements.  A field that is not materialised is returned as
+ * NULL.  Valid until the next render or destroy. */
 isti_status isti_renderer_view_buffers(const isti_renderer *r, int32_t view, const uint64_t **splat, const float **cam_ff,
                                        const float **full_ff, uint32_t *width, uint32_t *height);
 

@@ -164,3 +164,51 @@ def test_invalid_arguments_are_rejected(cuda):
     with pytest.raises(native.IstiError):
         r.render(out, big.client(0, 1), DeviceFrame.from_host(big.frame(0)))
     r.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1, 3])
+def test_batch_equals_sequential_renders(cuda, mode):
+    """isti_render_batch == isti_render frame by frame (chained: one persistent buffer)."""
+    import torch
+    seq = Sequence(480, 270, 2, seed=909 + mode, aux_offsets=(-0.3, 0.3), shadows=True, max_speed=3.0)
+    frame = DeviceFrame.from_host(seq.frame(0))
+    clients = [seq.client(0, b, mode=mode) for b in (0, 1, 2, 3)] + [seq.client(0, 0, mode=mode, alpha=a) for a in (0.6, 1.0)]
+    g = torch.Generator().manual_seed(mode)
+    prev = torch.randint(0, 256, (270, 480, 4), dtype=torch.uint8, generator=g).cuda()
+    nv = len(frame.views())
+    r = Renderer()
+    buf, snaps, keys = prev.clone(), [], []
+    for c in clients:
+        r.render(buf, c, frame)
+        snaps.append(buf.clone())
+        keys.append([r.view_buffers(v)[0] for v in range(nv)])
+    outs = [prev.clone()] + [torch.zeros_like(prev) for _ in clients[1:]]
+    r.render_batch(outs, clients, frame, chain=True)
+    torch.cuda.synchronize()
+    for k in range(len(clients)):
+        assert torch.equal(outs[k], snaps[k]), f"chained frame {k} differs"
+        for v in range(nv):
+            assert torch.equal(r.view_buffers(k * nv + v)[0], keys[k][v]), f"frame {k} view {v} keys differ"
+    outs = [prev.clone() for _ in clients]
+    r.render_batch(outs, clients, frame, chain=False)
+    for k, c in enumerate(clients):
+        single = prev.clone()
+        r.render(single, c, frame)
+        assert torch.equal(outs[k], single), f"unchained frame {k} differs"
+    r.close()
+
+
+def test_batch_limits(cuda):
+    import torch
+    seq = Sequence(64, 36, 2, seed=11)
+    frame = DeviceFrame.from_host(seq.frame(0))
+    r = Renderer()
+    bufs = [torch.zeros((36, 64, 4), dtype=torch.uint8, device="cuda") for _ in range(9)]
+    clients = [seq.client(0, b % 4) for b in range(9)]
+    r.render_batch(bufs[:8], clients[:8], frame)
+    with pytest.raises(ValueError):
+        r.render_batch(bufs, clients, frame)
+    mixed = [seq.client(0, 1), seq.client(0, 2, mode=3)]
+    with pytest.raises(native.IstiError):
+        r.render_batch(bufs[:2], mixed, frame)
+    r.close()
