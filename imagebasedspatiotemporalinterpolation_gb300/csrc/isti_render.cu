@@ -441,129 +441,151 @@ __device__ __forceinline__ bool resolve_pixel(const DirRes *res, int lane, const
 }
 
 // bidirectionalReprojection_kernel<SW, SI, MAIN_ALWAYS_VALID>, src/renderer.cu:400-465
-// block = (32, n_views): 32 output pixels of row blockIdx.y, one warp per source view,
-// looping over the frames of the batch.
+// block = (32, n_views): 32 output pixels of row blockIdx.y, one warp per source view.
+//  phase 1: each warp runs its view for every frame of the batch (window, search, error);
+//  phase 2: warp w resolves frames w, w + n_views, ... (camera choice and colour);
+//  phase 3: outputs are written (chained: frame k keeps frame k-1's pixel where invalid).
 template <int SW, int SI, bool MAV>
 __global__ void __launch_bounds__(32 * MAX_VIEWS) reproj_kernel(const __grid_constant__ FrameParams p)
 {
     using T = Tile<SW>;
     extern __shared__ __align__(16) unsigned char smem[];
-    const int nv = p.n_views;
-    DirRes *res2 = reinterpret_cast<DirRes *>(smem);                    // [2][nv][32], double-buffered over frames
-    uint32_t *chain = reinterpret_cast<uint32_t *>(res2 + 2 * nv * 32); // [32] running output when chaining
-    unsigned long long *tiles = reinterpret_cast<unsigned long long *>(chain + 32);
+    const int nv = p.n_views, nf = p.n_frames;
+    DirRes *res = reinterpret_cast<DirRes *>(smem);                      // [nf][nv][32]
+    uint32_t *cols = reinterpret_cast<uint32_t *>(res + nf * nv * 32);   // [nf][32] colour, bit-packed validity below
+    uint32_t *valid = cols + nf * 32;                                    // [nf][32]
+    unsigned long long *tiles = reinterpret_cast<unsigned long long *>(valid + nf * 32);
 
     const int lane = threadIdx.x, vw = threadIdx.y;
     const uint32_t x0 = blockIdx.x * 32, x = x0 + lane, y = blockIdx.y;
-    const DevView &v = p.v[vw];
-    const uint32_t ix = v.sx == 1 ? x : x / v.sx, iy = v.sy == 1 ? y : y / v.sy, tx0 = v.sx == 1 ? x0 : x0 / v.sx;
-    const bool fwd = (vw & 1) == 0;
-    unsigned long long *tile = tiles + vw * (T::H * T::W);
-    const int cx = (int)(ix - tx0) + SW;
-    const float qx = __ldg(p.v[0].lut + min(x, p.out_w - 1)), qy = __ldg(p.v[0].lut + p.v[0].w + y); // pixel2CS(idx, res)
-    const float pcx = __ldg(v.lut + min(ix, v.w - 1)), pcy = __ldg(v.lut + v.w + iy);              // pixel2CS in this view
-
-    for (int k = 0; k < p.n_frames; k++)
     {
-        const unsigned long long *keys = v.splat + k * p.key_stride;
-        const float4 *cam = v.cam_ff + k * p.cam_stride;
-        // splat keys around this warp's pixels (initializeSearchFromSplatting<SW>, src/renderer.cu:148-175);
-        // a key outside the view reads as 0 (depth +0.0), which the window never selects, exactly like the
-        // reference's skipped out-of-range neighbours
-#pragma unroll
-        for (int r = 0; r < T::H; r++)
+        const DevView &v = p.v[vw];
+        const uint32_t ix = v.sx == 1 ? x : x / v.sx, iy = v.sy == 1 ? y : y / v.sy, tx0 = v.sx == 1 ? x0 : x0 / v.sx;
+        const bool fwd = (vw & 1) == 0;
+        unsigned long long *tile = tiles + vw * (T::H * T::W);
+        const int cx = (int)(ix - tx0) + SW;
+#pragma unroll 1
+        for (int k = 0; k < nf; k++)
         {
-            const int gy = (int)iy - SW + r;
-            const bool row_ok = gy >= 0 && gy < (int)v.h;
-            for (int c = lane; c < T::W; c += 32)
+            const unsigned long long *keys = v.splat + k * p.key_stride;
+            // splat keys around this warp's pixels (initializeSearchFromSplatting<SW>, src/renderer.cu:148-175);
+            // a key outside the view reads as 0 (depth +0.0), which the window never selects, exactly like
+            // the reference's skipped out-of-range neighbours
+            if (k > 0)
+                __syncwarp();
+#pragma unroll
+            for (int r = 0; r < T::H; r++)
             {
-                const int gx = (int)tx0 - SW + c;
-                tile[r * T::W + c] = (row_ok && gx >= 0 && gx < (int)v.w) ? __ldg(keys + (size_t)gy * v.w + gx) : 0ull;
+                const int gy = (int)iy - SW + r;
+                const bool row_ok = gy >= 0 && gy < (int)v.h;
+                for (int c = lane; c < T::W; c += 32)
+                {
+                    const int gx = (int)tx0 - SW + c;
+                    tile[r * T::W + c] = (row_ok && gx >= 0 && gx < (int)v.w) ? __ldg(keys + (size_t)gy * v.w + gx) : 0ull;
+                }
             }
-        }
-        __syncwarp();
+            __syncwarp();
 
-        DirRes d;
-        d.error = FLT_MAX_F;
-        d.depth = 0.0f;
-        d.src = 0;
-        d.vis = 0;
-        if (x < p.out_w)
-        {
-            KeyInfo lowest = decode_key(tile[SW * T::W + cx]);
-#pragma unroll
-            for (int yo = -SW; yo <= SW; yo++)
-#pragma unroll
-                for (int xo = -SW; xo <= SW; xo++)
-                {
-                    const KeyInfo cur = decode_key(tile[(SW + yo) * T::W + cx + xo]);
-                    if (cur.depth > 0.0f && (!isfinite(lowest.depth) || lowest.depth < 0.0f || cur.depth < lowest.depth))
-                        lowest = cur;
-                }
-            uint32_t ssx = lowest.sx, ssy = lowest.sy;
-            d.depth = lowest.depth;
-            if (lowest.depth > 0.0f && (!fwd || p.f[k].alpha < 1.0f))
+            DirRes d;
+            d.error = FLT_MAX_F;
+            d.depth = 0.0f;
+            d.src = 0;
+            d.vis = 0;
+            if (x < p.out_w)
             {
-                // iterativeSearch<SI>, src/renderer.cu:177-202.  The start is a splatted source pixel
-                // and every accepted step is in range, so no border handling is needed.
+                KeyInfo lowest = decode_key(tile[SW * T::W + cx]);
 #pragma unroll
-                for (int i = 0; i < SI; i++)
-                {
-                    const float4 m = __ldg(cam + (size_t)ssy * v.w + ssx);
-                    const int2 t = cs2pixel(__fsub_rn(qx, m.x), __fsub_rn(qy, m.y), v.w, v.h);
-                    if (in_range(t, v.w, v.h))
+                for (int yo = -SW; yo <= SW; yo++)
+#pragma unroll
+                    for (int xo = -SW; xo <= SW; xo++)
                     {
-                        ssx = (uint32_t)t.x;
-                        ssy = (uint32_t)t.y;
+                        const KeyInfo cur = decode_key(tile[(SW + yo) * T::W + cx + xo]);
+                        if (cur.depth > 0.0f && (!isfinite(lowest.depth) || lowest.depth < 0.0f || cur.depth < lowest.depth))
+                            lowest = cur;
                     }
+                uint32_t ssx = lowest.sx, ssy = lowest.sy;
+                d.depth = lowest.depth;
+                if (lowest.depth > 0.0f && (!fwd || p.f[k].alpha < 1.0f))
+                {
+                    // iterativeSearch<SI>, src/renderer.cu:177-202.  The start is a splatted source pixel
+                    // and every accepted step is in range, so no border handling is needed.
+                    const float4 *cam = v.cam_ff + k * p.cam_stride;
+                    const float qx = __ldg(p.v[0].lut + x), qy = __ldg(p.v[0].lut + p.v[0].w + y); // pixel2CS(idx, res)
+#pragma unroll
+                    for (int i = 0; i < SI; i++)
+                    {
+                        const float4 m = __ldg(cam + (size_t)ssy * v.w + ssx);
+                        const int2 t = cs2pixel(__fsub_rn(qx, m.x), __fsub_rn(qy, m.y), v.w, v.h);
+                        if (in_range(t, v.w, v.h))
+                        {
+                            ssx = (uint32_t)t.x;
+                            ssy = (uint32_t)t.y;
+                        }
+                    }
+                    const size_t si = (size_t)ssy * v.w + ssx;
+                    const float4 m = __ldg(cam + si);
+                    d.depth = z_to_depth(__fadd_rn(__ldg(v.z + si), m.z));
+                    // computeReprojError, src/renderer.cu:204-215 (pixelCS of the output pixel in this view)
+                    const float pcx = __ldg(v.lut + ix), pcy = __ldg(v.lut + v.w + iy);
+                    const float pfx = __ldg(v.lut + ssx), pfy = __ldg(v.lut + v.w + ssy);
+                    float ex = __fsub_rn(__fadd_rn(pfx, m.x), pcx);
+                    float ey = __fsub_rn(__fadd_rn(pfy, m.y), pcy);
+                    ex = __fmul_rn(ex, v.err_sx);
+                    ey = __fmul_rn(ey, v.err_sy);
+                    d.error = __fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)));
+                    d.vis = m.w > 0.0f;
                 }
-                const size_t si = (size_t)ssy * v.w + ssx;
-                const float4 m = __ldg(cam + si);
-                d.depth = z_to_depth(__fadd_rn(__ldg(v.z + si), m.z));
-                // computeReprojError, src/renderer.cu:204-215
-                const float pfx = __ldg(v.lut + ssx), pfy = __ldg(v.lut + v.w + ssy);
-                float ex = __fsub_rn(__fadd_rn(pfx, m.x), pcx);
-                float ey = __fsub_rn(__fadd_rn(pfy, m.y), pcy);
-                ex = __fmul_rn(ex, v.err_sx);
-                ey = __fmul_rn(ey, v.err_sy);
-                d.error = __fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)));
-                d.vis = m.w > 0.0f;
+                d.src = (ssx << 16) | ssy;
             }
-            d.src = (ssx << 16) | ssy;
+            res[(k * nv + vw) * 32 + lane] = d;
         }
-        DirRes *res = res2 + (k & 1) * nv * 32;
-        res[vw * 32 + lane] = d;
-        __syncthreads();
-        // The choice and colour of frame k run on warp k % nv while the other warps go
-        // on with frame k + 1 (double-buffered results).  The barrier of the next frame
-        // orders the running output of the chain from frame k to frame k + 1.
-        if (vw == k % nv && x < p.out_w)
+    }
+    __syncthreads();
+
+    const bool px_ok = x < p.out_w;
+#pragma unroll 1
+    for (int k = vw; k < nf; k += nv)
+    {
+        uint32_t color = 0;
+        const bool ok = px_ok && resolve_pixel<MAV>(res + k * nv * 32, lane, p, p.f[k], color);
+        cols[k * 32 + lane] = color;
+        valid[k * 32 + lane] = ok ? 1u : 0u;
+    }
+    __syncthreads();
+
+    if (!px_ok)
+        return;
+    if (!p.chain)
+    {
+        for (int k = vw; k < nf; k += nv)
+            if (valid[k * 32 + lane])
+                p.out[k][(size_t)y * p.out_w + x] = cols[k * 32 + lane];
+        return;
+    }
+    if (vw != 0)
+        return;
+    // one persistent buffer starting as out[0], copied to out[k] after frame k
+    uint32_t run = 0;
+    for (int k = 0; k < nf; k++)
+    {
+        uint32_t *o = p.out[k] + (size_t)y * p.out_w + x;
+        if (k == 0)
+            run = *o;
+        if (valid[k * 32 + lane])
         {
-            uint32_t color = 0;
-            const bool valid = resolve_pixel<MAV>(res, lane, p, p.f[k], color);
-            uint32_t *o = p.out[k] + (size_t)y * p.out_w + x;
-            if (!p.chain)
-            {
-                if (valid)
-                    *o = color;
-            }
-            else
-            {
-                uint32_t run = k == 0 ? *o : chain[lane];
-                if (valid)
-                    run = color;
-                if (k > 0 || valid)
-                    *o = run;
-                chain[lane] = run;
-            }
+            run = cols[k * 32 + lane];
+            *o = run;
         }
+        else if (k > 0)
+            *o = run;
     }
 }
 
 template <int SW>
-constexpr size_t reproj_smem(int n_views)
+constexpr size_t reproj_smem(int n_views, int n_frames)
 {
-    return (size_t)n_views * (2 * 32 * sizeof(DirRes) + Tile<SW>::H * Tile<SW>::W * sizeof(unsigned long long)) + 32 * sizeof(uint32_t);
+    return (size_t)n_frames * (n_views * 32 * sizeof(DirRes) + 2 * 32 * sizeof(uint32_t)) +
+           (size_t)n_views * Tile<SW>::H * Tile<SW>::W * sizeof(unsigned long long);
 }
 } // namespace isti
 
@@ -765,6 +787,20 @@ void fill_params(isti::FrameParams &p, int n_frames, void *const *outs, const is
     p.chain = chain ? 1 : 0;
 }
 
+template <int SW, int SI, bool MAV>
+cudaError_t launch_reproj(const isti::FrameParams &p, dim3 gr, dim3 br, cudaStream_t stream)
+{
+    const size_t smem = isti::reproj_smem<SW>(p.n_views, p.n_frames); // beyond 48 KiB for large batches
+    if (smem > 48 * 1024)
+    {
+        cudaError_t e = cudaFuncSetAttribute(isti::reproj_kernel<SW, SI, MAV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+    }
+    isti::reproj_kernel<SW, SI, MAV><<<gr, br, smem, stream>>>(p);
+    return cudaGetLastError();
+}
+
 // Enqueues the splat and reprojection kernels of one batch.
 cudaError_t launch_batch(const isti::FrameParams &p, int mode, cudaStream_t stream, cudaEvent_t after_splat)
 {
@@ -785,23 +821,11 @@ cudaError_t launch_batch(const isti::FrameParams &p, int mode, cudaStream_t stre
     {
     case ISTI_MODE_OURS:
     case ISTI_MODE_BACKWARD_UNIDIRECTIONAL:
-        isti::reproj_kernel<1, 3, false><<<gr, br, isti::reproj_smem<1>(p.n_views), stream>>>(p);
-        break;
+        return launch_reproj<1, 3, false>(p, gr, br, stream);
     case ISTI_MODE_SPLATTING:
-        isti::reproj_kernel<1, 0, false><<<gr, br, isti::reproj_smem<1>(p.n_views), stream>>>(p);
-        break;
+        return launch_reproj<1, 0, false>(p, gr, br, stream);
     case ISTI_MODE_BACKWARD_BIDIRECTIONAL:
-    {
-        const size_t smem = isti::reproj_smem<3>(p.n_views); // above 48 KiB from 7 aux cameras on
-        if (smem > 48 * 1024)
-        {
-            cudaError_t e = cudaFuncSetAttribute(isti::reproj_kernel<3, 5, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess)
-                return e;
-        }
-        isti::reproj_kernel<3, 5, true><<<gr, br, smem, stream>>>(p);
-        break;
-    }
+        return launch_reproj<3, 5, true>(p, gr, br, stream);
     }
     return cudaGetLastError();
 }
