@@ -325,7 +325,7 @@ def main_ours(args):
     # shadow A/B/Info for the reprojection launch) and the 3 output frames once.
     px = W * H
     n_views = 2 * n_cams
-    calls = max(1, tim["kernel_launches"] // 2)
+    calls = max(1, tim["kernel_launches"] // 3)  # init, splat, reprojection per call
     alg = {"splat_kernel": n_views * (4 + 6) * px, "reproj_kernel": n_views * (4 + 12) * px + len(TS) * 4 * px}
     per_launch_ms = {"splat_kernel": tim["splat_ms"] / calls, "reproj_kernel": tim["reproj_ms"] / calls}
     dom = max(per_launch_ms, key=per_launch_ms.get)

@@ -66,9 +66,29 @@ __device__ __forceinline__ int2 cs2pixel(float cx, float cy, uint32_t w, uint32_
     return make_int2(__float2int_rz(floorf(ax)), __float2int_rz(floorf(ay)));
 }
 
+// inRange, include/util/helper_common.h:8-11 (a negative coordinate wraps to >= 2^31 > w)
 __device__ __forceinline__ bool in_range(int2 p, uint32_t w, uint32_t h)
 {
-    return p.x >= 0 && (uint32_t)p.x < w && p.y >= 0 && (uint32_t)p.y < h;
+    return (uint32_t)p.x < w && (uint32_t)p.y < h;
+}
+
+// -lim < RN(n / d) < lim, IEEE-exact.  __fdividef is within 2 ulp for
+// 2^-126 <= |d| <= 2^126 (CUDA programming guide, intrinsic functions); the
+// exact division is only carried out outside that range or when the
+// approximate quotient lies within 1e-4 (relative) of the bounds.
+__device__ __forceinline__ bool quotient_inside(float n, float d, float lim)
+{
+    const float ad = fabsf(d);
+    if (ad >= 0x1p-126f && ad <= 0x1p126f)
+    {
+        const float q = fabsf(__fdividef(n, d));
+        if (q < lim * 0.9999f)
+            return true;
+        if (q > lim * 1.0001f)
+            return false;
+    }
+    const float e = __fdiv_rn(n, d);
+    return e > -lim && e < lim;
 }
 
 // glm-subset mat4 * vec4: (m0*x + m1*y) + (m2*z + m3*w), column-major m

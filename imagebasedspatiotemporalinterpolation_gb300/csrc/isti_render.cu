@@ -1,34 +1,34 @@
-// Per-frame interpolation path on GB300: splat kernel + bidirectional
-// reprojection kernel, and the C ABI of include/isti.h.
+// Per-frame interpolation path on GB300: init, splat and bidirectional
+// reprojection kernels, and the C ABI of include/isti.h.
 //
 // Reference: src/renderer.cu (DerThomy/ImageBasedSpatioTemporalInterpolation).
 //
-// A launch pair renders a batch of 1..ISTI_MAX_BATCH_FRAMES client frames of
-// one keyframe pair (isti_render is a batch of one).
+// A launch sequence renders a batch of 1..ISTI_MAX_BATCH_FRAMES client frames
+// of one keyframe pair (isti_render is a batch of one).
 //
 // Layout in HBM (renderer-owned arena, one allocation):
 //   [splat keys, u64/px: frame-major, every view][cam flow f32x4/px: frame-major, every view]
 //   [full flow f32x4/px, every view][pixel->clip tables, (w + h) f32 per view]
-// The key block is contiguous so one memset initialises all frames and views.
 // Pixel inputs are caller-owned device images (include/isti.h).
 //
-// Launches per batch: 1 memset + 1 splat launch (blockIdx.z = source view;
-// one extra z-slice fills the pixel->clip tables) + 1 reprojection launch.
-// Nothing blocks the host.
-//
-// Splat: per source pixel, the keyframe part (world positions, flow to the
-// other keyframe, visibility in the main view) is computed once, then the
-// client-camera projection, flow store and 64-bit atomicMin per frame.
-//
-// Reprojection: a block covers 32 output pixels of one row with one warp per
-// source view (view = threadIdx.y) and loops over the frames.  Each warp runs
-// window initialisation + iterative search + reprojection error for its view
-// (one direction of one camera); then one warp chooses the direction per
-// camera, the winning camera, and computes the colour (second chance, soft
-// shadows) only for the result that is written.  The reference computes the
-// colour of every camera's result (src/renderer.cu:378-396,436); only the
-// written one is observable and colour never feeds a choice, so the output is
-// identical.
+// Launches per batch (nothing blocks the host):
+//  1. init:  every key <- 0xfefe...fe (the reference's cudaMemset(0xfe),
+//            src/renderer.cu:632-638) and the pixel->clip tables;
+//  2. splat: blockIdx.z = source view; per source pixel the keyframe part
+//            (world positions, flow to the other keyframe, visibility in the
+//            main view) once, then per frame the client-camera projection,
+//            flow store and 64-bit atomicMin;
+//  3. reprojection: a block covers 2 rows x 32 output pixels with one warp
+//            per source view (view = threadIdx.y).  Phase 1: each thread runs
+//            window initialisation + iterative search + reprojection error
+//            for its view and both rows, interleaved, for every frame.
+//            Phase 2: the (frame, row) tasks are spread over the warps; each
+//            chooses the direction per camera and the winning camera and
+//            computes the colour (second chance, soft shadows) only for the
+//            result that is written.  The reference colours every camera's
+//            result (src/renderer.cu:378-396,436); only the written one is
+//            observable and colour never feeds a choice, so the output is
+//            identical.  Phase 3 writes chained outputs.
 #include "isti.h"
 #include "isti_device.cuh"
 
@@ -45,6 +45,7 @@ namespace isti
 {
 constexpr int MAX_VIEWS = 2 + 2 * ISTI_MAX_AUX_CAMS;
 constexpr int MAX_FRAMES = ISTI_MAX_BATCH_FRAMES;
+constexpr int ROWS = 2; // output rows per reprojection block
 constexpr float FLT_MAX_F = 3.402823466e+38f;
 
 struct DevView
@@ -83,6 +84,8 @@ struct FrameParams
     FrameCfg f[MAX_FRAMES];
     size_t key_stride; // elements between frames in the key block
     size_t cam_stride; // elements between frames in the cam-flow block
+    ulonglong2 *keys;  // the whole key block (16-byte units) for the init kernel
+    size_t key_units;
     uint32_t out_w, out_h;
     int32_t n_views, n_aux, n_frames, linear, chain;
 };
@@ -91,24 +94,24 @@ struct FrameParams
 
 __device__ __forceinline__ float ld_f(const float *img, uint32_t x, uint32_t y, uint32_t w, uint32_t h)
 {
-    return (x < w && y < h) ? __ldg(img + (size_t)y * w + x) : 0.0f;
+    return (x < w && y < h) ? __ldg(img + (y * w + x)) : 0.0f;
 }
 __device__ __forceinline__ float4 ld_f4(const float4 *img, uint32_t x, uint32_t y, uint32_t w, uint32_t h)
 {
-    return (x < w && y < h) ? __ldg(img + (size_t)y * w + x) : make_float4(0.f, 0.f, 0.f, 0.f);
+    return (x < w && y < h) ? __ldg(img + (y * w + x)) : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 __device__ __forceinline__ uint32_t ld_c(const uint32_t *img, uint32_t x, uint32_t y, uint32_t w, uint32_t h)
 {
-    return (x < w && y < h) ? __ldg(img + (size_t)y * w + x) : 0u;
+    return (x < w && y < h) ? __ldg(img + (y * w + x)) : 0u;
 }
 
-__device__ __forceinline__ float4 load_motion(const DevView &v, size_t idx)
+__device__ __forceinline__ float4 load_motion(const DevView &v, uint32_t idx)
 {
     if (v.motion_fmt == ISTI_MOTION_F32X4)
         return __ldg(static_cast<const float4 *>(v.motion) + idx);
     if (v.motion_fmt == ISTI_MOTION_F16X3)
     {
-        const __half *m = static_cast<const __half *>(v.motion) + 3 * idx;
+        const __half *m = static_cast<const __half *>(v.motion) + 3 * (size_t)idx;
         return make_float4(__half2float(m[0]), __half2float(m[1]), __half2float(m[2]), 0.0f);
     }
     return make_float4(0.f, 0.f, 0.f, 0.f);
@@ -122,43 +125,50 @@ __device__ __forceinline__ float2 view_pixel2cs(const DevView &v, uint32_t x, ui
     return pixel2cs(x, y, v.w, v.h);
 }
 
-// ---- computeFlowFields_sortedSplatting_kernel, src/renderer.cu:76-146 ----
-// blockIdx.z < n_views: one source view; blockIdx.z == n_views: pixel->clip tables.
+// ---- key initialisation (cudaMemset 0xfe, src/renderer.cu:632-638) + pixel->clip tables ----
 
-__global__ void __launch_bounds__(256) splat_kernel(const __grid_constant__ FrameParams p)
+__global__ void __launch_bounds__(256) init_kernel(const __grid_constant__ FrameParams p)
 {
-    if ((int)blockIdx.z == p.n_views)
-    {
-        const uint32_t t = ((blockIdx.y * gridDim.x + blockIdx.x) * blockDim.y + threadIdx.y) * blockDim.x + threadIdx.x;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const ulonglong2 empty = make_ulonglong2(SPLAT_EMPTY, SPLAT_EMPTY);
+    for (size_t i = t; i < p.key_units; i += stride)
+        p.keys[i] = empty;
+    if (t < 65536)
         for (int k = 0; k < p.n_views; k++)
         {
             const DevView &v = p.v[k];
             if (t < v.w)
-                v.lut[t] = pixel2cs(t, 0, v.w, 1).x;
+                v.lut[t] = pixel2cs((uint32_t)t, 0, v.w, 1).x;
             if (t < v.h)
-                v.lut[v.w + t] = pixel2cs(0, t, 1, v.h).y;
+                v.lut[v.w + t] = pixel2cs(0, (uint32_t)t, 1, v.h).y;
         }
-        return;
-    }
+}
+
+// ---- computeFlowFields_sortedSplatting_kernel, src/renderer.cu:76-146 ----
+
+__global__ void __launch_bounds__(256) splat_kernel(const __grid_constant__ FrameParams p)
+{
     const DevView &v = p.v[blockIdx.z];
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= v.w || y >= v.h)
         return;
-    const size_t idx = (size_t)y * v.w + x;
+    const uint32_t idx = y * v.w + x;
 
     // keyframe part, independent of the client camera
     const float z_from = __ldg(v.z + idx);
     const float4 om = load_motion(v, idx);
-    const float2 pcs = pixel2cs(x, y, v.w, v.h);
-    const float4 cs_from = make_float4(pcs.x, pcs.y, z_from, 1.0f);
+    const float pcx = __ldg(v.lut + x), pcy = __ldg(v.lut + v.w + y); // pixel2CS(idx2D, resolution)
+    const float4 cs_from = make_float4(pcx, pcy, z_from, 1.0f);
     const float4 ws_from = project(v.inv_vp, cs_from);
-    const float4 moved = make_float4(__fadd_rn(pcs.x, om.x), __fadd_rn(pcs.y, om.y), __fadd_rn(z_from, om.z), 1.0f);
+    const float4 moved = make_float4(__fadd_rn(pcx, om.x), __fadd_rn(pcy, om.y), __fadd_rn(z_from, om.z), 1.0f);
     const float4 ws_to = project(v.inv_vp, moved);
 
-    const float4 cm = project(v.vp_main, ws_from);
+    // visible_in_main: WS2CS(posWS_from, viewproj_mat_from_main) inside +-(1 - 1e-3), src/renderer.cu:104-107
+    const float4 cm = matvec(v.vp_main, ws_from);
     const float lim = 1.0f - 1e-3f;
-    const bool visible = cm.x > -lim && cm.x < lim && cm.y > -lim && cm.y < lim && cm.z > -lim && cm.z < lim;
+    const bool visible = quotient_inside(cm.x, cm.w, lim) && quotient_inside(cm.y, cm.w, lim) && quotient_inside(cm.z, cm.w, lim);
     const float vis = visible ? 1.0f : 0.0f;
 
     const float4 cs_to = project(v.vp_to, ws_to);
@@ -166,7 +176,6 @@ __global__ void __launch_bounds__(256) splat_kernel(const __grid_constant__ Fram
     v.full_ff[idx] = make_float4(fmx, fmy, fmz, vis);
     const float4 d_ws = make_float4(__fsub_rn(ws_to.x, ws_from.x), __fsub_rn(ws_to.y, ws_from.y), __fsub_rn(ws_to.z, ws_from.z),
                                     __fsub_rn(ws_to.w, ws_from.w));
-    const unsigned long long key_src = encode_key(z_to_depth(z_from), x, y);
 
     // client-camera part, per frame
     for (int k = 0; k < p.n_frames; k++)
@@ -183,12 +192,12 @@ __global__ void __launch_bounds__(256) splat_kernel(const __grid_constant__ Fram
             const float depth_cam = z_to_depth(pc.z);
             const int2 pix = cs2pixel(pc.x, pc.y, v.w, v.h);
             if (in_range(pix, v.w, v.h) && !(depth_cam < 0.0f))
-                atomicMin(keys + (size_t)pix.y * v.w + pix.x, encode_key(depth_cam, x, y));
+                atomicMin(keys + ((uint32_t)pix.y * v.w + (uint32_t)pix.x), encode_key(depth_cam, x, y));
         }
         else
         {
             cam[idx] = make_float4(__fmul_rn(fmx, wg), __fmul_rn(fmy, wg), __fmul_rn(fmz, wg), vis);
-            atomicMin(keys + idx, key_src);
+            atomicMin(keys + idx, encode_key(z_to_depth(z_from), x, y));
         }
     }
 }
@@ -284,7 +293,7 @@ __device__ uint32_t second_chance(float weight, const ShadowFrames &sf, const Fr
         return out;
     if (in_range(pp, to.w, to.h))
     {
-        const size_t pi = (size_t)pp.y * to.w + pp.x;
+        const uint32_t pi = (uint32_t)pp.y * to.w + (uint32_t)pp.x;
         const float az = __ldg(to.z + pi);
         const float4 m_tf = __ldg(to.full_ff + pi);
         const float dx = __fsub_rn(m_ft.x, -m_tf.x), dy = __fsub_rn(m_ft.y, -m_tf.y), dz = __fsub_rn(m_ft.z, -m_tf.z);
@@ -323,7 +332,7 @@ template <int SW>
 struct Tile
 {
     static constexpr int W = 32 + 2 * SW;
-    static constexpr int H = 2 * SW + 1;
+    static constexpr int H = ROWS + 2 * SW;
 };
 
 __device__ __forceinline__ CamRes cam_result(const DirRes &f, const DirRes &b, const DevView &vf, const DevView &vb, float eps1, float eps2,
@@ -372,7 +381,8 @@ __device__ __forceinline__ CamRes cam_result(const DirRes &f, const DirRes &b, c
 }
 
 // Chooses among the cameras of one output pixel and returns the colour to
-// write (valid = false: keep the previous output), src/renderer.cu:400-465.
+// write (false: keep the previous output), src/renderer.cu:400-465.
+// res points at the [n_views][32] results of this pixel's row and frame.
 template <bool MAV>
 __device__ __forceinline__ bool resolve_pixel(const DirRes *res, int lane, const FrameParams &p, const FrameCfg &c, uint32_t &color)
 {
@@ -440,140 +450,189 @@ __device__ __forceinline__ bool resolve_pixel(const DirRes *res, int lane, const
     return true;
 }
 
+// initializeSearchFromSplatting<SW> on a shared-memory tile, src/renderer.cu:148-175.
+// tile row `row` holds the view row of this pixel; keys outside the view read as 0
+// (depth +0.0), which the window never selects, exactly like the reference's
+// skipped out-of-range neighbours.
+template <int SW>
+__device__ __forceinline__ KeyInfo window_min(const unsigned long long *tile, int row, int col)
+{
+    using T = Tile<SW>;
+    KeyInfo lowest = decode_key(tile[row * T::W + col]);
+#pragma unroll
+    for (int yo = -SW; yo <= SW; yo++)
+#pragma unroll
+        for (int xo = -SW; xo <= SW; xo++)
+        {
+            const KeyInfo cur = decode_key(tile[(row + yo) * T::W + col + xo]);
+            if (cur.depth > 0.0f && (!isfinite(lowest.depth) || lowest.depth < 0.0f || cur.depth < lowest.depth))
+                lowest = cur;
+        }
+    return lowest;
+}
+
 // bidirectionalReprojection_kernel<SW, SI, MAIN_ALWAYS_VALID>, src/renderer.cu:400-465
-// block = (32, n_views): 32 output pixels of row blockIdx.y, one warp per source view.
-//  phase 1: each warp runs its view for every frame of the batch (window, search, error);
-//  phase 2: warp w resolves frames w, w + n_views, ... (camera choice and colour);
-//  phase 3: outputs are written (chained: frame k keeps frame k-1's pixel where invalid).
+// block = (32, n_views): output rows ROWS * blockIdx.y + {0, 1}, 32 pixels each, one warp per source view.
 template <int SW, int SI, bool MAV>
 __global__ void __launch_bounds__(32 * MAX_VIEWS) reproj_kernel(const __grid_constant__ FrameParams p)
 {
     using T = Tile<SW>;
     extern __shared__ __align__(16) unsigned char smem[];
     const int nv = p.n_views, nf = p.n_frames;
-    DirRes *res = reinterpret_cast<DirRes *>(smem);                      // [nf][nv][32]
-    uint32_t *cols = reinterpret_cast<uint32_t *>(res + nf * nv * 32);   // [nf][32] colour, bit-packed validity below
-    uint32_t *valid = cols + nf * 32;                                    // [nf][32]
-    unsigned long long *tiles = reinterpret_cast<unsigned long long *>(valid + nf * 32);
+    DirRes *res = reinterpret_cast<DirRes *>(smem);                        // [nf][ROWS][nv][32]
+    uint32_t *cols = reinterpret_cast<uint32_t *>(res + nf * ROWS * nv * 32); // [nf][ROWS][32]
+    uint32_t *valid = cols + nf * ROWS * 32;                               // [nf][ROWS][32]
+    unsigned long long *tiles = reinterpret_cast<unsigned long long *>(valid + nf * ROWS * 32);
 
     const int lane = threadIdx.x, vw = threadIdx.y;
-    const uint32_t x0 = blockIdx.x * 32, x = x0 + lane, y = blockIdx.y;
+    const uint32_t x0 = blockIdx.x * 32, x = x0 + lane, y0 = blockIdx.y * ROWS;
+    const bool xok = x < p.out_w;
     {
         const DevView &v = p.v[vw];
-        const uint32_t ix = v.sx == 1 ? x : x / v.sx, iy = v.sy == 1 ? y : y / v.sy, tx0 = v.sx == 1 ? x0 : x0 / v.sx;
+        const uint32_t ix = v.sx == 1 ? x : x / v.sx, tx0 = v.sx == 1 ? x0 : x0 / v.sx;
+        const uint32_t iy0 = v.sy == 1 ? y0 : y0 / v.sy, iy1 = v.sy == 1 ? y0 + 1 : (y0 + 1) / v.sy;
+        const bool ok0 = xok, ok1 = xok && y0 + 1 < p.out_h;
         const bool fwd = (vw & 1) == 0;
         unsigned long long *tile = tiles + vw * (T::H * T::W);
-        const int cx = (int)(ix - tx0) + SW;
+        const int col = (int)(ix - tx0) + SW, row1 = (int)(iy1 - iy0) + SW;
+        // pixel2CS of the output pixels in the main view (the search target) and in this view (the error)
+        const DevView &v0 = p.v[0];
+        const uint32_t xc = min(x, p.out_w - 1), y1c = min(y0 + 1, p.out_h - 1);
+        const float qx = __ldg(v0.lut + xc), qy0 = __ldg(v0.lut + v0.w + y0), qy1 = __ldg(v0.lut + v0.w + y1c);
+        const float pcx = __ldg(v.lut + min(ix, v.w - 1)), pcy0 = __ldg(v.lut + v.w + iy0), pcy1 = __ldg(v.lut + v.w + min(iy1, v.h - 1));
 #pragma unroll 1
         for (int k = 0; k < nf; k++)
         {
             const unsigned long long *keys = v.splat + k * p.key_stride;
-            // splat keys around this warp's pixels (initializeSearchFromSplatting<SW>, src/renderer.cu:148-175);
-            // a key outside the view reads as 0 (depth +0.0), which the window never selects, exactly like
-            // the reference's skipped out-of-range neighbours
-            if (k > 0)
-                __syncwarp();
+            const float4 *cam = v.cam_ff + k * p.cam_stride;
+            __syncwarp();
 #pragma unroll
             for (int r = 0; r < T::H; r++)
             {
-                const int gy = (int)iy - SW + r;
-                const bool row_ok = gy >= 0 && gy < (int)v.h;
+                const uint32_t gy = iy0 - SW + r;
+                const bool row_ok = gy < v.h;
                 for (int c = lane; c < T::W; c += 32)
                 {
-                    const int gx = (int)tx0 - SW + c;
-                    tile[r * T::W + c] = (row_ok && gx >= 0 && gx < (int)v.w) ? __ldg(keys + (size_t)gy * v.w + gx) : 0ull;
+                    const uint32_t gx = tx0 - SW + c;
+                    tile[r * T::W + c] = (row_ok && gx < v.w) ? __ldg(keys + (gy * v.w + gx)) : 0ull;
                 }
             }
             __syncwarp();
 
-            DirRes d;
-            d.error = FLT_MAX_F;
-            d.depth = 0.0f;
-            d.src = 0;
-            d.vis = 0;
-            if (x < p.out_w)
+            const KeyInfo lo0 = window_min<SW>(tile, SW, col);
+            const KeyInfo lo1 = window_min<SW>(tile, row1, col);
+            const bool search_ok = !fwd || p.f[k].alpha < 1.0f;
+            const bool s0 = ok0 && lo0.depth > 0.0f && search_ok, s1 = ok1 && lo1.depth > 0.0f && search_ok;
+            uint32_t a0x = lo0.sx, a0y = lo0.sy, a1x = lo1.sx, a1y = lo1.sy;
+            // iterativeSearch<SI>, src/renderer.cu:177-202, both rows interleaved.  The start is a
+            // splatted source pixel and every accepted step is in range: no border handling needed.
+#pragma unroll
+            for (int i = 0; i < SI; i++)
             {
-                KeyInfo lowest = decode_key(tile[SW * T::W + cx]);
-#pragma unroll
-                for (int yo = -SW; yo <= SW; yo++)
-#pragma unroll
-                    for (int xo = -SW; xo <= SW; xo++)
-                    {
-                        const KeyInfo cur = decode_key(tile[(SW + yo) * T::W + cx + xo]);
-                        if (cur.depth > 0.0f && (!isfinite(lowest.depth) || lowest.depth < 0.0f || cur.depth < lowest.depth))
-                            lowest = cur;
-                    }
-                uint32_t ssx = lowest.sx, ssy = lowest.sy;
-                d.depth = lowest.depth;
-                if (lowest.depth > 0.0f && (!fwd || p.f[k].alpha < 1.0f))
+                float4 m0 = make_float4(0.f, 0.f, 0.f, 0.f), m1 = m0;
+                if (s0)
+                    m0 = __ldg(cam + (a0y * v.w + a0x));
+                if (s1)
+                    m1 = __ldg(cam + (a1y * v.w + a1x));
+                const int2 t0 = cs2pixel(__fsub_rn(qx, m0.x), __fsub_rn(qy0, m0.y), v.w, v.h);
+                const int2 t1 = cs2pixel(__fsub_rn(qx, m1.x), __fsub_rn(qy1, m1.y), v.w, v.h);
+                if (s0 && in_range(t0, v.w, v.h))
                 {
-                    // iterativeSearch<SI>, src/renderer.cu:177-202.  The start is a splatted source pixel
-                    // and every accepted step is in range, so no border handling is needed.
-                    const float4 *cam = v.cam_ff + k * p.cam_stride;
-                    const float qx = __ldg(p.v[0].lut + x), qy = __ldg(p.v[0].lut + p.v[0].w + y); // pixel2CS(idx, res)
-#pragma unroll
-                    for (int i = 0; i < SI; i++)
-                    {
-                        const float4 m = __ldg(cam + (size_t)ssy * v.w + ssx);
-                        const int2 t = cs2pixel(__fsub_rn(qx, m.x), __fsub_rn(qy, m.y), v.w, v.h);
-                        if (in_range(t, v.w, v.h))
-                        {
-                            ssx = (uint32_t)t.x;
-                            ssy = (uint32_t)t.y;
-                        }
-                    }
-                    const size_t si = (size_t)ssy * v.w + ssx;
-                    const float4 m = __ldg(cam + si);
-                    d.depth = z_to_depth(__fadd_rn(__ldg(v.z + si), m.z));
-                    // computeReprojError, src/renderer.cu:204-215 (pixelCS of the output pixel in this view)
-                    const float pcx = __ldg(v.lut + ix), pcy = __ldg(v.lut + v.w + iy);
-                    const float pfx = __ldg(v.lut + ssx), pfy = __ldg(v.lut + v.w + ssy);
-                    float ex = __fsub_rn(__fadd_rn(pfx, m.x), pcx);
-                    float ey = __fsub_rn(__fadd_rn(pfy, m.y), pcy);
-                    ex = __fmul_rn(ex, v.err_sx);
-                    ey = __fmul_rn(ey, v.err_sy);
-                    d.error = __fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)));
-                    d.vis = m.w > 0.0f;
+                    a0x = (uint32_t)t0.x;
+                    a0y = (uint32_t)t0.y;
                 }
-                d.src = (ssx << 16) | ssy;
+                if (s1 && in_range(t1, v.w, v.h))
+                {
+                    a1x = (uint32_t)t1.x;
+                    a1y = (uint32_t)t1.y;
+                }
             }
-            res[(k * nv + vw) * 32 + lane] = d;
+            DirRes d0, d1;
+            d0.error = d1.error = FLT_MAX_F;
+            d0.depth = lo0.depth;
+            d1.depth = lo1.depth;
+            d0.vis = d1.vis = 0;
+            float4 m0 = make_float4(0.f, 0.f, 0.f, 0.f), m1 = m0;
+            float z0 = 0.f, z1 = 0.f, f0x = 0.f, f0y = 0.f, f1x = 0.f, f1y = 0.f;
+            if (s0)
+            {
+                const uint32_t si = a0y * v.w + a0x;
+                m0 = __ldg(cam + si);
+                z0 = __ldg(v.z + si);
+                f0x = __ldg(v.lut + a0x);
+                f0y = __ldg(v.lut + v.w + a0y);
+            }
+            if (s1)
+            {
+                const uint32_t si = a1y * v.w + a1x;
+                m1 = __ldg(cam + si);
+                z1 = __ldg(v.z + si);
+                f1x = __ldg(v.lut + a1x);
+                f1y = __ldg(v.lut + v.w + a1y);
+            }
+            // computeReprojError, src/renderer.cu:204-215
+            if (s0)
+            {
+                d0.depth = z_to_depth(__fadd_rn(z0, m0.z));
+                const float ex = __fmul_rn(__fsub_rn(__fadd_rn(f0x, m0.x), pcx), v.err_sx);
+                const float ey = __fmul_rn(__fsub_rn(__fadd_rn(f0y, m0.y), pcy0), v.err_sy);
+                d0.error = __fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)));
+                d0.vis = m0.w > 0.0f;
+            }
+            if (s1)
+            {
+                d1.depth = z_to_depth(__fadd_rn(z1, m1.z));
+                const float ex = __fmul_rn(__fsub_rn(__fadd_rn(f1x, m1.x), pcx), v.err_sx);
+                const float ey = __fmul_rn(__fsub_rn(__fadd_rn(f1y, m1.y), pcy1), v.err_sy);
+                d1.error = __fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)));
+                d1.vis = m1.w > 0.0f;
+            }
+            d0.src = (a0x << 16) | a0y;
+            d1.src = (a1x << 16) | a1y;
+            res[((k * ROWS + 0) * nv + vw) * 32 + lane] = d0;
+            res[((k * ROWS + 1) * nv + vw) * 32 + lane] = d1;
         }
     }
     __syncthreads();
 
-    const bool px_ok = x < p.out_w;
+    // phase 2: (frame, row) tasks over the warps
 #pragma unroll 1
-    for (int k = vw; k < nf; k += nv)
+    for (int t = vw; t < nf * ROWS; t += nv)
     {
+        const int k = t / ROWS, r = t % ROWS;
+        const uint32_t y = y0 + r;
         uint32_t color = 0;
-        const bool ok = px_ok && resolve_pixel<MAV>(res + k * nv * 32, lane, p, p.f[k], color);
-        cols[k * 32 + lane] = color;
-        valid[k * 32 + lane] = ok ? 1u : 0u;
+        const bool ok = xok && y < p.out_h && resolve_pixel<MAV>(res + t * nv * 32, lane, p, p.f[k], color);
+        if (!p.chain)
+        {
+            if (ok)
+                p.out[k][y * p.out_w + x] = color;
+        }
+        else
+        {
+            cols[t * 32 + lane] = color;
+            valid[t * 32 + lane] = ok ? 1u : 0u;
+        }
     }
-    __syncthreads();
-
-    if (!px_ok)
-        return;
     if (!p.chain)
-    {
-        for (int k = vw; k < nf; k += nv)
-            if (valid[k * 32 + lane])
-                p.out[k][(size_t)y * p.out_w + x] = cols[k * 32 + lane];
         return;
-    }
-    if (vw != 0)
+    __syncthreads();
+    // phase 3: one persistent buffer per row, starting as out[0], copied to out[k] after frame k
+    if (vw >= ROWS)
         return;
-    // one persistent buffer starting as out[0], copied to out[k] after frame k
+    const uint32_t y = y0 + vw;
+    if (!xok || y >= p.out_h)
+        return;
     uint32_t run = 0;
     for (int k = 0; k < nf; k++)
     {
-        uint32_t *o = p.out[k] + (size_t)y * p.out_w + x;
+        uint32_t *o = p.out[k] + (y * p.out_w + x);
+        const int t = k * ROWS + vw;
         if (k == 0)
             run = *o;
-        if (valid[k * 32 + lane])
+        if (valid[t * 32 + lane])
         {
-            run = cols[k * 32 + lane];
+            run = cols[t * 32 + lane];
             *o = run;
         }
         else if (k > 0)
@@ -584,7 +643,7 @@ __global__ void __launch_bounds__(32 * MAX_VIEWS) reproj_kernel(const __grid_con
 template <int SW>
 constexpr size_t reproj_smem(int n_views, int n_frames)
 {
-    return (size_t)n_frames * (n_views * 32 * sizeof(DirRes) + 2 * 32 * sizeof(uint32_t)) +
+    return (size_t)n_frames * ROWS * (n_views * 32 * sizeof(DirRes) + 2 * 32 * sizeof(uint32_t)) +
            (size_t)n_views * Tile<SW>::H * Tile<SW>::W * sizeof(unsigned long long);
 }
 } // namespace isti
@@ -778,6 +837,8 @@ void fill_params(isti::FrameParams &p, int n_frames, void *const *outs, const is
     }
     p.key_stride = l.key_frame_bytes / sizeof(unsigned long long);
     p.cam_stride = l.cam_frame_bytes / sizeof(float4);
+    p.keys = reinterpret_cast<ulonglong2 *>(base);
+    p.key_units = l.key_bytes / sizeof(ulonglong2);
     p.out_w = info.width;
     p.out_h = info.height;
     p.n_views = n_views;
@@ -788,7 +849,7 @@ void fill_params(isti::FrameParams &p, int n_frames, void *const *outs, const is
 }
 
 template <int SW, int SI, bool MAV>
-cudaError_t launch_reproj(const isti::FrameParams &p, dim3 gr, dim3 br, cudaStream_t stream)
+cudaError_t launch_reproj(const isti::FrameParams &p, cudaStream_t stream)
 {
     const size_t smem = isti::reproj_smem<SW>(p.n_views, p.n_frames); // beyond 48 KiB for large batches
     if (smem > 48 * 1024)
@@ -797,12 +858,13 @@ cudaError_t launch_reproj(const isti::FrameParams &p, dim3 gr, dim3 br, cudaStre
         if (e != cudaSuccess)
             return e;
     }
-    isti::reproj_kernel<SW, SI, MAV><<<gr, br, smem, stream>>>(p);
+    const dim3 gr((p.out_w + 31) / 32, (p.out_h + isti::ROWS - 1) / isti::ROWS);
+    isti::reproj_kernel<SW, SI, MAV><<<gr, dim3(32, p.n_views), smem, stream>>>(p);
     return cudaGetLastError();
 }
 
-// Enqueues the splat and reprojection kernels of one batch.
-cudaError_t launch_batch(const isti::FrameParams &p, int mode, cudaStream_t stream, cudaEvent_t after_splat)
+// Enqueues the three kernels of one batch; events (optional) are recorded after init and splat.
+cudaError_t launch_batch(const isti::FrameParams &p, int mode, cudaStream_t stream, cudaEvent_t after_init, cudaEvent_t after_splat)
 {
     uint32_t max_w = 0, max_h = 0;
     for (int k = 0; k < p.n_views; k++)
@@ -810,22 +872,28 @@ cudaError_t launch_batch(const isti::FrameParams &p, int mode, cudaStream_t stre
         max_w = p.v[k].w > max_w ? p.v[k].w : max_w;
         max_h = p.v[k].h > max_h ? p.v[k].h : max_h;
     }
-    const dim3 blk(32, 8);
-    const dim3 gs((max_w + 31) / 32, (max_h + 7) / 8, p.n_views + 1);
-    isti::splat_kernel<<<gs, blk, 0, stream>>>(p);
+    // init: about 8 x 16-byte stores per thread, at least enough threads for the tables (<= 65535 entries)
+    size_t init_blocks = (p.key_units + 8 * 256 - 1) / (8 * 256);
+    if (init_blocks < 256)
+        init_blocks = 256;
+    if (init_blocks > 152 * 64)
+        init_blocks = 152 * 64;
+    isti::init_kernel<<<(unsigned)init_blocks, 256, 0, stream>>>(p);
+    if (after_init)
+        cudaEventRecord(after_init, stream);
+    const dim3 gs((max_w + 31) / 32, (max_h + 7) / 8, p.n_views);
+    isti::splat_kernel<<<gs, dim3(32, 8), 0, stream>>>(p);
     if (after_splat)
         cudaEventRecord(after_splat, stream);
-    const dim3 gr((p.out_w + 31) / 32, p.out_h);
-    const dim3 br(32, p.n_views);
     switch (mode)
     {
     case ISTI_MODE_OURS:
     case ISTI_MODE_BACKWARD_UNIDIRECTIONAL:
-        return launch_reproj<1, 3, false>(p, gr, br, stream);
+        return launch_reproj<1, 3, false>(p, stream);
     case ISTI_MODE_SPLATTING:
-        return launch_reproj<1, 0, false>(p, gr, br, stream);
+        return launch_reproj<1, 0, false>(p, stream);
     case ISTI_MODE_BACKWARD_BIDIRECTIONAL:
-        return launch_reproj<3, 5, true>(p, gr, br, stream);
+        return launch_reproj<3, 5, true>(p, stream);
     }
     return cudaGetLastError();
 }
@@ -883,15 +951,10 @@ isti_status render_batch(isti_renderer *r, int n_frames, void *const *outs, cons
         r->event_frames[r->events_used / 4] = n_frames;
         ev = &r->events[r->events_used];
         r->events_used += 4;
-        r->timed_launches += 2;
+        r->timed_launches += 3;
         cudaEventRecord(ev[0], stream);
     }
-    e = cudaMemsetAsync(base, 0xfe, l.key_bytes, stream);
-    if (e != cudaSuccess)
-        return cuda_fail(e, "cudaMemsetAsync");
-    if (ev)
-        cudaEventRecord(ev[1], stream);
-    e = launch_batch(r->last, infos[0].mode, stream, ev ? ev[2] : nullptr);
+    e = launch_batch(r->last, infos[0].mode, stream, ev ? ev[1] : nullptr, ev ? ev[2] : nullptr);
     if (ev)
         cudaEventRecord(ev[3], stream);
     if (e != cudaSuccess)
@@ -1092,14 +1155,10 @@ extern "C" isti_status isti_render_noalloc(void *out_rgba, const isti_render_inf
         return st;
     isti::FrameParams p;
     fill_params(p, 1, outs, info, frame, views, n_views, l, base, false);
-    // The array keeps the previous call's contents: every key starts as the
-    // reference's empty value (all bytes 0xfe); flow fields and tables are fully
-    // rewritten by the splat launch before the reprojection reads them.
-    cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
-    e = cudaMemsetAsync(base, 0xfe, l.key_bytes, stream);
-    if (e != cudaSuccess)
-        return cuda_fail(e, "cudaMemsetAsync");
-    e = launch_batch(p, info->mode, stream, nullptr);
+    // The array keeps the previous call's contents: the init kernel resets every key to
+    // the reference's empty value (all bytes 0xfe) and rewrites the tables; the flow
+    // fields are fully rewritten by the splat kernel before the reprojection reads them.
+    e = launch_batch(p, info->mode, static_cast<cudaStream_t>(stream_ptr), nullptr, nullptr);
     if (e != cudaSuccess)
         return cuda_fail(e, "kernel launch");
     return ISTI_OK;
