@@ -450,30 +450,48 @@ __device__ __forceinline__ bool resolve_pixel(const DirRes *res, int lane, const
     return true;
 }
 
-// initializeSearchFromSplatting<SW> on a shared-memory tile, src/renderer.cu:148-175.
-// tile row `row` holds the view row of this pixel; keys outside the view read as 0
-// (depth +0.0), which the window never selects, exactly like the reference's
-// skipped out-of-range neighbours.
+// Upper bound for the window comparison, from the depth bits l of the current lowest key.
+// The reference replaces the lowest entry by a candidate c with c > 0 when
+//   !isfinite(l) || l < 0 || c < l            (src/renderer.cu:167)
+// For c > 0 (bits in [1, 0x7f800000], +inf included) this is c_bits < bound(l_bits):
+//   l = +-inf, NaN, or negative non-zero  -> always true  -> bound 0xffffffff;
+//   l = -0.0                              -> always false -> bound 0;
+//   l in [+0, +max finite]                -> c < l, monotonic in the bits -> bound l_bits.
+__device__ __forceinline__ uint32_t key_bound(uint32_t l)
+{
+    return l == 0x80000000u ? 0u : (l >= 0x7f800000u ? 0xffffffffu : l);
+}
+
+// initializeSearchFromSplatting<SW> on a shared-memory tile, src/renderer.cu:148-175, same
+// scan order.  Tile row `row` holds the view row of this pixel; keys outside the view read
+// as 0 (depth +0.0), which the window never selects, exactly like the reference's skipped
+// out-of-range neighbours.  Returns the selected raw key.
 template <int SW>
-__device__ __forceinline__ KeyInfo window_min(const unsigned long long *tile, int row, int col)
+__device__ __forceinline__ unsigned long long window_key(const unsigned long long *tile, int row, int col)
 {
     using T = Tile<SW>;
-    KeyInfo lowest = decode_key(tile[row * T::W + col]);
+    unsigned long long best = tile[row * T::W + col];
+    uint32_t bound = key_bound((uint32_t)(best >> 32));
 #pragma unroll
     for (int yo = -SW; yo <= SW; yo++)
 #pragma unroll
         for (int xo = -SW; xo <= SW; xo++)
         {
-            const KeyInfo cur = decode_key(tile[(row + yo) * T::W + col + xo]);
-            if (cur.depth > 0.0f && (!isfinite(lowest.depth) || lowest.depth < 0.0f || cur.depth < lowest.depth))
-                lowest = cur;
+            const unsigned long long c = tile[(row + yo) * T::W + col + xo];
+            const uint32_t cb = (uint32_t)(c >> 32);
+            if (cb - 1u < 0x7f800000u && cb < bound) // c > 0 && (the reference's replacement test)
+            {
+                best = c;
+                bound = key_bound(cb);
+            }
         }
-    return lowest;
+    return best;
 }
 
 // bidirectionalReprojection_kernel<SW, SI, MAIN_ALWAYS_VALID>, src/renderer.cu:400-465
 // block = (32, n_views): output rows ROWS * blockIdx.y + {0, 1}, 32 pixels each, one warp per source view.
-template <int SW, int SI, bool MAV>
+// Phase 1 takes G frames at a time, so each thread has ROWS x G independent search chains in flight.
+template <int SW, int SI, bool MAV, int G>
 __global__ void __launch_bounds__(32 * MAX_VIEWS) reproj_kernel(const __grid_constant__ FrameParams p)
 {
     using T = Tile<SW>;
@@ -482,7 +500,7 @@ __global__ void __launch_bounds__(32 * MAX_VIEWS) reproj_kernel(const __grid_con
     DirRes *res = reinterpret_cast<DirRes *>(smem);                        // [nf][ROWS][nv][32]
     uint32_t *cols = reinterpret_cast<uint32_t *>(res + nf * ROWS * nv * 32); // [nf][ROWS][32]
     uint32_t *valid = cols + nf * ROWS * 32;                               // [nf][ROWS][32]
-    unsigned long long *tiles = reinterpret_cast<unsigned long long *>(valid + nf * ROWS * 32);
+    unsigned long long *tiles = reinterpret_cast<unsigned long long *>(valid + nf * ROWS * 32); // [nv][G][H][W]
 
     const int lane = threadIdx.x, vw = threadIdx.y;
     const uint32_t x0 = blockIdx.x * 32, x = x0 + lane, y0 = blockIdx.y * ROWS;
@@ -493,104 +511,131 @@ __global__ void __launch_bounds__(32 * MAX_VIEWS) reproj_kernel(const __grid_con
         const uint32_t iy0 = v.sy == 1 ? y0 : y0 / v.sy, iy1 = v.sy == 1 ? y0 + 1 : (y0 + 1) / v.sy;
         const bool ok0 = xok, ok1 = xok && y0 + 1 < p.out_h;
         const bool fwd = (vw & 1) == 0;
-        unsigned long long *tile = tiles + vw * (T::H * T::W);
-        const int col = (int)(ix - tx0) + SW, row1 = (int)(iy1 - iy0) + SW;
+        unsigned long long *tile = tiles + vw * (G * T::H * T::W);
+        const int col = (int)(ix - tx0) + SW;
+        const int wrow[ROWS] = {SW, (int)(iy1 - iy0) + SW}; // tile row of each output row's window centre
+        const bool rok[ROWS] = {ok0, ok1};
         // pixel2CS of the output pixels in the main view (the search target) and in this view (the error)
         const DevView &v0 = p.v[0];
         const uint32_t xc = min(x, p.out_w - 1), y1c = min(y0 + 1, p.out_h - 1);
-        const float qx = __ldg(v0.lut + xc), qy0 = __ldg(v0.lut + v0.w + y0), qy1 = __ldg(v0.lut + v0.w + y1c);
-        const float pcx = __ldg(v.lut + min(ix, v.w - 1)), pcy0 = __ldg(v.lut + v.w + iy0), pcy1 = __ldg(v.lut + v.w + min(iy1, v.h - 1));
+        const float qx = __ldg(v0.lut + xc);
+        const float qy[ROWS] = {__ldg(v0.lut + v0.w + y0), __ldg(v0.lut + v0.w + y1c)};
+        const float pcx = __ldg(v.lut + min(ix, v.w - 1));
+        const float pcy[ROWS] = {__ldg(v.lut + v.w + iy0), __ldg(v.lut + v.w + min(iy1, v.h - 1))};
+        const uint32_t vwid = v.w, vhei = v.h;
 #pragma unroll 1
-        for (int k = 0; k < nf; k++)
+        for (int k0 = 0; k0 < nf; k0 += G)
         {
-            const unsigned long long *keys = v.splat + k * p.key_stride;
-            const float4 *cam = v.cam_ff + k * p.cam_stride;
             __syncwarp();
 #pragma unroll
-            for (int r = 0; r < T::H; r++)
+            for (int g = 0; g < G; g++)
             {
-                const uint32_t gy = iy0 - SW + r;
-                const bool row_ok = gy < v.h;
-                for (int c = lane; c < T::W; c += 32)
+                if (k0 + g < nf)
                 {
-                    const uint32_t gx = tx0 - SW + c;
-                    tile[r * T::W + c] = (row_ok && gx < v.w) ? __ldg(keys + (gy * v.w + gx)) : 0ull;
+                    const unsigned long long *keys = v.splat + (k0 + g) * p.key_stride;
+                    unsigned long long *tg = tile + g * (T::H * T::W);
+#pragma unroll
+                    for (int r = 0; r < T::H; r++)
+                    {
+                        const uint32_t gy = iy0 - SW + r;
+                        const bool row_ok = gy < vhei;
+                        for (int c = lane; c < T::W; c += 32)
+                        {
+                            const uint32_t gx = tx0 - SW + c;
+                            tg[r * T::W + c] = (row_ok && gx < vwid) ? __ldg(keys + (gy * vwid + gx)) : 0ull;
+                        }
+                    }
                 }
             }
             __syncwarp();
 
-            const KeyInfo lo0 = window_min<SW>(tile, SW, col);
-            const KeyInfo lo1 = window_min<SW>(tile, row1, col);
-            const bool search_ok = !fwd || p.f[k].alpha < 1.0f;
-            const bool s0 = ok0 && lo0.depth > 0.0f && search_ok, s1 = ok1 && lo1.depth > 0.0f && search_ok;
-            uint32_t a0x = lo0.sx, a0y = lo0.sy, a1x = lo1.sx, a1y = lo1.sy;
-            // iterativeSearch<SI>, src/renderer.cu:177-202, both rows interleaved.  The start is a
+            bool s[G][ROWS];
+            uint32_t ax[G][ROWS], ay[G][ROWS];
+            float d_init[G][ROWS];
+            const float4 *cam[G];
+#pragma unroll
+            for (int g = 0; g < G; g++)
+            {
+                const int k = min(k0 + g, nf - 1);
+                const bool search_ok = (k0 + g < nf) && (!fwd || p.f[k].alpha < 1.0f);
+                cam[g] = v.cam_ff + k * p.cam_stride;
+#pragma unroll
+                for (int r = 0; r < ROWS; r++)
+                {
+                    const unsigned long long lo = window_key<SW>(tile + g * (T::H * T::W), wrow[r], col);
+                    d_init[g][r] = __uint_as_float((uint32_t)(lo >> 32));
+                    ax[g][r] = ((uint32_t)lo) >> 16;
+                    ay[g][r] = (uint32_t)lo & 0xFFFFu;
+                    s[g][r] = rok[r] && search_ok && d_init[g][r] > 0.0f;
+                }
+            }
+            // iterativeSearch<SI>, src/renderer.cu:177-202, all chains interleaved.  The start is a
             // splatted source pixel and every accepted step is in range: no border handling needed.
 #pragma unroll
             for (int i = 0; i < SI; i++)
             {
-                float4 m0 = make_float4(0.f, 0.f, 0.f, 0.f), m1 = m0;
-                if (s0)
-                    m0 = __ldg(cam + (a0y * v.w + a0x));
-                if (s1)
-                    m1 = __ldg(cam + (a1y * v.w + a1x));
-                const int2 t0 = cs2pixel(__fsub_rn(qx, m0.x), __fsub_rn(qy0, m0.y), v.w, v.h);
-                const int2 t1 = cs2pixel(__fsub_rn(qx, m1.x), __fsub_rn(qy1, m1.y), v.w, v.h);
-                if (s0 && in_range(t0, v.w, v.h))
+                float4 m[G][ROWS];
+#pragma unroll
+                for (int g = 0; g < G; g++)
+#pragma unroll
+                    for (int r = 0; r < ROWS; r++)
+                        m[g][r] = s[g][r] ? __ldg(cam[g] + (ay[g][r] * vwid + ax[g][r])) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int g = 0; g < G; g++)
+#pragma unroll
+                    for (int r = 0; r < ROWS; r++)
+                    {
+                        const int2 t = cs2pixel(__fsub_rn(qx, m[g][r].x), __fsub_rn(qy[r], m[g][r].y), vwid, vhei);
+                        if (s[g][r] && in_range(t, vwid, vhei))
+                        {
+                            ax[g][r] = (uint32_t)t.x;
+                            ay[g][r] = (uint32_t)t.y;
+                        }
+                    }
+            }
+            // final flow, depth and computeReprojError, src/renderer.cu:338-341, 204-215
+            float4 m[G][ROWS];
+            float zz[G][ROWS], fx[G][ROWS], fy[G][ROWS];
+#pragma unroll
+            for (int g = 0; g < G; g++)
+#pragma unroll
+                for (int r = 0; r < ROWS; r++)
                 {
-                    a0x = (uint32_t)t0.x;
-                    a0y = (uint32_t)t0.y;
+                    m[g][r] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    zz[g][r] = fx[g][r] = fy[g][r] = 0.f;
+                    if (s[g][r])
+                    {
+                        const uint32_t si = ay[g][r] * vwid + ax[g][r];
+                        m[g][r] = __ldg(cam[g] + si);
+                        zz[g][r] = __ldg(v.z + si);
+                        fx[g][r] = __ldg(v.lut + ax[g][r]);
+                        fy[g][r] = __ldg(v.lut + vwid + ay[g][r]);
+                    }
                 }
-                if (s1 && in_range(t1, v.w, v.h))
+#pragma unroll
+            for (int g = 0; g < G; g++)
+            {
+                if (k0 + g >= nf)
+                    break;
+#pragma unroll
+                for (int r = 0; r < ROWS; r++)
                 {
-                    a1x = (uint32_t)t1.x;
-                    a1y = (uint32_t)t1.y;
+                    DirRes d;
+                    d.error = FLT_MAX_F;
+                    d.depth = d_init[g][r];
+                    d.vis = 0;
+                    if (s[g][r])
+                    {
+                        d.depth = z_to_depth(__fadd_rn(zz[g][r], m[g][r].z));
+                        const float ex = __fmul_rn(__fsub_rn(__fadd_rn(fx[g][r], m[g][r].x), pcx), v.err_sx);
+                        const float ey = __fmul_rn(__fsub_rn(__fadd_rn(fy[g][r], m[g][r].y), pcy[r]), v.err_sy);
+                        d.error = __fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)));
+                        d.vis = m[g][r].w > 0.0f;
+                    }
+                    d.src = (ax[g][r] << 16) | ay[g][r];
+                    res[(((k0 + g) * ROWS + r) * nv + vw) * 32 + lane] = d;
                 }
             }
-            DirRes d0, d1;
-            d0.error = d1.error = FLT_MAX_F;
-            d0.depth = lo0.depth;
-            d1.depth = lo1.depth;
-            d0.vis = d1.vis = 0;
-            float4 m0 = make_float4(0.f, 0.f, 0.f, 0.f), m1 = m0;
-            float z0 = 0.f, z1 = 0.f, f0x = 0.f, f0y = 0.f, f1x = 0.f, f1y = 0.f;
-            if (s0)
-            {
-                const uint32_t si = a0y * v.w + a0x;
-                m0 = __ldg(cam + si);
-                z0 = __ldg(v.z + si);
-                f0x = __ldg(v.lut + a0x);
-                f0y = __ldg(v.lut + v.w + a0y);
-            }
-            if (s1)
-            {
-                const uint32_t si = a1y * v.w + a1x;
-                m1 = __ldg(cam + si);
-                z1 = __ldg(v.z + si);
-                f1x = __ldg(v.lut + a1x);
-                f1y = __ldg(v.lut + v.w + a1y);
-            }
-            // computeReprojError, src/renderer.cu:204-215
-            if (s0)
-            {
-                d0.depth = z_to_depth(__fadd_rn(z0, m0.z));
-                const float ex = __fmul_rn(__fsub_rn(__fadd_rn(f0x, m0.x), pcx), v.err_sx);
-                const float ey = __fmul_rn(__fsub_rn(__fadd_rn(f0y, m0.y), pcy0), v.err_sy);
-                d0.error = __fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)));
-                d0.vis = m0.w > 0.0f;
-            }
-            if (s1)
-            {
-                d1.depth = z_to_depth(__fadd_rn(z1, m1.z));
-                const float ex = __fmul_rn(__fsub_rn(__fadd_rn(f1x, m1.x), pcx), v.err_sx);
-                const float ey = __fmul_rn(__fsub_rn(__fadd_rn(f1y, m1.y), pcy1), v.err_sy);
-                d1.error = __fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)));
-                d1.vis = m1.w > 0.0f;
-            }
-            d0.src = (a0x << 16) | a0y;
-            d1.src = (a1x << 16) | a1y;
-            res[((k * ROWS + 0) * nv + vw) * 32 + lane] = d0;
-            res[((k * ROWS + 1) * nv + vw) * 32 + lane] = d1;
         }
     }
     __syncthreads();
@@ -640,11 +685,11 @@ __global__ void __launch_bounds__(32 * MAX_VIEWS) reproj_kernel(const __grid_con
     }
 }
 
-template <int SW>
+template <int SW, int G>
 constexpr size_t reproj_smem(int n_views, int n_frames)
 {
     return (size_t)n_frames * ROWS * (n_views * 32 * sizeof(DirRes) + 2 * 32 * sizeof(uint32_t)) +
-           (size_t)n_views * Tile<SW>::H * Tile<SW>::W * sizeof(unsigned long long);
+           (size_t)n_views * G * Tile<SW>::H * Tile<SW>::W * sizeof(unsigned long long);
 }
 } // namespace isti
 
@@ -848,19 +893,27 @@ void fill_params(isti::FrameParams &p, int n_frames, void *const *outs, const is
     p.chain = chain ? 1 : 0;
 }
 
-template <int SW, int SI, bool MAV>
-cudaError_t launch_reproj(const isti::FrameParams &p, cudaStream_t stream)
+template <int SW, int SI, bool MAV, int G>
+cudaError_t launch_reproj_g(const isti::FrameParams &p, cudaStream_t stream)
 {
-    const size_t smem = isti::reproj_smem<SW>(p.n_views, p.n_frames); // beyond 48 KiB for large batches
+    const size_t smem = isti::reproj_smem<SW, G>(p.n_views, p.n_frames); // beyond 48 KiB for large batches
     if (smem > 48 * 1024)
     {
-        cudaError_t e = cudaFuncSetAttribute(isti::reproj_kernel<SW, SI, MAV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(isti::reproj_kernel<SW, SI, MAV, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess)
             return e;
     }
     const dim3 gr((p.out_w + 31) / 32, (p.out_h + isti::ROWS - 1) / isti::ROWS);
-    isti::reproj_kernel<SW, SI, MAV><<<gr, dim3(32, p.n_views), smem, stream>>>(p);
+    isti::reproj_kernel<SW, SI, MAV, G><<<gr, dim3(32, p.n_views), smem, stream>>>(p);
     return cudaGetLastError();
+}
+
+// One frame searched at a time: measured on GB300 (1080p, 6 views, 3 frames), searching
+// 2 or 3 frames together raises the register count to 64-92 and the launch time by ~65 %.
+template <int SW, int SI, bool MAV>
+cudaError_t launch_reproj(const isti::FrameParams &p, cudaStream_t stream)
+{
+    return launch_reproj_g<SW, SI, MAV, 1>(p, stream);
 }
 
 // Enqueues the three kernels of one batch; events (optional) are recorded after init and splat.
