@@ -21,7 +21,7 @@ CSRC = os.path.join(PKG_DIR, "csrc")
 INCLUDE = os.path.join(REPO_DIR, "include")
 
 CUDA_ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CUDA_SOURCES = ["isti_render.cu"]
+CUDA_SOURCES = ["isti_render.cu"]  # includes isti_kernels.cuh
 
 
 def _nvcc() -> str:

@@ -1,0 +1,770 @@
+// Device code of the interpolation path: init, splat and bidirectional
+// reprojection kernels (reference: src/renderer.cu of
+// DerThomy/ImageBasedSpatioTemporalInterpolation).  Included by isti_render.cu,
+// which holds the host side and the C ABI.
+//
+// A launch sequence renders a batch of 1..ISTI_MAX_BATCH_FRAMES client frames of
+// one keyframe pair:
+//  1. init:  every 64-bit splat key <- 0xfefe...fe (the reference's
+//            cudaMemset(0xfe), src/renderer.cu:632-638), pixel->clip tables,
+//            device status word <- 0;
+//  2. splat: blockIdx.z = source view; per source pixel the keyframe part
+//            (world positions, flow to the other keyframe, visibility in the main
+//            view) once, then per frame the client-camera projection, flow store
+//            and 64-bit atomicMin;
+//  3. reprojection: a block covers 2 rows x 32 output pixels with one warp per
+//            source view (view = threadIdx.y).  The block's splat-key tiles (every
+//            view, a group of frames) are fetched into shared memory by TMA
+//            (cp.async.bulk.tensor, one elected thread, mbarrier completion).
+//            Phase 1: each thread runs window initialisation + iterative search +
+//            reprojection error for its view and both rows, frame by frame.
+//            Phase 2: the (frame, row) tasks are spread over the warps; each
+//            chooses the direction per camera and the winning camera and computes
+//            the colour (second chance, soft shadows) only for the result that is
+//            written.  The reference colours every camera's result
+//            (src/renderer.cu:378-396,436); only the written one is observable and
+//            colour never feeds a choice, so the output is identical.  Phase 3
+//            writes chained outputs.
+#pragma once
+
+#include "isti.h"
+#include "isti_device.cuh"
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <utility>
+
+namespace isti
+{
+constexpr int MAX_VIEWS = 2 + 2 * ISTI_MAX_AUX_CAMS;
+constexpr int MAX_FRAMES = ISTI_MAX_BATCH_FRAMES;
+constexpr int ROWS = 2; // output rows searched together by one reprojection thread
+constexpr float FLT_MAX_F = 3.402823466e+38f;
+
+struct DevView
+{
+    const uint32_t *color; // RGBA8 packed, R in bits 0-7
+    const float *z;
+    const void *motion;
+    const uint32_t *sha, *shb, *shi;
+    unsigned long long *splat; // frame 0; frame k at + k * FrameParams::key_stride
+    float4 *cam_ff;            // frame 0; frame k at + k * FrameParams::cam_stride
+    float4 *full_ff;
+    float *lut;                // pixel2CS tables: x at [0, w), y at [w, w + h)
+    uint32_t w, h;
+    uint32_t sx, sy;           // output pixels per view pixel (aux_idx = idx / s, src/renderer.cu:433)
+    int32_t motion_fmt;
+    int32_t forward;
+    int32_t priority;
+    float err_sx, err_sy;      // res / min(res.x, res.y), computeReprojError scale (src/renderer.cu:213)
+    float inv_vp[16];          // this view's inverse viewproj
+    float vp_to[16];           // the other keyframe's viewproj (same camera)
+    float vp_main[16];         // main camera viewproj at this keyframe (visible_in_main test)
+};
+
+// Per-frame settings (RenderInfo / AdditionalRenderInfo, include/renderer.h:18-35)
+struct FrameCfg
+{
+    float alpha;
+    int32_t fpa, sfpa, no_shadows;
+};
+
+struct FrameParams
+{
+    DevView v[MAX_VIEWS];
+    float cam_vp[MAX_FRAMES][16];
+    uint32_t *out[MAX_FRAMES];
+    FrameCfg f[MAX_FRAMES];
+    size_t key_stride; // elements between frames in the key block
+    size_t cam_stride; // elements between frames in the cam-flow block
+    ulonglong2 *keys;  // the whole key block (16-byte units) for the init kernel
+    size_t key_units;
+    int32_t *status;   // device status word: 0 ok, ISTI_ERR_TIMEOUT after a bounded wait gave up
+    uint32_t out_w, out_h;
+    int32_t n_views, n_aux, n_frames, linear, chain;
+    int32_t use_tma;          // key tiles fetched by TMA (every view's row pitch a multiple of 16 bytes)
+    int32_t frames_per_group; // frames whose key tiles are resident in shared memory together
+};
+
+// One 3-D tensor map per source view over its splat keys: (x, y, frame), u64 elements.
+struct KeyMaps
+{
+    CUtensorMap m[MAX_VIEWS];
+};
+
+// ---- TMA / mbarrier (PTX) ----
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.b32 %0, 1, 0, p;\n}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+// Waits for phase `parity` of the barrier with an iteration limit; on timeout the device
+// status word is set and the wait is retried once more with the same limit (the copies
+// may still be landing), then the block carries on.
+__device__ __forceinline__ void mbar_wait_bounded(unsigned long long *bar, uint32_t parity, int32_t *status)
+{
+    constexpr uint32_t LIMIT = 1u << 22;
+    for (uint32_t i = 0; i < LIMIT; i++)
+        if (mbar_try_wait(bar, parity))
+            return;
+    atomicExch(status, (int32_t)ISTI_ERR_TIMEOUT);
+    for (uint32_t i = 0; i < LIMIT; i++)
+        if (mbar_try_wait(bar, parity))
+            return;
+}
+
+// 3-D tiled bulk copy global -> shared, completion counted on `bar`.  x * 8 bytes must be a
+// multiple of 16 (x even); x and y may be negative or past the end (zero fill).
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, unsigned long long *bar)
+{
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// ---- border-addressed loads: zero outside the image (cudaAddressModeBorder) ----
+
+__device__ __forceinline__ float ld_f(const float *img, uint32_t x, uint32_t y, uint32_t w, uint32_t h)
+{
+    return (x < w && y < h) ? __ldg(img + (y * w + x)) : 0.0f;
+}
+__device__ __forceinline__ float4 ld_f4(const float4 *img, uint32_t x, uint32_t y, uint32_t w, uint32_t h)
+{
+    return (x < w && y < h) ? __ldg(img + (y * w + x)) : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+__device__ __forceinline__ uint32_t ld_c(const uint32_t *img, uint32_t x, uint32_t y, uint32_t w, uint32_t h)
+{
+    return (x < w && y < h) ? __ldg(img + (y * w + x)) : 0u;
+}
+
+__device__ __forceinline__ float4 load_motion(const DevView &v, uint32_t idx)
+{
+    if (v.motion_fmt == ISTI_MOTION_F32X4)
+        return __ldg(static_cast<const float4 *>(v.motion) + idx);
+    if (v.motion_fmt == ISTI_MOTION_F16X3)
+    {
+        const __half *m = static_cast<const __half *>(v.motion) + 3 * (size_t)idx;
+        return make_float4(__half2float(m[0]), __half2float(m[1]), __half2float(m[2]), 0.0f);
+    }
+    return make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// pixel2CS of pixel (x, y) of view v from its tables; direct formula outside the image
+__device__ __forceinline__ float2 view_pixel2cs(const DevView &v, uint32_t x, uint32_t y)
+{
+    if (x < v.w && y < v.h)
+        return make_float2(__ldg(v.lut + x), __ldg(v.lut + v.w + y));
+    return pixel2cs(x, y, v.w, v.h);
+}
+
+// ---- key initialisation (cudaMemset 0xfe, src/renderer.cu:632-638) + pixel->clip tables ----
+
+__global__ void __launch_bounds__(256) init_kernel(const __grid_constant__ FrameParams p)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const ulonglong2 empty = make_ulonglong2(SPLAT_EMPTY, SPLAT_EMPTY);
+    for (size_t i = t; i < p.key_units; i += stride)
+        p.keys[i] = empty;
+    if (t == 0)
+        *p.status = 0;
+    if (t < 65536)
+        for (int k = 0; k < p.n_views; k++)
+        {
+            const DevView &v = p.v[k];
+            if (t < v.w)
+                v.lut[t] = pixel2cs((uint32_t)t, 0, v.w, 1).x;
+            if (t < v.h)
+                v.lut[v.w + t] = pixel2cs(0, (uint32_t)t, 1, v.h).y;
+        }
+}
+
+// ---- computeFlowFields_sortedSplatting_kernel, src/renderer.cu:76-146 ----
+
+__global__ void __launch_bounds__(256) splat_kernel(const __grid_constant__ FrameParams p)
+{
+    const DevView &v = p.v[blockIdx.z];
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= v.w || y >= v.h)
+        return;
+    const uint32_t idx = y * v.w + x;
+
+    // keyframe part, independent of the client camera
+    const float z_from = __ldg(v.z + idx);
+    const float4 om = load_motion(v, idx);
+    const float pcx = __ldg(v.lut + x), pcy = __ldg(v.lut + v.w + y); // pixel2CS(idx2D, resolution)
+    const float4 cs_from = make_float4(pcx, pcy, z_from, 1.0f);
+    const float4 ws_from = project(v.inv_vp, cs_from);
+    const float4 moved = make_float4(__fadd_rn(pcx, om.x), __fadd_rn(pcy, om.y), __fadd_rn(z_from, om.z), 1.0f);
+    const float4 ws_to = project(v.inv_vp, moved);
+
+    // visible_in_main: WS2CS(posWS_from, viewproj_mat_from_main) inside +-(1 - 1e-3), src/renderer.cu:104-107
+    const float4 cm = matvec(v.vp_main, ws_from);
+    const float lim = 1.0f - 1e-3f;
+    const bool visible = quotient_inside(cm.x, cm.w, lim) && quotient_inside(cm.y, cm.w, lim) && quotient_inside(cm.z, cm.w, lim);
+    const float vis = visible ? 1.0f : 0.0f;
+
+    const float4 cs_to = project(v.vp_to, ws_to);
+    const float fmx = __fsub_rn(cs_to.x, cs_from.x), fmy = __fsub_rn(cs_to.y, cs_from.y), fmz = __fsub_rn(cs_to.z, cs_from.z);
+    v.full_ff[idx] = make_float4(fmx, fmy, fmz, vis);
+    const float4 d_ws = make_float4(__fsub_rn(ws_to.x, ws_from.x), __fsub_rn(ws_to.y, ws_from.y), __fsub_rn(ws_to.z, ws_from.z),
+                                    __fsub_rn(ws_to.w, ws_from.w));
+
+    // client-camera part, per frame
+    for (int k = 0; k < p.n_frames; k++)
+    {
+        const float wg = v.forward ? p.f[k].alpha : __fsub_rn(1.0f, p.f[k].alpha);
+        unsigned long long *keys = v.splat + k * p.key_stride;
+        float4 *cam = v.cam_ff + k * p.cam_stride;
+        if (!p.linear)
+        {
+            const float4 scaled = make_float4(__fadd_rn(ws_from.x, __fmul_rn(wg, d_ws.x)), __fadd_rn(ws_from.y, __fmul_rn(wg, d_ws.y)),
+                                              __fadd_rn(ws_from.z, __fmul_rn(wg, d_ws.z)), __fadd_rn(ws_from.w, __fmul_rn(wg, d_ws.w)));
+            const float4 pc = project(p.cam_vp[k], scaled);
+            cam[idx] = make_float4(__fsub_rn(pc.x, cs_from.x), __fsub_rn(pc.y, cs_from.y), __fsub_rn(pc.z, cs_from.z), vis);
+            const float depth_cam = z_to_depth(pc.z);
+            const int2 pix = cs2pixel(pc.x, pc.y, v.w, v.h);
+            if (in_range(pix, v.w, v.h) && !(depth_cam < 0.0f))
+                atomicMin(keys + ((uint32_t)pix.y * v.w + (uint32_t)pix.x), encode_key(depth_cam, x, y));
+        }
+        else
+        {
+            cam[idx] = make_float4(__fmul_rn(fmx, wg), __fmul_rn(fmy, wg), __fmul_rn(fmz, wg), vis);
+            atomicMin(keys + idx, encode_key(z_to_depth(z_from), x, y));
+        }
+    }
+}
+
+// ---- colour: colorFromShadow / secondChanceAndBlend_kernel, src/renderer.cu:217-327 ----
+
+// colorFromShadow (level-index form), src/renderer.cu:217-268
+__device__ uint32_t color_from_shadow_idx(uint32_t sidx, int32_t sfpa, const DevView &v, uint32_t px, uint32_t py)
+{
+    const uint32_t main_color = ld_c(v.color, px, py, v.w, v.h);
+    if (sidx < (uint32_t)sfpa && sidx > 0)
+    {
+        const uint32_t si = ld_c(v.shi, px, py, v.w, v.h);
+        const uint32_t bf = ((si & 255u) << 16) | (((si >> 8) & 255u) << 8) | ((si >> 16) & 255u);
+        if (v.shb != nullptr && bf != 0)
+        {
+            const int32_t init_val = (int32_t)(bf & SOFTSHADOW_VAL_MASK);
+            const int32_t my_val = (int32_t)((bf >> (SOFTSHADOW_BITS * sidx)) & SOFTSHADOW_VAL_MASK);
+            int32_t mn = (int32_t)SOFTSHADOW_VAL_MASK, mx = 0;
+            for (int32_t i = 0; i < sfpa; i++)
+            {
+                const int32_t lv = (int32_t)((bf >> (SOFTSHADOW_BITS * (uint32_t)i)) & SOFTSHADOW_VAL_MASK);
+                mn = min(mn, lv);
+                mx = max(mx, lv);
+            }
+            const float t = __fdiv_rn((float)(my_val - mn), (float)(mx - mn));
+            const uint32_t cmin = mn == init_val ? main_color : ld_c(v.sha, px, py, v.w, v.h);
+            const uint32_t cmax = mx == init_val ? main_color : ld_c(v.shb, px, py, v.w, v.h);
+            // (float)(1.0 - (double)t): t is k / d with d in {1, 2, 3} (or NaN), for which the
+            // double difference is exact, so one float subtraction rounds identically.
+            const float omt = __fsub_rn(1.0f, t);
+            uint32_t r = 255u << 24;
+#pragma unroll
+            for (int c = 0; c < 3; c++)
+            {
+                const float a = (float)((cmin >> (8 * c)) & 255u), b = (float)((cmax >> (8 * c)) & 255u);
+                r |= cvt_u8(__fadd_rn(__fmul_rn(a, omt), __fmul_rn(b, t))) << (8 * c);
+            }
+            return r;
+        }
+    }
+    return main_color;
+}
+
+struct ShadowFrames
+{
+    uint32_t frame_idx, sfx, sfy;
+    float sft;
+};
+
+// frame_idx / shadow sub-frames, src/renderer.cu:359-364
+__device__ __forceinline__ ShadowFrames shadow_frames(const FrameCfg &c)
+{
+    ShadowFrames sf;
+    const float fa = __fmul_rn((float)c.fpa, c.alpha);
+    const float sa = __fmul_rn((float)c.sfpa, c.alpha);
+    sf.frame_idx = __float2uint_rn(fa);
+    sf.sfx = __float2uint_rd(__fadd_rn(sa, 1e-9f));
+    sf.sfy = __float2uint_ru(__fsub_rn(sa, 1e-9f));
+    sf.sft = __fsub_rn(sa, (float)sf.sfx);
+    return sf;
+}
+
+// colorFromShadow (two sub-frame form), src/renderer.cu:270-295
+__device__ uint32_t color_from_shadow(const ShadowFrames &sf, const FrameCfg &c, const DevView &v, uint32_t px, uint32_t py)
+{
+    if (c.no_shadows || sf.sfx >= (uint32_t)c.sfpa || sf.sfy == 0 || v.sha == nullptr)
+        return ld_c(v.color, px, py, v.w, v.h);
+    const int32_t sfpa = c.sfpa;
+    const uint32_t vx = (uint32_t)(v.forward ? (int32_t)sf.sfx : sfpa - (int32_t)sf.sfx);
+    const uint32_t vy = (uint32_t)(v.forward ? (int32_t)sf.sfy : sfpa - (int32_t)sf.sfy);
+    if (vx == vy || vy >= (uint32_t)sfpa)
+        return color_from_shadow_idx(vx, sfpa, v, px, py);
+    if (vx >= (uint32_t)sfpa)
+        return color_from_shadow_idx(vy, sfpa, v, px, py);
+    const uint32_t a = color_from_shadow_idx(vx, sfpa, v, px, py);
+    const uint32_t b = color_from_shadow_idx(vy, sfpa, v, px, py);
+    return lerp_color_u8(a, b, sf.sft);
+}
+
+// secondChanceAndBlend_kernel<EPS_2>, src/renderer.cu:297-327
+__device__ uint32_t second_chance(float weight, const ShadowFrames &sf, const FrameCfg &c, uint32_t sx, uint32_t sy, const DevView &from,
+                                  const DevView &to, float eps2)
+{
+    const float4 m_ft = ld_f4(from.full_ff, sx, sy, from.w, from.h);
+    const float2 spcs = view_pixel2cs(from, sx, sy);
+    const float sz = ld_f(from.z, sx, sy, from.w, from.h);
+    const float pcx = __fadd_rn(spcs.x, m_ft.x), pcy = __fadd_rn(spcs.y, m_ft.y), pcz = __fadd_rn(sz, m_ft.z);
+    const int2 pp = cs2pixel(pcx, pcy, to.w, to.h);
+
+    uint32_t out = color_from_shadow(sf, c, from, sx, sy);
+    if (sf.frame_idx >= (uint32_t)c.fpa)
+        return out;
+    if (in_range(pp, to.w, to.h))
+    {
+        const uint32_t pi = (uint32_t)pp.y * to.w + (uint32_t)pp.x;
+        const float az = __ldg(to.z + pi);
+        const float4 m_tf = __ldg(to.full_ff + pi);
+        const float dx = __fsub_rn(m_ft.x, -m_tf.x), dy = __fsub_rn(m_ft.y, -m_tf.y), dz = __fsub_rn(m_ft.z, -m_tf.z);
+        if (sqrt_less(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)), EPS_3) &&
+            fabsf(__fsub_rn(az, pcz)) < eps2)
+            out = lerp_color_u8(color_from_shadow(sf, c, to, pp.x, pp.y), out, weight);
+    }
+    return out;
+}
+
+// ---- bidirectional reprojection, src/renderer.cu:148-465 ----
+
+// One direction of one camera for one output pixel: window init + search + error.
+struct DirRes
+{
+    float error;  // FLT_MAX when not searched
+    float depth;  // searched depth, else the window-initialisation depth
+    uint32_t src; // source pixel, x << 16 | y
+    uint32_t vis; // visible_in_main
+};
+
+// Result of bidirectionalReprojection for one camera (src/renderer.cu:366-397), without its colour.
+struct CamRes
+{
+    bool valid;
+    bool vis;
+    bool blend;      // always-valid 50/50 blend of both directions
+    int32_t priority;
+    float error;     // indeterminate in the reference for the blend; 0 here
+    float depth;
+    int32_t dir;     // 0 forward keyframe, 1 backward keyframe
+    uint32_t src;
+};
+
+// Shared-memory key tile of one view and frame: rows iy0 - SW .. iy0 + ROWS - 1 + SW and
+// W columns from x = (tx0 - SW) rounded down to even (the TMA start-coordinate rule for
+// 8-byte elements), covering the 32 + 2 * SW columns the window reads.
+template <int SW>
+struct Tile
+{
+    static constexpr int W = SW == 1 ? 36 : 40;
+    static constexpr int H = ROWS + 2 * SW;
+    static constexpr int ELEMS = W * H;
+    static constexpr int BYTES = ELEMS * 8; // a multiple of 128: TMA destinations stay 128-byte aligned
+};
+
+__device__ __forceinline__ int tile_x0(uint32_t tx0, int sw) { return ((int)tx0 - sw) & ~1; }
+
+__device__ __forceinline__ CamRes cam_result(const DirRes &f, const DirRes &b, const DevView &vf, const DevView &vb, float eps1, float eps2,
+                                             bool always_valid)
+{
+    CamRes r;
+    r.valid = false;
+    r.vis = false;
+    r.blend = false;
+    r.priority = 0;
+    r.error = 0.0f;
+    r.depth = 0.0f;
+    r.dir = 0;
+    r.src = 0;
+    if (f.error < eps1 || b.error < eps1)
+    {
+        const bool both = f.error < eps1 && b.error < eps1;
+        const bool similar = fabsf(__fsub_rn(depth_to_z(f.depth), depth_to_z(b.depth))) < eps2;
+        const bool choose_fwd = (both && !similar && f.depth < b.depth) || ((!both || similar) && f.error < b.error);
+        r.valid = true;
+        if (choose_fwd)
+        {
+            r.vis = f.vis || (both && similar && b.vis);
+            r.priority = vf.priority;
+            r.error = f.error;
+            r.depth = f.depth;
+            r.dir = 0;
+            r.src = f.src;
+        }
+        else
+        {
+            r.vis = b.vis || (both && similar && f.vis);
+            r.priority = vb.priority;
+            r.error = b.error;
+            r.depth = b.depth;
+            r.dir = 1;
+            r.src = b.src;
+        }
+    }
+    else if (always_valid)
+    {
+        r.valid = true;
+        r.blend = true;
+    }
+    return r;
+}
+
+// Chooses among the cameras of one output pixel and returns the colour to
+// write (false: keep the previous output), src/renderer.cu:400-465.
+// res points at the [n_views][32] results of this pixel's row and frame.
+template <bool MAV>
+__device__ __forceinline__ bool resolve_pixel(const DirRes *res, int lane, const FrameParams &p, const FrameCfg &c, uint32_t &color)
+{
+    const CamRes m = cam_result(res[lane], res[32 + lane], p.v[0], p.v[1], EPS_1_FULL_RES, EPS_2_FULL_RES, MAV);
+    CamRes best;
+    best.valid = false;
+    best.vis = false;
+    best.priority = 0;
+    best.error = 0.0f;
+    best.depth = 0.0f;
+    int best_cam = 0;
+    const int n_cams = p.n_views / 2;
+    for (int cam = 1; cam < n_cams; cam++)
+    {
+        const CamRes r = cam_result(res[(2 * cam) * 32 + lane], res[(2 * cam + 1) * 32 + lane], p.v[2 * cam], p.v[2 * cam + 1], EPS_1_LOW_RES,
+                                    EPS_2_LOW_RES, false);
+        bool take = !best.valid;
+        if (best.valid && r.valid)
+        {
+            const bool similar = fabsf(__fsub_rn(depth_to_z(best.depth), depth_to_z(r.depth))) < EPS_2_LOW_RES;
+            take = (!similar && r.depth < best.depth) || (similar && r.priority >= best.priority && r.error < best.error);
+        }
+        if (take)
+        {
+            best = r;
+            best_cam = cam;
+        }
+    }
+    int cam = -1;
+    CamRes fin = m;
+    if (m.valid)
+        cam = 0;
+    if (best.valid)
+    {
+        bool choose_aux = !m.valid;
+        if (m.valid && !best.vis)
+        {
+            const bool similar = fabsf(__fsub_rn(depth_to_z(best.depth), depth_to_z(m.depth))) < EPS_2_LOW_RES;
+            choose_aux = !similar && best.depth < m.depth;
+        }
+        if (choose_aux)
+        {
+            cam = best_cam;
+            fin = best;
+        }
+    }
+    if (cam < 0)
+        return false; // temporal hole filling: keep the previous output (src/renderer.cu:416-419,462-463)
+
+    const ShadowFrames sf = shadow_frames(c);
+    const DevView &vf = p.v[2 * cam], &vb = p.v[2 * cam + 1];
+    const float eps2 = cam == 0 ? EPS_2_FULL_RES : EPS_2_LOW_RES;
+    const float oma = __fsub_rn(1.0f, c.alpha);
+    if (fin.blend)
+    {
+        const DirRes &f = res[lane], &b = res[32 + lane];
+        const uint32_t cf = second_chance(oma, sf, c, f.src >> 16, f.src & 0xFFFFu, vf, vb, eps2);
+        const uint32_t cb = second_chance(c.alpha, sf, c, b.src >> 16, b.src & 0xFFFFu, vb, vf, eps2);
+        color = lerp_color_u8(cf, cb, 0.5f);
+    }
+    else if (fin.dir == 0)
+        color = second_chance(oma, sf, c, fin.src >> 16, fin.src & 0xFFFFu, vf, vb, eps2);
+    else
+        color = second_chance(c.alpha, sf, c, fin.src >> 16, fin.src & 0xFFFFu, vb, vf, eps2);
+    return true;
+}
+
+// Upper bound for the window comparison, from the depth bits l of the current lowest key.
+// The reference replaces the lowest entry by a candidate c with c > 0 when
+//   !isfinite(l) || l < 0 || c < l            (src/renderer.cu:167)
+// For c > 0 (bits in [1, 0x7f800000], +inf included) this is c_bits < bound(l_bits):
+//   l = +-inf, NaN, or negative non-zero  -> always true  -> bound 0xffffffff;
+//   l = -0.0                              -> always false -> bound 0;
+//   l in [+0, +max finite]                -> c < l, monotonic in the bits -> bound l_bits.
+__device__ __forceinline__ uint32_t key_bound(uint32_t l)
+{
+    return l == 0x80000000u ? 0u : (l >= 0x7f800000u ? 0xffffffffu : l);
+}
+
+// initializeSearchFromSplatting<SW> on a shared-memory tile, src/renderer.cu:148-175, same
+// scan order.  Tile row `row` holds the view row of this pixel; keys outside the view read
+// as 0 (depth +0.0), which the window never selects, exactly like the reference's skipped
+// out-of-range neighbours.  Returns the selected raw key.
+template <int SW>
+__device__ __forceinline__ unsigned long long window_key(const unsigned long long *tile, int row, int col)
+{
+    using T = Tile<SW>;
+    unsigned long long best = tile[row * T::W + col];
+    uint32_t bound = key_bound((uint32_t)(best >> 32));
+#pragma unroll
+    for (int yo = -SW; yo <= SW; yo++)
+#pragma unroll
+        for (int xo = -SW; xo <= SW; xo++)
+        {
+            const unsigned long long c = tile[(row + yo) * T::W + col + xo];
+            const uint32_t cb = (uint32_t)(c >> 32);
+            if (cb - 1u < 0x7f800000u && cb < bound) // c > 0 && (the reference's replacement test)
+            {
+                best = c;
+                bound = key_bound(cb);
+            }
+        }
+    return best;
+}
+
+// bidirectionalReprojection_kernel<SW, SI, MAIN_ALWAYS_VALID>, src/renderer.cu:400-465
+// block = (32, n_views): output rows ROWS * blockIdx.y + {0, 1}, 32 pixels each, one warp per source view.
+template <int SW, int SI, bool MAV>
+__global__ void __launch_bounds__(32 * MAX_VIEWS) reproj_kernel(const __grid_constant__ FrameParams p, const __grid_constant__ KeyMaps km)
+{
+    using T = Tile<SW>;
+    // dynamic shared memory only (no static __shared__ in front of it): the key tiles start at
+    // the 1 KiB-aligned window base, so every TMA destination is 128-byte aligned
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const int nv = p.n_views, nf = p.n_frames, fg = p.frames_per_group;
+    unsigned long long *tiles = reinterpret_cast<unsigned long long *>(smem);                 // [fg][nv][H][W]
+    DirRes *res = reinterpret_cast<DirRes *>(smem + (size_t)fg * nv * T::BYTES);             // [nf][ROWS][nv][32]
+    uint32_t *cols = reinterpret_cast<uint32_t *>(res + nf * ROWS * nv * 32);                 // [nf][ROWS][32]
+    uint32_t *valid = cols + nf * ROWS * 32;                                                 // [nf][ROWS][32]
+    unsigned long long &bar = *reinterpret_cast<unsigned long long *>(valid + nf * ROWS * 32); // TMA completion barrier
+
+    const int lane = threadIdx.x, vw = threadIdx.y;
+    const uint32_t x0 = blockIdx.x * 32, x = x0 + lane, y0 = blockIdx.y * ROWS;
+    const bool xok = x < p.out_w;
+    const bool leader = lane == 0 && vw == 0;
+    if (p.use_tma)
+    {
+        if (leader)
+            mbar_init(&bar, 1);
+        __syncthreads();
+    }
+    {
+        const DevView &v = p.v[vw];
+        const uint32_t ix = v.sx == 1 ? x : x / v.sx, tx0 = v.sx == 1 ? x0 : x0 / v.sx;
+        const uint32_t iy0 = v.sy == 1 ? y0 : y0 / v.sy, iy1 = v.sy == 1 ? y0 + 1 : (y0 + 1) / v.sy;
+        const bool rok[ROWS] = {xok, xok && y0 + 1 < p.out_h};
+        const bool fwd = (vw & 1) == 0;
+        const int xs = tile_x0(tx0, SW);
+        const int col = (int)ix - xs;
+        const int wrow[ROWS] = {SW, (int)(iy1 - iy0) + SW}; // tile row of each output row's window centre
+        // pixel2CS of the output pixels in the main view (the search target) and in this view (the error)
+        const DevView &v0 = p.v[0];
+        const uint32_t xc = min(x, p.out_w - 1), y1c = min(y0 + 1, p.out_h - 1);
+        const float qx = __ldg(v0.lut + xc);
+        const float qy[ROWS] = {__ldg(v0.lut + v0.w + y0), __ldg(v0.lut + v0.w + y1c)};
+        const float pcx = __ldg(v.lut + min(ix, v.w - 1));
+        const float pcy[ROWS] = {__ldg(v.lut + v.w + iy0), __ldg(v.lut + v.w + min(iy1, v.h - 1))};
+        const uint32_t vwid = v.w, vhei = v.h;
+#pragma unroll 1
+        for (int k0 = 0, grp = 0; k0 < nf; k0 += fg, grp++)
+        {
+            const int ng = min(fg, nf - k0);
+            if (k0 > 0)
+                __syncthreads(); // every warp is done with the previous group's tiles
+            if (p.use_tma)
+            {
+                if (leader)
+                {
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    mbar_expect_tx(&bar, (uint32_t)(ng * nv * T::BYTES));
+                    for (int g = 0; g < ng; g++)
+                        for (int w = 0; w < nv; w++)
+                        {
+                            const DevView &vv = p.v[w];
+                            const uint32_t wx0 = vv.sx == 1 ? x0 : x0 / vv.sx, wy0 = vv.sy == 1 ? y0 : y0 / vv.sy;
+                            tma_load_3d(tiles + (size_t)(g * nv + w) * T::ELEMS, &km.m[w], tile_x0(wx0, SW), (int)wy0 - SW, k0 + g, &bar);
+                        }
+                }
+                mbar_wait_bounded(&bar, (uint32_t)(grp & 1), p.status);
+            }
+            else
+            {
+                for (int g = 0; g < ng; g++)
+                {
+                    const unsigned long long *keys = v.splat + (k0 + g) * p.key_stride;
+                    unsigned long long *tg = tiles + (size_t)(g * nv + vw) * T::ELEMS;
+#pragma unroll
+                    for (int r = 0; r < T::H; r++)
+                    {
+                        const uint32_t gy = iy0 - SW + r;
+                        const bool row_ok = gy < vhei;
+                        for (int c = lane; c < T::W; c += 32)
+                        {
+                            const uint32_t gx = (uint32_t)(xs + c);
+                            tg[r * T::W + c] = (row_ok && gx < vwid) ? __ldg(keys + (gy * vwid + gx)) : 0ull;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+
+#pragma unroll 1
+            for (int g = 0; g < ng; g++)
+            {
+                const int k = k0 + g;
+                const unsigned long long *tg = tiles + (size_t)(g * nv + vw) * T::ELEMS;
+                const float4 *cam = v.cam_ff + k * p.cam_stride;
+                const bool search_ok = !fwd || p.f[k].alpha < 1.0f;
+                bool s[ROWS];
+                uint32_t ax[ROWS], ay[ROWS];
+                float d_init[ROWS];
+#pragma unroll
+                for (int r = 0; r < ROWS; r++)
+                {
+                    const unsigned long long lo = window_key<SW>(tg, wrow[r], col);
+                    d_init[r] = __uint_as_float((uint32_t)(lo >> 32));
+                    ax[r] = ((uint32_t)lo) >> 16;
+                    ay[r] = (uint32_t)lo & 0xFFFFu;
+                    s[r] = rok[r] && search_ok && d_init[r] > 0.0f;
+                }
+                // iterativeSearch<SI>, src/renderer.cu:177-202, both rows interleaved.  The start is a
+                // splatted source pixel and every accepted step is in range: no border handling needed.
+#pragma unroll
+                for (int i = 0; i < SI; i++)
+                {
+                    float4 m[ROWS];
+#pragma unroll
+                    for (int r = 0; r < ROWS; r++)
+                        m[r] = s[r] ? __ldg(cam + (ay[r] * vwid + ax[r])) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                    for (int r = 0; r < ROWS; r++)
+                    {
+                        const int2 t = cs2pixel(__fsub_rn(qx, m[r].x), __fsub_rn(qy[r], m[r].y), vwid, vhei);
+                        if (s[r] && in_range(t, vwid, vhei))
+                        {
+                            ax[r] = (uint32_t)t.x;
+                            ay[r] = (uint32_t)t.y;
+                        }
+                    }
+                }
+                // final flow, depth and computeReprojError, src/renderer.cu:338-341, 204-215
+                float4 m[ROWS];
+                float zz[ROWS], fx[ROWS], fy[ROWS];
+#pragma unroll
+                for (int r = 0; r < ROWS; r++)
+                {
+                    m[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    zz[r] = fx[r] = fy[r] = 0.f;
+                    if (s[r])
+                    {
+                        const uint32_t si = ay[r] * vwid + ax[r];
+                        m[r] = __ldg(cam + si);
+                        zz[r] = __ldg(v.z + si);
+                        fx[r] = __ldg(v.lut + ax[r]);
+                        fy[r] = __ldg(v.lut + vwid + ay[r]);
+                    }
+                }
+#pragma unroll
+                for (int r = 0; r < ROWS; r++)
+                {
+                    DirRes d;
+                    d.error = FLT_MAX_F;
+                    d.depth = d_init[r];
+                    d.vis = 0;
+                    if (s[r])
+                    {
+                        d.depth = z_to_depth(__fadd_rn(zz[r], m[r].z));
+                        const float ex = __fmul_rn(__fsub_rn(__fadd_rn(fx[r], m[r].x), pcx), v.err_sx);
+                        const float ey = __fmul_rn(__fsub_rn(__fadd_rn(fy[r], m[r].y), pcy[r]), v.err_sy);
+                        d.error = __fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)));
+                        d.vis = m[r].w > 0.0f;
+                    }
+                    d.src = (ax[r] << 16) | ay[r];
+                    res[((k * ROWS + r) * nv + vw) * 32 + lane] = d;
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    // phase 2: (frame, row) tasks over the warps
+#pragma unroll 1
+    for (int t = vw; t < nf * ROWS; t += nv)
+    {
+        const int k = t / ROWS, r = t % ROWS;
+        const uint32_t y = y0 + r;
+        uint32_t color = 0;
+        const bool ok = xok && y < p.out_h && resolve_pixel<MAV>(res + t * nv * 32, lane, p, p.f[k], color);
+        if (!p.chain)
+        {
+            if (ok)
+                p.out[k][y * p.out_w + x] = color;
+        }
+        else
+        {
+            cols[t * 32 + lane] = color;
+            valid[t * 32 + lane] = ok ? 1u : 0u;
+        }
+    }
+    if (!p.chain)
+        return;
+    __syncthreads();
+    // phase 3: one persistent buffer per row, starting as out[0], copied to out[k] after frame k
+    if (vw >= ROWS)
+        return;
+    const uint32_t y = y0 + vw;
+    if (!xok || y >= p.out_h)
+        return;
+    uint32_t run = 0;
+    for (int k = 0; k < nf; k++)
+    {
+        uint32_t *o = p.out[k] + (y * p.out_w + x);
+        const int t = k * ROWS + vw;
+        if (k == 0)
+            run = *o;
+        if (valid[t * 32 + lane])
+        {
+            run = cols[t * 32 + lane];
+            *o = run;
+        }
+        else if (k > 0)
+            *o = run;
+    }
+}
+
+// Dynamic shared memory of one reprojection block.
+template <int SW>
+constexpr size_t reproj_smem(int n_views, int n_frames, int frames_per_group)
+{
+    return (size_t)frames_per_group * n_views * Tile<SW>::BYTES +
+           (size_t)n_frames * ROWS * (n_views * 32 * sizeof(DirRes) + 2 * 32 * sizeof(uint32_t)) + 16; // + mbarrier
+}
+} // namespace isti

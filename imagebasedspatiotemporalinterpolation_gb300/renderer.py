@@ -191,6 +191,12 @@ class Renderer:
         s = (stream or torch.cuda.current_stream()).cuda_stream
         check(self._lib.isti_render_batch(self._h, n, outs, ris, C.byref(frame_data.to_c()), int(chain), C.c_void_p(s)))
 
+    def device_status(self) -> int:
+        """Waits for the device; 0, or ISTI_ERR_TIMEOUT when a kernel's bounded wait gave up."""
+        s = C.c_int32()
+        check(self._lib.isti_renderer_device_status(self._h, C.byref(s)))
+        return s.value
+
     def enable_timing(self, on: bool = True) -> None:
         check(self._lib.isti_renderer_enable_timing(self._h, int(on)))
 

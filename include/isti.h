@@ -173,6 +173,11 @@ typedef struct isti_timing
     float reproj_ms;         /* summed device time of the reprojection kernel */
 } isti_timing;
 
+/* Device-side status of the last render call (no counterpart in the reference):
+ * waits for the device, then stores ISTI_OK, or ISTI_ERR_TIMEOUT when a bounded
+ * wait inside a kernel gave up (its frame is then not trustworthy). */
+isti_status isti_renderer_device_status(isti_renderer *r, int32_t *device_status);
+
 isti_status isti_renderer_enable_timing(isti_renderer *r, int32_t on);
 /* Waits for the recorded events, returns the sums and resets them. */
 isti_status isti_renderer_timing(isti_renderer *r, isti_timing *out);

@@ -32,6 +32,7 @@ def render_gpu(frame, client, prev, motion_format="f16x3", renderer=None):
     r = renderer or Renderer()
     r.render(out, client, dev)
     torch.cuda.synchronize()
+    assert r.device_status() == 0
     bufs = [r.view_buffers(k) for k in range(len(dev.views()))]
     res = (out.cpu().numpy(), [b[0].cpu().numpy().view(np.uint64) for b in bufs], [b[1].cpu().numpy() for b in bufs],
            [b[2].cpu().numpy() for b in bufs])
