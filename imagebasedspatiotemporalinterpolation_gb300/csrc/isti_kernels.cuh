@@ -61,6 +61,7 @@ struct DevView
     float inv_vp[16];          // this view's inverse viewproj
     float vp_to[16];           // the other keyframe's viewproj (same camera)
     float vp_main[16];         // main camera viewproj at this keyframe (visible_in_main test)
+    float vp_self[16];         // this view's viewproj (timewarp)
 };
 
 // Per-frame settings (RenderInfo / AdditionalRenderInfo, include/renderer.h:18-35)
@@ -74,6 +75,9 @@ struct FrameParams
 {
     DevView v[MAX_VIEWS];
     float cam_vp[MAX_FRAMES][16];
+    float cam_ivp[MAX_FRAMES][16]; // client inverse viewproj (timewarp rays)
+    double *tw_rows;               // timewarp: per-row sums of the forward keyframe's z
+    float *tw_mean;                // timewarp: mean z (the reference's ImageBuffer::average)
     uint32_t *out[MAX_FRAMES];
     FrameCfg f[MAX_FRAMES];
     size_t key_stride; // elements between frames in the key block
@@ -753,6 +757,118 @@ __global__ void __launch_bounds__(32 * MAX_VIEWS) reproj_kernel(const __grid_con
         if (valid[t * 32 + lane])
         {
             run = cols[t * 32 + lane];
+            *o = run;
+        }
+        else if (k > 0)
+            *o = run;
+    }
+}
+
+// ---- timewarp (mode 4), src/renderer.cu:467-522, 615-629 ----
+//
+// Mean NDC z of the forward keyframe (ImageBuffer::average, src/util/image_buffer.cu:80-100).
+// The reference accumulates with a float atomicAdd in an unspecified order; here every row is
+// summed left to right in double (one thread per row), the rows top to bottom in double, and
+// the total is rounded to float and divided by the pixel count in float like the reference's
+// final division.  The C oracle uses the same order.
+
+__global__ void __launch_bounds__(128) timewarp_rowsum_kernel(const __grid_constant__ FrameParams p)
+{
+    const DevView &v = p.v[0];
+    const uint32_t y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y >= v.h)
+        return;
+    double acc = 0.0;
+    for (uint32_t x = 0; x < v.w; x++)
+        acc = __dadd_rn(acc, (double)__ldg(v.z + (y * v.w + x)));
+    p.tw_rows[y] = acc;
+}
+
+__global__ void timewarp_mean_kernel(const __grid_constant__ FrameParams p)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0)
+        return;
+    const DevView &v = p.v[0];
+    double acc = 0.0;
+    for (uint32_t y = 0; y < v.h; y++)
+        acc = __dadd_rn(acc, p.tw_rows[y]);
+    *p.tw_mean = __fdiv_rn(__double2float_rn(acc), (float)(v.w * v.h));
+    *p.status = 0;
+}
+
+__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz)
+{
+    return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
+}
+
+// timewarp_kernel body for one pixel and client camera; false: the ray is parallel to the plane (no write)
+__device__ __forceinline__ bool timewarp_pixel(const float *cam_ivp, const DevView &to, const DevView &aux, bool has_aux, float depth_to,
+                                               uint32_t x, uint32_t y, uint32_t out_w, uint32_t out_h, uint32_t &color)
+{
+    const float2 pcs = pixel2cs(x, y, out_w, out_h);
+    const float4 nws = project(cam_ivp, make_float4(pcs.x, pcs.y, 0.0f, 1.0f));
+    const float4 fws = project(cam_ivp, make_float4(pcs.x, pcs.y, 1.0f, 1.0f));
+    // ray_dir = normalize(vec3(farWS - nearWS)), glm-subset normalize: v * (1 / sqrt(dot(v, v)))
+    float dx = __fsub_rn(fws.x, nws.x), dy = __fsub_rn(fws.y, nws.y), dz = __fsub_rn(fws.z, nws.z);
+    const float sd = __fdiv_rn(1.0f, __fsqrt_rn(dot3(dx, dy, dz, dx, dy, dz)));
+    dx = __fmul_rn(dx, sd);
+    dy = __fmul_rn(dy, sd);
+    dz = __fmul_rn(dz, sd);
+    // plane through inv_viewproj_mat_to[3] facing the centre of the keyframe at depth_to
+    const float4 cws = project(to.inv_vp, make_float4(0.0f, 0.0f, depth_to, 1.0f));
+    const float cpx = to.inv_vp[12], cpy = to.inv_vp[13], cpz = to.inv_vp[14], cpw = to.inv_vp[15];
+    float nx = __fsub_rn(cws.x, cpx), ny = __fsub_rn(cws.y, cpy), nz = __fsub_rn(cws.z, cpz);
+    const float nw = __fsub_rn(cws.w, cpw);
+    const float sn = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(dot3(nx, ny, nz, nx, ny, nz), __fmul_rn(nw, nw)))); // 4-component normalize
+    nx = __fmul_rn(nx, sn);
+    ny = __fmul_rn(ny, sn);
+    nz = __fmul_rn(nz, sn);
+    const float denom = dot3(dx, dy, dz, nx, ny, nz);
+    if (fabsf(denom) < 1e-6f)
+        return false;
+    const float t = __fdiv_rn(dot3(__fsub_rn(cpx, nws.x), __fsub_rn(cpy, nws.y), __fsub_rn(cpz, nws.z), nx, ny, nz), denom);
+    const float4 hit = make_float4(__fadd_rn(nws.x, __fmul_rn(t, dx)), __fadd_rn(nws.y, __fmul_rn(t, dy)), __fadd_rn(nws.z, __fmul_rn(t, dz)), 1.0f);
+    const float4 pc = project(to.vp_self, hit); // WS2CS(intersection, viewproj_mat_to)
+    int2 pix = cs2pixel(pc.x, pc.y, to.w, to.h);
+    const DevView *src = &to;
+    if (!in_range(pix, to.w, to.h) && has_aux)
+    {
+        const float4 pa = project(aux.vp_self, hit);
+        pix = cs2pixel(pa.x, pa.y, aux.w, aux.h);
+        src = &aux;
+    }
+    pix.x = min(max(pix.x, 0), (int)src->w - 1);
+    pix.y = min(max(pix.y, 0), (int)src->h - 1);
+    color = __ldg(src->color + ((uint32_t)pix.y * src->w + (uint32_t)pix.x));
+    return true;
+}
+
+// One thread per output pixel, looping over the frames of the batch (chained like the reprojection).
+__global__ void __launch_bounds__(256) timewarp_kernel(const __grid_constant__ FrameParams p)
+{
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= p.out_w || y >= p.out_h)
+        return;
+    const bool has_aux = p.n_aux > 0;
+    const float depth_to = *p.tw_mean;
+    uint32_t run = 0;
+    for (int k = 0; k < p.n_frames; k++)
+    {
+        uint32_t color = 0;
+        const bool ok = timewarp_pixel(p.cam_ivp[k], p.v[0], p.v[has_aux ? 2 : 0], has_aux, depth_to, x, y, p.out_w, p.out_h, color);
+        uint32_t *o = p.out[k] + (y * p.out_w + x);
+        if (!p.chain)
+        {
+            if (ok)
+                *o = color;
+            continue;
+        }
+        if (k == 0)
+            run = *o;
+        if (ok)
+        {
+            run = color;
             *o = run;
         }
         else if (k > 0)

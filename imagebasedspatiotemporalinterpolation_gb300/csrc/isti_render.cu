@@ -88,8 +88,6 @@ isti_status validate(int n_frames, void *const *outs, const isti_render_info *in
             return fail(ISTI_ERR_INVALID_ARG, "NULL output buffer");
         if (reinterpret_cast<uintptr_t>(outs[k]) & 3u)
             return fail(ISTI_ERR_INVALID_ARG, "output buffers must be 4-byte aligned");
-        if (f.mode == ISTI_MODE_TIMEWARP)
-            return fail(ISTI_ERR_UNSUPPORTED, "timewarp mode is not implemented");
         if (f.mode < 0 || f.mode > ISTI_MODE_TIMEWARP)
             return fail(ISTI_ERR_INVALID_ARG, "unknown render mode");
         if (f.shadow_frames_per_anchor < 0 || f.shadow_frames_per_anchor > 16)
@@ -156,6 +154,36 @@ Layout layout_of(const isti_view *const *views, int n_views, int n_frames)
     return l;
 }
 
+// Timewarp (mode 4) needs no splat intermediates: [row sums, double per row of the
+// forward keyframe][mean z][status word].
+Layout timewarp_layout(const isti_view *const *views)
+{
+    Layout l{};
+    l.total = align_up((size_t)views[0]->height * sizeof(double), 256) + 256 + STATUS_BYTES;
+    return l;
+}
+
+Layout layout_for(int mode, const isti_view *const *views, int n_views, int n_frames)
+{
+    return mode == ISTI_MODE_TIMEWARP ? timewarp_layout(views) : layout_of(views, n_views, n_frames);
+}
+
+// Enqueues the timewarp of one batch (src/renderer.cu:615-629): mean z of the forward
+// keyframe (two kernels), then one kernel over the output pixels.
+cudaError_t launch_timewarp(isti::FrameParams &p, char *base, cudaStream_t stream, cudaEvent_t after_mean, cudaEvent_t after_nothing)
+{
+    p.tw_rows = reinterpret_cast<double *>(base);
+    p.tw_mean = reinterpret_cast<float *>(base + align_up((size_t)p.v[0].h * sizeof(double), 256));
+    isti::timewarp_rowsum_kernel<<<(p.v[0].h + 127) / 128, 128, 0, stream>>>(p);
+    isti::timewarp_mean_kernel<<<1, 32, 0, stream>>>(p);
+    if (after_mean)
+        cudaEventRecord(after_mean, stream);
+    if (after_nothing)
+        cudaEventRecord(after_nothing, stream); // no splat stage in this mode
+    isti::timewarp_kernel<<<dim3((p.out_w + 31) / 32, (p.out_h + 7) / 8), dim3(32, 8), 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
 // Fills the kernel parameters for one batch whose intermediates live at `base`.
 void fill_params(isti::FrameParams &p, int n_frames, void *const *outs, const isti_render_info *infos, const isti_frame_data *frame,
                  const isti_view *const *views, int n_views, const Layout &l, char *base, bool chain)
@@ -190,6 +218,7 @@ void fill_params(isti::FrameParams &p, int n_frames, void *const *outs, const is
         std::memcpy(d.inv_vp, v.inv_viewproj, sizeof d.inv_vp);
         std::memcpy(d.vp_to, vp_to, sizeof d.vp_to);
         std::memcpy(d.vp_main, vp_main, sizeof d.vp_main);
+        std::memcpy(d.vp_self, v.viewproj, sizeof d.vp_self);
         const size_t px = (size_t)v.width * v.height;
         d.splat = reinterpret_cast<unsigned long long *>(base + off_key);
         d.cam_ff = reinterpret_cast<float4 *>(base + off_cam);
@@ -203,6 +232,7 @@ void fill_params(isti::FrameParams &p, int n_frames, void *const *outs, const is
     for (int k = 0; k < n_frames; k++)
     {
         std::memcpy(p.cam_vp[k], infos[k].viewproj, sizeof p.cam_vp[k]);
+        std::memcpy(p.cam_ivp[k], infos[k].inv_viewproj, sizeof p.cam_ivp[k]);
         p.out[k] = static_cast<uint32_t *>(outs[k]);
         p.f[k].alpha = infos[k].alpha;
         p.f[k].fpa = infos[k].frames_per_anchor;
@@ -336,7 +366,8 @@ isti_status render_batch(isti_renderer *r, int n_frames, void *const *outs, cons
     isti_status st = validate(n_frames, outs, infos, frame, views, n_views);
     if (st != ISTI_OK)
         return st;
-    const Layout l = layout_of(views, n_views, n_frames);
+    const bool timewarp = infos[0].mode == ISTI_MODE_TIMEWARP;
+    const Layout l = layout_for(infos[0].mode, views, n_views, n_frames);
 
     int cur = 0;
     cudaError_t e = cudaGetDevice(&cur);
@@ -384,7 +415,8 @@ isti_status render_batch(isti_renderer *r, int n_frames, void *const *outs, cons
         r->timed_launches += 3;
         cudaEventRecord(ev[0], stream);
     }
-    e = launch_batch(r->last, infos[0].mode, stream, ev ? ev[1] : nullptr, ev ? ev[2] : nullptr);
+    e = timewarp ? launch_timewarp(r->last, base, stream, ev ? ev[1] : nullptr, ev ? ev[2] : nullptr)
+                 : launch_batch(r->last, infos[0].mode, stream, ev ? ev[1] : nullptr, ev ? ev[2] : nullptr);
     if (ev)
         cudaEventRecord(ev[3], stream);
     if (e != cudaSuccess)
@@ -523,12 +555,13 @@ isti_status isti_renderer_view_buffers(const isti_renderer *r, int32_t view, con
         return fail(ISTI_ERR_INVALID_ARG, "view index out of range");
     const int k = view / nv;
     const isti::DevView &d = r->last.v[view % nv];
+    const bool materialised = r->last.tw_mean == nullptr; // timewarp keeps no splat intermediates
     if (splat)
-        *splat = reinterpret_cast<const uint64_t *>(d.splat + k * r->last.key_stride);
+        *splat = materialised ? reinterpret_cast<const uint64_t *>(d.splat + k * r->last.key_stride) : nullptr;
     if (cam_ff)
-        *cam_ff = reinterpret_cast<const float *>(d.cam_ff + k * r->last.cam_stride);
+        *cam_ff = materialised ? reinterpret_cast<const float *>(d.cam_ff + k * r->last.cam_stride) : nullptr;
     if (full_ff)
-        *full_ff = reinterpret_cast<const float *>(d.full_ff);
+        *full_ff = materialised ? reinterpret_cast<const float *>(d.full_ff) : nullptr;
     if (width)
         *width = d.w;
     if (height)
@@ -587,7 +620,7 @@ extern "C" isti_status isti_render_noalloc(void *out_rgba, const isti_render_inf
     isti_status st = validate(1, outs, info, frame, views, n_views);
     if (st != ISTI_OK)
         return st;
-    const Layout l = layout_of(views, n_views, 1);
+    const Layout l = layout_for(info->mode, views, n_views, 1);
     if (l.total > ISTI_NOALLOC_SCRATCH_BYTES)
         return fail(ISTI_ERR_INVALID_ARG, "frame needs " + std::to_string(l.total) + " bytes of scratch; isti_render_noalloc holds at most " +
                                               std::to_string((size_t)ISTI_NOALLOC_SCRATCH_BYTES) + " (use isti_render for larger frames)");
@@ -604,7 +637,8 @@ extern "C" isti_status isti_render_noalloc(void *out_rgba, const isti_render_inf
     // The array keeps the previous call's contents: the init kernel resets every key to
     // the reference's empty value (all bytes 0xfe), the tables and the status word; the
     // flow fields are fully rewritten by the splat kernel before the reprojection reads them.
-    e = launch_batch(p, info->mode, static_cast<cudaStream_t>(stream_ptr), nullptr, nullptr);
+    e = info->mode == ISTI_MODE_TIMEWARP ? launch_timewarp(p, base, static_cast<cudaStream_t>(stream_ptr), nullptr, nullptr)
+                                         : launch_batch(p, info->mode, static_cast<cudaStream_t>(stream_ptr), nullptr, nullptr);
     if (e != cudaSuccess)
         return cuda_fail(e, "kernel launch");
     return ISTI_OK;

@@ -568,6 +568,94 @@ static void reproj_pixel(const oracle_render_info *s, const view_ctx *views, int
     }
 }
 
+/* ---- timewarp (mode 4), src/renderer.cu:467-522,615-629 ---- */
+
+typedef struct { float x, y, z; } v3f;
+
+static float dot3(v3f a, v3f b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }           /* glm-subset order */
+static float dot4(f4 a, f4 b) { return ((a.x * b.x + a.y * b.y) + a.z * b.z) + a.w * b.w; }
+static v3f normalize3(v3f v)
+{
+    const float s = 1.0f / sqrtf(dot3(v, v));
+    v3f r = {v.x * s, v.y * s, v.z * s};
+    return r;
+}
+static f4 normalize4(f4 v)
+{
+    const float s = 1.0f / sqrtf(dot4(v, v));
+    f4 r = {v.x * s, v.y * s, v.z * s, v.w * s};
+    return r;
+}
+
+/* Mean of the forward keyframe's NDC z (ImageBuffer::average, src/util/image_buffer.cu:80-100).
+ * The reference adds with a float atomicAdd in an unspecified order; here every row is summed
+ * left to right in double, the rows top to bottom in double, and the total is rounded to float
+ * and divided by the pixel count in float, as the reference's final division does. */
+static float mean_z(const float *z, uint32_t w, uint32_t h)
+{
+    double total = 0.0;
+    for (uint32_t y = 0; y < h; y++)
+    {
+        double row = 0.0;
+        for (uint32_t x = 0; x < w; x++)
+            row += (double)z[(size_t)y * w + x];
+        total += row;
+    }
+    return (float)total / (float)(w * h);
+}
+
+static void timewarp_pixel(const oracle_render_info *s, const oracle_view *to, const oracle_view *aux, float depth_to, uint32_t x, uint32_t y,
+                           uint8_t *out)
+{
+    const u2 res = {s->width, s->height}, px = {x, y};
+    const f2 pcs = pixel2CS(px, res);
+    const f4 near_cs = {pcs.x, pcs.y, 0.0f, 1.0f}, far_cs = {pcs.x, pcs.y, 1.0f, 1.0f};
+    const f4 near_ws = project(s->inv_viewproj, near_cs), far_ws = project(s->inv_viewproj, far_cs);
+    const v3f ro = {near_ws.x, near_ws.y, near_ws.z};
+    const v3f rd = normalize3((v3f){far_ws.x - near_ws.x, far_ws.y - near_ws.y, far_ws.z - near_ws.z});
+    const f4 center_cs = {0.0f, 0.0f, depth_to, 1.0f};
+    const f4 center_ws = project(to->inv_viewproj, center_cs);
+    const f4 campos = {to->inv_viewproj[12], to->inv_viewproj[13], to->inv_viewproj[14], to->inv_viewproj[15]}; /* inv_viewproj_mat_to[3] */
+    const f4 vd4 = normalize4((f4){center_ws.x - campos.x, center_ws.y - campos.y, center_ws.z - campos.z, center_ws.w - campos.w});
+    const v3f n = {vd4.x, vd4.y, vd4.z};
+    const v3f pp = {campos.x, campos.y, campos.z};
+    const float denom = dot3(rd, n);
+    if (fabsf(denom) < 1e-6f) /* the ray is parallel to the plane: no write */
+        return;
+    const float t = dot3((v3f){pp.x - ro.x, pp.y - ro.y, pp.z - ro.z}, n) / denom;
+    const f4 hit = {ro.x + t * rd.x, ro.y + t * rd.y, ro.z + t * rd.z, 1.0f};
+    const f4 pc = project(to->viewproj, hit);
+    const f2 pcxy = {pc.x, pc.y};
+    const u2 tres = {to->width, to->height};
+    i2 pix = CS2pixel(pcxy, tres);
+    const oracle_view *src = to;
+    u2 sres = tres;
+    if (!in_range(pix, tres) && aux)
+    {
+        const f4 pa = project(aux->viewproj, hit);
+        const f2 paxy = {pa.x, pa.y};
+        sres.x = aux->width;
+        sres.y = aux->height;
+        pix = CS2pixel(paxy, sres);
+        src = aux;
+    }
+    /* clamp(pixel, 0, res - 1), include/util/helper_math.h clamp(int2, int2, int2) */
+    pix.x = pix.x < 0 ? 0 : (pix.x > (int32_t)sres.x - 1 ? (int32_t)sres.x - 1 : pix.x);
+    pix.y = pix.y < 0 ? 0 : (pix.y > (int32_t)sres.y - 1 ? (int32_t)sres.y - 1 : pix.y);
+    memcpy(out, src->color + 4 * ((size_t)pix.y * sres.x + (uint32_t)pix.x), 4);
+}
+
+static int oracle_timewarp(const oracle_frame *frame, const oracle_render_info *s, uint8_t *out_rgba, int nt)
+{
+    const float depth_to = mean_z(frame->fwd.z, frame->fwd.width, frame->fwd.height);
+    const oracle_view *aux = frame->num_aux > 0 ? &frame->aux_curr[0] : NULL;
+#pragma omp parallel for schedule(static) num_threads(nt)
+    for (int32_t y = 0; y < (int32_t)s->height; y++)
+        for (uint32_t x = 0; x < s->width; x++)
+            timewarp_pixel(s, &frame->fwd, aux, depth_to, x, (uint32_t)y, out_rgba + 4 * ((size_t)y * s->width + x));
+    return 0;
+}
+
 static int view_ok(const oracle_view *v)
 {
     if (!v || !v->color || !v->z || v->width == 0 || v->height == 0 || v->width > 65535u || v->height > 65535u)
@@ -579,7 +667,7 @@ static int view_ok(const oracle_view *v)
 
 int oracle_render(const oracle_frame *frame, const oracle_render_info *s, uint8_t *out_rgba, oracle_view_out *outs, int nthreads)
 {
-    if (!frame || !s || !out_rgba || s->mode < 0 || s->mode > 3)
+    if (!frame || !s || !out_rgba || s->mode < 0 || s->mode > 4)
         return -1;
     /* shadow levels sit at bits 2i of a 32-bit field: more than 16 sub-frames
      * would shift past its width (undefined in the reference) */
@@ -607,6 +695,8 @@ int oracle_render(const oracle_frame *frame, const oracle_render_info *s, uint8_
     const int nt = 1;
     (void)nthreads;
 #endif
+    if (s->mode == 4) /* TIMEWARP returns before any splatting, src/renderer.cu:615-629 */
+        return oracle_timewarp(frame, s, out_rgba, nt);
     const int n_views = 2 + 2 * n_aux;
     view_ctx *views = (view_ctx *)calloc((size_t)n_views, sizeof(view_ctx));
     void **scratch = (void **)calloc((size_t)n_views * 3, sizeof(void *));

@@ -54,10 +54,21 @@ def nan_levels(frame):
             v.shadow_info[10:20, :, 2] = 0x55
 
 
+def timewarp_cases():
+    tw = Sequence(160, 90, 2, seed=15, aux_offsets=(0.3,), aux_size=(80, 45))
+    case("tw_aux_half_res_t025_mode4", tw, 0, 1, mode=4, meta="timewarp with an aux fallback camera")
+    tw_main = Sequence(128, 72, 2, seed=16)
+    case("tw_main_t075_mode4", tw_main, 0, 3, mode=4, meta="timewarp, main camera only")
+
+
 def main():
     oracle.build()
     if not oracle.reference_available():
         raise SystemExit("reference renderer not built (needs the reference tree)")
+    if sys.argv[1:] == ["timewarp"]:
+        timewarp_cases()
+        return
+    timewarp_cases()
     c1 = Sequence(320, 180, 3, seed=11)
     case("c1_t050_mode0", c1, 0, 2, meta="main only, no shadows")
     case("c1_t025_mode3", c1, 1, 1, mode=3, meta="splatting only")

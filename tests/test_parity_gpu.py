@@ -34,8 +34,8 @@ def render_gpu(frame, client, prev, motion_format="f16x3", renderer=None):
     torch.cuda.synchronize()
     assert r.device_status() == 0
     bufs = [r.view_buffers(k) for k in range(len(dev.views()))]
-    res = (out.cpu().numpy(), [b[0].cpu().numpy().view(np.uint64) for b in bufs], [b[1].cpu().numpy() for b in bufs],
-           [b[2].cpu().numpy() for b in bufs])
+    npy = lambda t, view=None: None if t is None else (t.cpu().numpy().view(view) if view else t.cpu().numpy())
+    res = (out.cpu().numpy(), [npy(b[0], np.uint64) for b in bufs], [npy(b[1]) for b in bufs], [npy(b[2]) for b in bufs])
     if renderer is None:
         r.close()
     return res
@@ -60,7 +60,29 @@ def assert_bit_exact(got, exp_out, exp_splat, exp_cam=None, exp_full=None):
 @pytest.mark.parametrize("path", fixtures.cases(), ids=lambda p: p.split("/")[-1][:-4])
 def test_golden_bit_exact(cuda, path, motion_format):
     frame, client, prev, exp = fixtures.load(path)
-    assert_bit_exact(render_gpu(frame, client, prev, motion_format), exp["out"], exp["splat"], exp["cam_ff"], exp["full_ff"])
+    got = render_gpu(frame, client, prev, motion_format)
+    if client.mode == native.MODE_TIMEWARP:  # no splat intermediates in this mode
+        assert np.array_equal(got[0], exp["out"]), f"{int((got[0] != exp['out']).any(-1).sum())} output pixels differ"
+        return
+    assert_bit_exact(got, exp["out"], exp["splat"], exp["cam_ff"], exp["full_ff"])
+
+
+@pytest.mark.parametrize("aux", [(), (-0.3, 0.3)])
+def test_timewarp_matches_oracle_1080p(cuda, aux):
+    """Mode 4 (planar timewarp at the forward keyframe's mean depth, src/renderer.cu:467-522)."""
+    import torch
+    seq = Sequence(1920, 1080, 2, seed=707, aux_offsets=aux)
+    frame = seq.frame(0)
+    dev = DeviceFrame.from_host(frame)
+    r = Renderer()
+    for b in (1, 3):
+        client = seq.client(0, b, mode=native.MODE_TIMEWARP)
+        prev = np.full((1080, 1920, 4), 11, np.uint8)
+        out = torch.from_numpy(prev.copy()).cuda()
+        r.render(out, client, dev)
+        exp = oracle.run_oracle(frame, client, prev, with_intermediates=False)[0]
+        assert np.array_equal(out.cpu().numpy(), exp)
+    r.close()
 
 
 @pytest.mark.parametrize("mode", [0, 1, 2, 3])
@@ -167,7 +189,7 @@ def test_invalid_arguments_are_rejected(cuda):
     r.close()
 
 
-@pytest.mark.parametrize("mode", [0, 1, 3])
+@pytest.mark.parametrize("mode", [0, 1, 3, 4])
 def test_batch_equals_sequential_renders(cuda, mode):
     """isti_render_batch == isti_render frame by frame (chained: one persistent buffer)."""
     import torch
@@ -188,6 +210,8 @@ def test_batch_equals_sequential_renders(cuda, mode):
     torch.cuda.synchronize()
     for k in range(len(clients)):
         assert torch.equal(outs[k], snaps[k]), f"chained frame {k} differs"
+        if mode == native.MODE_TIMEWARP:
+            continue  # no splat keys in this mode
         for v in range(nv):
             assert torch.equal(r.view_buffers(k * nv + v)[0], keys[k][v]), f"frame {k} view {v} keys differ"
     outs = [prev.clone() for _ in clients]
