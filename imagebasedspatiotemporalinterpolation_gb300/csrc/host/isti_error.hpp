@@ -1,0 +1,13 @@
+// Thread-local "last error" shared by every translation unit of libisti
+// (the renderer, the image codecs and the dataset reader).
+#pragma once
+
+#include "isti.h"
+
+#include <string>
+
+namespace isti
+{
+// Stores `msg` as the calling thread's isti_last_error() and returns `s`.
+isti_status set_error(isti_status s, const std::string &msg);
+} // namespace isti

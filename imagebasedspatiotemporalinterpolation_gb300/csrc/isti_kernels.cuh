@@ -876,6 +876,38 @@ __global__ void __launch_bounds__(256) timewarp_kernel(const __grid_constant__ F
     }
 }
 
+// Unity depth (reversed, [0,1]) to NDC z in place: convertDepthToZ_kernel
+// (src/file_reader.cu:17-37) with the reader's settings, d <- 1 - d, then
+// d <- 2 d - 1 (2 d is exact, so the two roundings are those of the
+// reference).  VEC: four pixels per thread with 16-byte accesses (z 16-byte
+// aligned), the last n % 4 pixels one per thread.
+__device__ __forceinline__ float unity_depth_to_z(float d) { return __fsub_rn(__fmul_rn(2.0f, __fsub_rn(1.0f, d)), 1.0f); }
+
+template <bool VEC>
+__global__ void depth_to_z_kernel(float *__restrict__ z, size_t n)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    if (!VEC)
+    {
+        for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+            z[i] = unity_depth_to_z(z[i]);
+        return;
+    }
+    const size_t n4 = n / 4;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride)
+    {
+        float4 v = reinterpret_cast<float4 *>(z)[i];
+        v.x = unity_depth_to_z(v.x);
+        v.y = unity_depth_to_z(v.y);
+        v.z = unity_depth_to_z(v.z);
+        v.w = unity_depth_to_z(v.w);
+        reinterpret_cast<float4 *>(z)[i] = v;
+    }
+    const size_t tail = n4 * 4 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tail < n)
+        z[tail] = unity_depth_to_z(z[tail]);
+}
+
 // Dynamic shared memory of one reprojection block.
 template <int SW>
 constexpr size_t reproj_smem(int n_views, int n_frames, int frames_per_group)

@@ -10,7 +10,11 @@
 // Launches per batch: init, splat, reprojection (isti_kernels.cuh); nothing
 // blocks the host.
 #include "isti.h"
+#include "isti_dataset.h"
 #include "isti_kernels.cuh"
+#include "host/isti_error.hpp"
+
+#include <algorithm>
 
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -426,6 +430,8 @@ isti_status render_batch(isti_renderer *r, int n_frames, void *const *outs, cons
 }
 } // namespace
 
+isti_status isti::set_error(isti_status s, const std::string &msg) { return fail(s, msg); }
+
 extern "C" {
 
 int32_t isti_abi_version(void) { return ISTI_ABI_VERSION; }
@@ -642,4 +648,22 @@ extern "C" isti_status isti_render_noalloc(void *out_rgba, const isti_render_inf
     if (e != cudaSuccess)
         return cuda_fail(e, "kernel launch");
     return ISTI_OK;
+}
+
+// convertDepthToZ_kernel (src/file_reader.cu:17-37), declared in include/isti_dataset.h.
+extern "C" isti_status isti_depth_to_z(float *depth, int32_t width, int32_t height, void *stream_ptr)
+{
+    if (!depth || width <= 0 || height <= 0)
+        return fail(ISTI_ERR_INVALID_ARG, "isti_depth_to_z: bad argument");
+    const size_t n = (size_t)width * (size_t)height;
+    const bool vec = ((uintptr_t)depth & 15) == 0;
+    const size_t work = vec ? n / 4 + 3 : n;
+    const unsigned blocks = (unsigned)std::min<size_t>((work + 255) / 256, 152 * 16);
+    cudaStream_t s = static_cast<cudaStream_t>(stream_ptr);
+    if (vec)
+        isti::depth_to_z_kernel<true><<<blocks, 256, 0, s>>>(depth, n);
+    else
+        isti::depth_to_z_kernel<false><<<blocks, 256, 0, s>>>(depth, n);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? ISTI_OK : cuda_fail(e, "isti_depth_to_z");
 }

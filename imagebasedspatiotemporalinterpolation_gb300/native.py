@@ -82,6 +82,54 @@ SIGNATURES = {
                                     C.POINTER(IstiFrameData), C.c_int32, C.c_void_p]),
 }
 
+
+class IstiCameraInfo(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("client_fps", C.c_int32), ("server_fps", C.c_int32),
+                ("shadow_fps", C.c_int32), ("priority", C.c_int32), ("n_frames", C.c_int32)]
+
+
+class IstiCameraFrame(C.Structure):
+    _fields_ = [("idx", C.c_int32), ("w2c", Mat16), ("proj", Mat16)]
+
+
+_P = C.POINTER
+_u8p, _f32p, _i32p = _P(C.c_uint8), _P(C.c_float), _P(C.c_int32)
+
+# include/isti_io.h
+IO_SIGNATURES = {
+    "isti_png_decode_file": (C.c_int, [C.c_char_p, _i32p, _i32p, _P(_u8p)]),
+    "isti_png_decode_memory": (C.c_int, [C.c_void_p, C.c_size_t, _i32p, _i32p, _P(_u8p)]),
+    "isti_png_encode_file": (C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
+    "isti_png_encode_memory": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, _P(_u8p), _P(C.c_size_t)]),
+    "isti_exr_decode_file": (C.c_int, [C.c_char_p, _i32p, _i32p, _i32p, _P(_f32p)]),
+    "isti_exr_decode_memory": (C.c_int, [C.c_void_p, C.c_size_t, _i32p, _i32p, _i32p, _P(_f32p)]),
+    "isti_exr_encode_file": (C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int32]),
+    "isti_zlib_decompress": (C.c_int, [C.c_void_p, C.c_size_t, _P(_u8p), _P(C.c_size_t)]),
+    "isti_image_free": (None, [C.c_void_p]),
+}
+
+# include/isti_dataset.h
+DATASET_SIGNATURES = {
+    "isti_camera_path_open": (C.c_int, [C.c_char_p, _P(C.c_void_p)]),
+    "isti_camera_path_info": (C.c_int, [C.c_void_p, _P(IstiCameraInfo)]),
+    "isti_camera_path_frame": (C.c_int, [C.c_void_p, C.c_int32, _P(IstiCameraFrame)]),
+    "isti_camera_path_close": (None, [C.c_void_p]),
+    "isti_dataset_open": (C.c_int, [C.c_char_p, C.c_int32, _P(C.c_char_p), C.c_void_p, _P(C.c_void_p)]),
+    "isti_dataset_read_next": (C.c_int, [C.c_void_p, _i32p]),
+    "isti_dataset_frame": (C.c_int, [C.c_void_p, _P(IstiFrameData)]),
+    "isti_dataset_camera": (C.c_int, [C.c_void_p, C.c_int32, _P(IstiCameraInfo)]),
+    "isti_dataset_matrices": (C.c_int, [C.c_void_p, C.c_int32, _f32p, _f32p]),
+    "isti_dataset_keyframe": (C.c_int32, [C.c_void_p]),
+    "isti_dataset_close": (None, [C.c_void_p]),
+    "isti_depth_to_z": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
+    "isti_normalize_proj": (C.c_int, [_f32p, _f32p]),
+    "isti_mat4_mul": (None, [_f32p, _f32p, _f32p]),
+    "isti_mat4_inverse": (None, [_f32p, _f32p]),
+    "isti_mat4_interpolate": (None, [_f32p, _f32p, C.c_float, _f32p]),
+}
+
+ALL_SIGNATURES = {**SIGNATURES, **IO_SIGNATURES, **DATASET_SIGNATURES}
+
 MAX_BATCH_FRAMES = 8  # ISTI_MAX_BATCH_FRAMES
 
 NOALLOC_SCRATCH_BYTES = 64 << 20  # ISTI_NOALLOC_SCRATCH_BYTES
@@ -105,7 +153,7 @@ def load(path: str | None = None) -> C.CDLL:
     if not os.path.exists(p):
         raise RuntimeError(f"{p} is missing: build the CUDA extension first (python -c 'import __graft_entry__ as g; g.build()')")
     lib = C.CDLL(p)
-    for name, (res, args) in SIGNATURES.items():
+    for name, (res, args) in ALL_SIGNATURES.items():
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args

@@ -56,10 +56,10 @@ class OracleViewOut(C.Structure):
 def build(verbose: bool = False) -> None:
     """Compile isti_oracle.c, and the reference's renderer when its tree is present."""
     os.makedirs(BUILD_DIR, exist_ok=True)
-    src = os.path.join(HERE, "isti_oracle.c")
+    srcs = [os.path.join(HERE, "isti_oracle.c"), os.path.join(HERE, "isti_oracle_glm.c")]
     hdr = os.path.join(HERE, "isti_oracle.h")
-    if not os.path.exists(ORACLE_LIB) or max(os.path.getmtime(src), os.path.getmtime(hdr)) > os.path.getmtime(ORACLE_LIB):
-        cmd = ["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", src, "-o", ORACLE_LIB, "-lm"]
+    if not os.path.exists(ORACLE_LIB) or max(os.path.getmtime(p) for p in srcs + [hdr]) > os.path.getmtime(ORACLE_LIB):
+        cmd = ["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", *srcs, "-o", ORACLE_LIB, "-lm"]
         if verbose:
             print(" ".join(cmd))
         subprocess.run(cmd, check=True)

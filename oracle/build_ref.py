@@ -63,6 +63,28 @@ def build(reference: str, verbose: bool = False) -> str | None:
     if verbose:
         print(" ".join(cmd))
     subprocess.run(cmd, check=True)
+    build_io(reference, verbose)
+    return lib
+
+
+def build_io(reference: str, verbose: bool = False) -> str | None:
+    """The reference's vendored image libraries (stb_image, stb_image_write,
+    tinyexr; dependencies/) with the configuration of
+    src/util/image_buffer.cu:8-17, wrapped by ref_host/ref_io.cpp."""
+    deps = os.path.join(reference, "dependencies")
+    if not os.path.isfile(os.path.join(deps, "tinyexr", "tinyexr.h")):
+        return None
+    os.makedirs(OUT_DIR, exist_ok=True)
+    lib = os.path.join(OUT_DIR, "libref_io.so")
+    src = os.path.join(HERE, "ref_host", "ref_io.cpp")
+    if os.path.exists(lib) and os.path.getmtime(lib) > os.path.getmtime(src):
+        return lib
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-w",
+           "-I", os.path.join(deps, "stb_image"), "-I", os.path.join(deps, "tinyexr"),
+           src, "-o", lib, "-lpthread"]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.run(cmd, check=True)
     return lib
 
 

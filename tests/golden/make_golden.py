@@ -4,7 +4,9 @@ Runs the reference's own src/renderer.cu (compiled for the CPU by
 oracle/build_ref.py, so it needs the reference tree) on small seeded
 procedural scenes and stores inputs and outputs with fixtures.save().
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            (everything)
+    python tests/golden/make_golden.py io         (codec fixtures only)
+    python tests/golden/make_golden.py timewarp   (timewarp fixtures only)
 """
 from __future__ import annotations
 
@@ -61,13 +63,118 @@ def timewarp_cases():
     case("tw_main_t075_mode4", tw_main, 0, 3, mode=4, meta="timewarp, main camera only")
 
 
+IO_DIR = os.path.join(fixtures.GOLDEN_DIR, "io")
+
+
+def io_cases():
+    """Codec fixtures: PNG files of every colour type / depth / tRNS form /
+    interlacing (tests/golden/png_writer.py) and from stb_image_write, EXR files
+    from tinyexr in every compression it writes; expected decodes from the
+    reference's own stb_image / LoadEXR (oracle/ref_io.py) in io/expected.npz."""
+    from oracle import ref_io
+    from tests.golden.png_writer import make_png
+
+    os.makedirs(IO_DIR, exist_ok=True)
+    rng = np.random.default_rng(2024)
+    expected = {}
+
+    def png(name, data):
+        path = os.path.join(IO_DIR, name + ".png")
+        with open(path, "wb") as f:
+            f.write(data)
+        expected[name + ".png"] = ref_io.png_load(path)
+
+    h, w = 11, 19
+    for depth in (1, 2, 4, 8, 16):
+        s = rng.integers(0, 1 << depth, (h, w))
+        png(f"grey{depth}", make_png(s, depth, 0))
+        png(f"grey{depth}_trns", make_png(s, depth, 0, trns=int(s[3, 4]).to_bytes(2, "big")))
+        png(f"grey{depth}_adam7", make_png(s, depth, 0, interlace=1))
+        if depth <= 8:
+            n = min(1 << depth, 200)
+            sp = rng.integers(0, n, (h, w))
+            pal = rng.integers(0, 256, 3 * n, dtype=np.uint8).tobytes()
+            png(f"palette{depth}", make_png(sp, depth, 3, palette=pal))
+            png(f"palette{depth}_trns", make_png(sp, depth, 3, palette=pal,
+                                                 trns=rng.integers(0, 256, n // 2 + 1, dtype=np.uint8).tobytes()))
+            png(f"palette{depth}_adam7", make_png(sp, depth, 3, palette=pal, interlace=1))
+    for depth in (8, 16):
+        for color in (2, 4, 6):
+            ch = {2: 3, 4: 2, 6: 4}[color]
+            s = rng.integers(0, 1 << depth, (13, 9, ch))
+            s[5:8] = s[0:1, 0:1]
+            png(f"color{color}_depth{depth}", make_png(s, depth, color))
+            png(f"color{color}_depth{depth}_adam7", make_png(s, depth, color, interlace=1))
+            if color == 2:
+                key = b"".join(int(k).to_bytes(2, "big") for k in s[0, 0])
+                png(f"color2_depth{depth}_trns", make_png(s, depth, color, trns=key))
+    for comp in (1, 2, 3, 4):
+        img = rng.integers(0, 256, (17, 23, comp), dtype=np.uint8)
+        path = os.path.join(IO_DIR, f"stb_{comp}ch.png")
+        ref_io.png_save(path, img)
+        expected[f"stb_{comp}ch.png"] = ref_io.png_load(path)
+
+    for comp_name, comp in (("none", 0), ("rle", 1), ("zips", 2), ("zip", 3), ("piz", 4)):
+        for pt_name, pt in (("half", 1), ("float", 2)):
+            for names in (["Y"], ["B", "G", "R"], ["A", "B", "G", "R", "Z"], ["G", "R"]):
+                planes = (rng.standard_normal((len(names), 11, 17)) * 50).astype(np.float32)
+                planes[:, 3:6] = 0.75  # runs for RLE
+                name = f"{comp_name}_{pt_name}_{''.join(names)}.exr"
+                path = os.path.join(IO_DIR, name)
+                ref_io.exr_save(path, planes, names, pt, comp)
+                expected[name] = ref_io.exr_load(path)
+    np.savez_compressed(os.path.join(IO_DIR, "expected.npz"),
+                        **{k: (np.array(v) if isinstance(v, str) else v) for k, v in expected.items()})
+    print(f"io: {len(expected)} files")
+
+
+def metrics_cases(reference="/root/reference"):
+    """PSNR / SSIM of seeded image pairs by the reference's own evaluation code:
+    scripts/loss_utils.ssim and eval.py's psnr_fn (torch, CPU), on (1, 3, H, W)
+    float tensors of the RGB bytes / 255 as eval.py's loader makes them."""
+    import torch
+    import torch.nn.functional as F
+
+    sys.path.insert(0, os.path.join(reference, "scripts"))
+    from loss_utils import ssim  # the reference's implementation
+
+    rng = np.random.default_rng(77)
+    pairs = {}
+    for name, (h, w) in (("noise", (30, 40)), ("odd", (45, 67)), ("tiny", (5, 8)), ("tall", (70, 12))):
+        a = rng.integers(0, 256, (h, w, 4), dtype=np.uint8)
+        b = np.clip(a.astype(int) + rng.integers(-40, 41, (h, w, 4)), 0, 255).astype(np.uint8)
+        pairs[name] = (a, b)
+    yy, xx = np.mgrid[0:48, 0:64]
+    smooth = np.stack([(xx * 4) % 256, (yy * 5) % 256, (xx + yy) % 256, np.full_like(xx, 255)], -1).astype(np.uint8)
+    pairs["smooth"] = (smooth, np.roll(smooth, 1, axis=1))
+    pairs["identical"] = (smooth, smooth.copy())
+    out = {}
+    for name, (a, b) in pairs.items():
+        ta = torch.from_numpy(np.ascontiguousarray(np.moveaxis(a[..., :3], -1, 0))).float().unsqueeze(0) / 255.0
+        tb = torch.from_numpy(np.ascontiguousarray(np.moveaxis(b[..., :3], -1, 0))).float().unsqueeze(0) / 255.0
+        s = ssim(ta, tb).mean().item()
+        p = (-10.0 * torch.log(F.mse_loss(ta, tb)) / np.log(10.0)).item()
+        out[f"{name}_a"], out[f"{name}_b"] = a, b
+        out[f"{name}_ssim"], out[f"{name}_psnr"] = np.float64(s), np.float64(p)
+    np.savez_compressed(os.path.join(fixtures.GOLDEN_DIR, "metrics.npz"), **out)
+    print(f"metrics: {len(pairs)} pairs")
+
+
 def main():
+    if sys.argv[1:] == ["metrics"]:
+        metrics_cases()
+        return
     oracle.build()
     if not oracle.reference_available():
         raise SystemExit("reference renderer not built (needs the reference tree)")
     if sys.argv[1:] == ["timewarp"]:
         timewarp_cases()
         return
+    if sys.argv[1:] == ["io"]:
+        io_cases()
+        return
+    io_cases()
+    metrics_cases()
     timewarp_cases()
     c1 = Sequence(320, 180, 3, seed=11)
     case("c1_t050_mode0", c1, 0, 2, meta="main only, no shadows")

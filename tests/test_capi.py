@@ -13,6 +13,7 @@ import pytest
 from imagebasedspatiotemporalinterpolation_gb300 import _build, native
 
 HEADER = os.path.join(_build.INCLUDE, "isti.h")
+HEADERS = [os.path.join(_build.INCLUDE, h) for h in ("isti.h", "isti_io.h", "isti_dataset.h")]
 
 
 def declared_functions(path):
@@ -30,18 +31,22 @@ def test_header_declares_expected_entry_points():
         assert n in names
 
 
-def test_library_exports_every_declared_symbol(built):
+@pytest.mark.parametrize("header", HEADERS, ids=os.path.basename)
+def test_library_exports_every_declared_symbol(built, header):
     lib = C.CDLL(_build.cuda_lib_path())
-    missing = [n for n in declared_functions(HEADER) if not hasattr(lib, n)]
+    declared = declared_functions(header)
+    assert declared
+    missing = [n for n in declared if not hasattr(lib, n)]
     assert not missing, f"not exported: {missing}"
-    assert set(declared_functions(HEADER)) <= set(native.SIGNATURES), "ctypes signatures incomplete"
+    assert set(declared) <= set(native.ALL_SIGNATURES), "ctypes signatures incomplete"
 
 
 def test_struct_layout_matches_header(built, tmp_path):
     prog = tmp_path / "layout.c"
     structs = {"isti_view": native.IstiView, "isti_frame_data": native.IstiFrameData,
-               "isti_render_info": native.IstiRenderInfo, "isti_timing": native.IstiTiming}
-    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "isti.h"', "int main(void){"]
+               "isti_render_info": native.IstiRenderInfo, "isti_timing": native.IstiTiming,
+               "isti_camera_info": native.IstiCameraInfo, "isti_camera_frame": native.IstiCameraFrame}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "isti.h"', '#include "isti_dataset.h"', "int main(void){"]
     for cname, cls in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
         for fname, _ in cls._fields_:
