@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-per-frame", action="store_true", help="skip the single-frame-call comparison")
+    ap.add_argument("--no-quality", action="store_true", help="skip PSNR / SSIM against the analytic ground truth")
     return ap.parse_args()
 
 
@@ -336,6 +337,31 @@ def main_ours(args):
             "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": traffic,
             "algorithmic_bytes_per_launch": alg[dom]}
 
+    # ---- quality of the interpolated frames of pair 0 against the analytic ray-cast of
+    # the client camera at its own time (outside the timed region), by the GPU metric
+    # kernels (PSNR / SSIM of the reference's evaluation script)
+    quality = None
+    if rank == 0 and not args.no_quality:
+        from imagebasedspatiotemporalinterpolation_gb300.metrics import Quality
+        qouts = [torch.zeros((H, W, 4), dtype=torch.uint8, device=dev) for _ in TS]
+        r.render_batch(qouts, clients[0], frames[0], chain=True, stream=stream)
+        q = Quality(W, H, dev)
+        vals = []
+        for o, b in zip(qouts, TS):
+            truth = up(seq.ground_truth(0, b))
+            vals.append(q(o, truth))
+        qa, qb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        qa.record(stream)
+        for _ in range(10):
+            q.launch(qouts[0], truth)
+        qb.record(stream)
+        torch.cuda.synchronize()
+        quality = {"psnr_db": round(sum(v["psnr"] for v in vals) / len(vals), 3),
+                   "ssim": round(sum(v["ssim"] for v in vals) / len(vals), 5),
+                   "per_t": {str(t): {"psnr_db": round(v["psnr"], 3), "ssim": round(v["ssim"], 5)} for t, v in zip(TS, vals)},
+                   "reference": "analytic ray-cast of the client camera at its time (procedural scene)",
+                   "metric_kernel_ms": round(qa.elapsed_time(qb) / 10, 4)}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         import oracle
@@ -364,6 +390,7 @@ def main_ours(args):
             "e2e": e2e,
             "roofline": roof,
             "cpu_baseline": cpu,
+            "quality": quality,
         }
         print(json.dumps(line), flush=True)
     r.close()

@@ -128,7 +128,17 @@ DATASET_SIGNATURES = {
     "isti_mat4_interpolate": (None, [_f32p, _f32p, C.c_float, _f32p]),
 }
 
-ALL_SIGNATURES = {**SIGNATURES, **IO_SIGNATURES, **DATASET_SIGNATURES}
+class IstiQuality(C.Structure):
+    _fields_ = [("mse", C.c_double), ("psnr", C.c_double), ("ssim", C.c_double)]
+
+
+# include/isti_metrics.h
+METRICS_SIGNATURES = {
+    "isti_quality_scratch_bytes": (C.c_size_t, [C.c_int32, C.c_int32]),
+    "isti_quality_rgba8": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+}
+
+ALL_SIGNATURES = {**SIGNATURES, **IO_SIGNATURES, **DATASET_SIGNATURES, **METRICS_SIGNATURES}
 
 MAX_BATCH_FRAMES = 8  # ISTI_MAX_BATCH_FRAMES
 

@@ -309,6 +309,23 @@ class Sequence:
             fr.aux_priority.append(prio)
         return fr
 
+    def ground_truth(self, k: int, b: int) -> np.ndarray:
+        """RGBA8 colour ray-cast for the client camera of (k, b) at its own time,
+        (k + b / frames_per_anchor) keyframe intervals: the frame that
+        interpolation approximates (the procedural scene makes it exact)."""
+        t = b / self.fpa
+        pose = self.poses[k].lerp(self.poses[min(k + 1, self.n_keyframes - 1)], t)
+        vp = self.proj_main @ view_matrix(pose.eye, pose.yaw, pose.pitch)
+        w, h = self.width, self.height
+        cam = _SceneCam(w, h, _cm(vp), _cm(np.linalg.inv(vp)), (k + t) * self.dt, self.dt, 0)
+        color = np.zeros((h, w, 4), np.uint8)
+        z = np.zeros((h, w), np.float32)
+        mf = np.zeros((h, w, 3), np.float32)
+        mb = np.zeros((h, w, 3), np.float32)
+        out = _SceneOut(_ptr(color), _ptr(z), _ptr(mf), _ptr(mb), *([None] * 6))
+        _lib().isti_scene_render(C.byref(self._desc), C.byref(cam), C.byref(out))
+        return color
+
     def client(self, k: int, b: int, mode: int = 0, no_shadows: bool = False, alpha: float | None = None) -> Client:
         """Client camera at t = b / frames_per_anchor between keyframes k and k + 1."""
         t = b / self.fpa if alpha is None else alpha

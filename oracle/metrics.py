@@ -4,7 +4,7 @@ Restates scripts/eval.py:66-68 (PSNR = -10 log10(MSE) over RGB in [0, 1]) and
 scripts/loss_utils.py:17-57 (SSIM: 11x11 Gaussian window, sigma 1.5, zero
 padding, per channel, C1 = 0.01^2, C2 = 0.03^2, mean of the map) in float64.
 Pinned against the reference's own loss_utils.ssim run with torch on the CPU
-(tests/golden/metrics.npz, written by tests/golden/make_golden.py metrics).
+(tests/golden/metrics/pairs.npz, written by tests/golden/make_golden.py metrics).
 """
 from __future__ import annotations
 

@@ -156,7 +156,8 @@ def metrics_cases(reference="/root/reference"):
         p = (-10.0 * torch.log(F.mse_loss(ta, tb)) / np.log(10.0)).item()
         out[f"{name}_a"], out[f"{name}_b"] = a, b
         out[f"{name}_ssim"], out[f"{name}_psnr"] = np.float64(s), np.float64(p)
-    np.savez_compressed(os.path.join(fixtures.GOLDEN_DIR, "metrics.npz"), **out)
+    os.makedirs(os.path.join(fixtures.GOLDEN_DIR, "metrics"), exist_ok=True)
+    np.savez_compressed(os.path.join(fixtures.GOLDEN_DIR, "metrics", "pairs.npz"), **out)
     print(f"metrics: {len(pairs)} pairs")
 
 

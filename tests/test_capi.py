@@ -13,7 +13,7 @@ import pytest
 from imagebasedspatiotemporalinterpolation_gb300 import _build, native
 
 HEADER = os.path.join(_build.INCLUDE, "isti.h")
-HEADERS = [os.path.join(_build.INCLUDE, h) for h in ("isti.h", "isti_io.h", "isti_dataset.h")]
+HEADERS = [os.path.join(_build.INCLUDE, h) for h in ("isti.h", "isti_io.h", "isti_dataset.h", "isti_metrics.h")]
 
 
 def declared_functions(path):
@@ -45,8 +45,10 @@ def test_struct_layout_matches_header(built, tmp_path):
     prog = tmp_path / "layout.c"
     structs = {"isti_view": native.IstiView, "isti_frame_data": native.IstiFrameData,
                "isti_render_info": native.IstiRenderInfo, "isti_timing": native.IstiTiming,
-               "isti_camera_info": native.IstiCameraInfo, "isti_camera_frame": native.IstiCameraFrame}
-    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "isti.h"', '#include "isti_dataset.h"', "int main(void){"]
+               "isti_camera_info": native.IstiCameraInfo, "isti_camera_frame": native.IstiCameraFrame,
+               "isti_quality": native.IstiQuality}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "isti.h"', '#include "isti_dataset.h"',
+             '#include "isti_metrics.h"', "int main(void){"]
     for cname, cls in structs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
         for fname, _ in cls._fields_:
