@@ -263,42 +263,71 @@ __global__ void __launch_bounds__(256) splat_kernel(const __grid_constant__ Fram
 
 // ---- colour: colorFromShadow / secondChanceAndBlend_kernel, src/renderer.cu:217-327 ----
 
-// colorFromShadow (level-index form), src/renderer.cu:217-268
-__device__ uint32_t color_from_shadow_idx(uint32_t sidx, int32_t sfpa, const DevView &v, uint32_t px, uint32_t py)
+// The colour inputs of one source pixel of one view: colour and, when soft shadows apply,
+// shadow info and the shadow colours A/B, fetched together (one round of loads; A/B are
+// fetched even when the levels end up not needing them) and the pixel's shadow levels
+// (min / max over the shadow sub-frames and the initial level) computed once for every
+// level index asked for.  Reads outside the view are zero (border addressing).
+struct PixelShade
 {
-    const uint32_t main_color = ld_c(v.color, px, py, v.w, v.h);
-    if (sidx < (uint32_t)sfpa && sidx > 0)
+    uint32_t color, sha, shb;
+    uint32_t bf;          // 24-bit level field (shadowInfo RGB, src/renderer.cu:241-242)
+    int32_t init, mn, mx; // initial level, min and max over the sfpa sub-frames
+    bool levels;          // colour B present and a non-zero level field
+};
+
+__device__ __forceinline__ PixelShade load_shade(const DevView &v, uint32_t px, uint32_t py, bool shadows, int32_t sfpa)
+{
+    PixelShade s;
+    const bool in = px < v.w && py < v.h;
+    const uint32_t idx = py * v.w + px;
+    s.color = in ? __ldg(v.color + idx) : 0u;
+    s.sha = s.shb = 0u;
+    uint32_t si = 0u;
+    if (shadows && in)
     {
-        const uint32_t si = ld_c(v.shi, px, py, v.w, v.h);
-        const uint32_t bf = ((si & 255u) << 16) | (((si >> 8) & 255u) << 8) | ((si >> 16) & 255u);
-        if (v.shb != nullptr && bf != 0)
-        {
-            const int32_t init_val = (int32_t)(bf & SOFTSHADOW_VAL_MASK);
-            const int32_t my_val = (int32_t)((bf >> (SOFTSHADOW_BITS * sidx)) & SOFTSHADOW_VAL_MASK);
-            int32_t mn = (int32_t)SOFTSHADOW_VAL_MASK, mx = 0;
-            for (int32_t i = 0; i < sfpa; i++)
-            {
-                const int32_t lv = (int32_t)((bf >> (SOFTSHADOW_BITS * (uint32_t)i)) & SOFTSHADOW_VAL_MASK);
-                mn = min(mn, lv);
-                mx = max(mx, lv);
-            }
-            const float t = __fdiv_rn((float)(my_val - mn), (float)(mx - mn));
-            const uint32_t cmin = mn == init_val ? main_color : ld_c(v.sha, px, py, v.w, v.h);
-            const uint32_t cmax = mx == init_val ? main_color : ld_c(v.shb, px, py, v.w, v.h);
-            // (float)(1.0 - (double)t): t is k / d with d in {1, 2, 3} (or NaN), for which the
-            // double difference is exact, so one float subtraction rounds identically.
-            const float omt = __fsub_rn(1.0f, t);
-            uint32_t r = 255u << 24;
-#pragma unroll
-            for (int c = 0; c < 3; c++)
-            {
-                const float a = (float)((cmin >> (8 * c)) & 255u), b = (float)((cmax >> (8 * c)) & 255u);
-                r |= cvt_u8(__fadd_rn(__fmul_rn(a, omt), __fmul_rn(b, t))) << (8 * c);
-            }
-            return r;
-        }
+        si = __ldg(v.shi + idx);
+        s.sha = __ldg(v.sha + idx);
+        if (v.shb != nullptr)
+            s.shb = __ldg(v.shb + idx);
     }
-    return main_color;
+    s.bf = ((si & 255u) << 16) | (((si >> 8) & 255u) << 8) | ((si >> 16) & 255u);
+    s.levels = shadows && v.shb != nullptr && s.bf != 0;
+    s.init = (int32_t)(s.bf & SOFTSHADOW_VAL_MASK);
+    s.mn = (int32_t)SOFTSHADOW_VAL_MASK;
+    s.mx = 0;
+    if (s.levels)
+        for (int32_t i = 0; i < sfpa; i++)
+        {
+            const int32_t lv = (int32_t)((s.bf >> (SOFTSHADOW_BITS * (uint32_t)i)) & SOFTSHADOW_VAL_MASK);
+            s.mn = min(s.mn, lv);
+            s.mx = max(s.mx, lv);
+        }
+    return s;
+}
+
+// colorFromShadow (level-index form), src/renderer.cu:217-268
+__device__ __forceinline__ uint32_t color_from_shadow_idx(uint32_t sidx, int32_t sfpa, const PixelShade &s)
+{
+    if (sidx < (uint32_t)sfpa && sidx > 0 && s.levels)
+    {
+        const int32_t my_val = (int32_t)((s.bf >> (SOFTSHADOW_BITS * sidx)) & SOFTSHADOW_VAL_MASK);
+        const float t = __fdiv_rn((float)(my_val - s.mn), (float)(s.mx - s.mn));
+        const uint32_t cmin = s.mn == s.init ? s.color : s.sha;
+        const uint32_t cmax = s.mx == s.init ? s.color : s.shb;
+        // (float)(1.0 - (double)t): t is k / d with d in {1, 2, 3} (or NaN), for which the
+        // double difference is exact, so one float subtraction rounds identically.
+        const float omt = __fsub_rn(1.0f, t);
+        uint32_t r = 255u << 24;
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+        {
+            const float a = (float)((cmin >> (8 * c)) & 255u), b = (float)((cmax >> (8 * c)) & 255u);
+            r |= cvt_u8(__fadd_rn(__fmul_rn(a, omt), __fmul_rn(b, t))) << (8 * c);
+        }
+        return r;
+    }
+    return s.color;
 }
 
 struct ShadowFrames
@@ -320,45 +349,59 @@ __device__ __forceinline__ ShadowFrames shadow_frames(const FrameCfg &c)
     return sf;
 }
 
-// colorFromShadow (two sub-frame form), src/renderer.cu:270-295
-__device__ uint32_t color_from_shadow(const ShadowFrames &sf, const FrameCfg &c, const DevView &v, uint32_t px, uint32_t py)
+// Whether colorFromShadow blends shadow levels for view v (src/renderer.cu:277).
+__device__ __forceinline__ bool shadows_on(const ShadowFrames &sf, const FrameCfg &c, const DevView &v)
 {
-    if (c.no_shadows || sf.sfx >= (uint32_t)c.sfpa || sf.sfy == 0 || v.sha == nullptr)
-        return ld_c(v.color, px, py, v.w, v.h);
+    return !(c.no_shadows || sf.sfx >= (uint32_t)c.sfpa || sf.sfy == 0 || v.sha == nullptr);
+}
+
+// colorFromShadow (two sub-frame form), src/renderer.cu:270-295, on loaded inputs
+__device__ __forceinline__ uint32_t color_from_shadow(const ShadowFrames &sf, const FrameCfg &c, const DevView &v, bool on,
+                                                      const PixelShade &s)
+{
+    if (!on)
+        return s.color;
     const int32_t sfpa = c.sfpa;
     const uint32_t vx = (uint32_t)(v.forward ? (int32_t)sf.sfx : sfpa - (int32_t)sf.sfx);
     const uint32_t vy = (uint32_t)(v.forward ? (int32_t)sf.sfy : sfpa - (int32_t)sf.sfy);
     if (vx == vy || vy >= (uint32_t)sfpa)
-        return color_from_shadow_idx(vx, sfpa, v, px, py);
+        return color_from_shadow_idx(vx, sfpa, s);
     if (vx >= (uint32_t)sfpa)
-        return color_from_shadow_idx(vy, sfpa, v, px, py);
-    const uint32_t a = color_from_shadow_idx(vx, sfpa, v, px, py);
-    const uint32_t b = color_from_shadow_idx(vy, sfpa, v, px, py);
+        return color_from_shadow_idx(vy, sfpa, s);
+    const uint32_t a = color_from_shadow_idx(vx, sfpa, s);
+    const uint32_t b = color_from_shadow_idx(vy, sfpa, s);
     return lerp_color_u8(a, b, sf.sft);
 }
 
-// secondChanceAndBlend_kernel<EPS_2>, src/renderer.cu:297-327
+// secondChanceAndBlend_kernel<EPS_2>, src/renderer.cu:297-327.  Two rounds of loads: the
+// source pixel's flow, z and colour inputs together, then at the projected pixel in the
+// other keyframe its z, flow and colour inputs together (the colour is used only when the
+// round trip is consistent).
 __device__ uint32_t second_chance(float weight, const ShadowFrames &sf, const FrameCfg &c, uint32_t sx, uint32_t sy, const DevView &from,
                                   const DevView &to, float eps2)
 {
+    const bool on_from = shadows_on(sf, c, from);
     const float4 m_ft = ld_f4(from.full_ff, sx, sy, from.w, from.h);
-    const float2 spcs = view_pixel2cs(from, sx, sy);
     const float sz = ld_f(from.z, sx, sy, from.w, from.h);
+    const PixelShade s_from = load_shade(from, sx, sy, on_from, c.sfpa);
+    const float2 spcs = view_pixel2cs(from, sx, sy);
     const float pcx = __fadd_rn(spcs.x, m_ft.x), pcy = __fadd_rn(spcs.y, m_ft.y), pcz = __fadd_rn(sz, m_ft.z);
     const int2 pp = cs2pixel(pcx, pcy, to.w, to.h);
 
-    uint32_t out = color_from_shadow(sf, c, from, sx, sy);
+    uint32_t out = color_from_shadow(sf, c, from, on_from, s_from);
     if (sf.frame_idx >= (uint32_t)c.fpa)
         return out;
     if (in_range(pp, to.w, to.h))
     {
+        const bool on_to = shadows_on(sf, c, to);
         const uint32_t pi = (uint32_t)pp.y * to.w + (uint32_t)pp.x;
         const float az = __ldg(to.z + pi);
         const float4 m_tf = __ldg(to.full_ff + pi);
+        const PixelShade s_to = load_shade(to, (uint32_t)pp.x, (uint32_t)pp.y, on_to, c.sfpa);
         const float dx = __fsub_rn(m_ft.x, -m_tf.x), dy = __fsub_rn(m_ft.y, -m_tf.y), dz = __fsub_rn(m_ft.z, -m_tf.z);
         if (sqrt_less(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)), EPS_3) &&
             fabsf(__fsub_rn(az, pcz)) < eps2)
-            out = lerp_color_u8(color_from_shadow(sf, c, to, pp.x, pp.y), out, weight);
+            out = lerp_color_u8(color_from_shadow(sf, c, to, on_to, s_to), out, weight);
     }
     return out;
 }
@@ -499,20 +542,22 @@ __device__ __forceinline__ bool resolve_pixel(const DirRes *res, int lane, const
         return false; // temporal hole filling: keep the previous output (src/renderer.cu:416-419,462-463)
 
     const ShadowFrames sf = shadow_frames(c);
-    const DevView &vf = p.v[2 * cam], &vb = p.v[2 * cam + 1];
     const float eps2 = cam == 0 ? EPS_2_FULL_RES : EPS_2_LOW_RES;
     const float oma = __fsub_rn(1.0f, c.alpha);
-    if (fin.blend)
+    if (MAV && fin.blend)
     {
+        const DevView &vf = p.v[2 * cam], &vb = p.v[2 * cam + 1];
         const DirRes &f = res[lane], &b = res[32 + lane];
         const uint32_t cf = second_chance(oma, sf, c, f.src >> 16, f.src & 0xFFFFu, vf, vb, eps2);
         const uint32_t cb = second_chance(c.alpha, sf, c, b.src >> 16, b.src & 0xFFFFu, vb, vf, eps2);
         color = lerp_color_u8(cf, cb, 0.5f);
+        return true;
     }
-    else if (fin.dir == 0)
-        color = second_chance(oma, sf, c, fin.src >> 16, fin.src & 0xFFFFu, vf, vb, eps2);
-    else
-        color = second_chance(c.alpha, sf, c, fin.src >> 16, fin.src & 0xFFFFu, vb, vf, eps2);
+    // one call for either direction (the lanes of a warp choose different ones): from = the
+    // chosen keyframe's view, to = the other one, weight 1 - t from the earlier keyframe
+    const int dir = fin.dir;
+    const DevView &from = p.v[2 * cam + dir], &to = p.v[2 * cam + 1 - dir];
+    color = second_chance(dir == 0 ? oma : c.alpha, sf, c, fin.src >> 16, fin.src & 0xFFFFu, from, to, eps2);
     return true;
 }
 
