@@ -175,7 +175,8 @@ __device__ __forceinline__ float4 load_motion(const DevView &v, uint32_t idx)
 }
 
 // pixel2CS of pixel (x, y) of view v from its tables; direct formula outside the image
-__device__ __forceinline__ float2 view_pixel2cs(const DevView &v, uint32_t x, uint32_t y)
+template <class V>
+__device__ __forceinline__ float2 view_pixel2cs(const V &v, uint32_t x, uint32_t y)
 {
     if (x < v.w && y < v.h)
         return make_float2(__ldg(v.lut + x), __ldg(v.lut + v.w + y));
@@ -276,7 +277,8 @@ struct PixelShade
     bool levels;          // colour B present and a non-zero level field
 };
 
-__device__ __forceinline__ PixelShade load_shade(const DevView &v, uint32_t px, uint32_t py, bool shadows, int32_t sfpa)
+template <class V>
+__device__ __forceinline__ PixelShade load_shade(const V &v, uint32_t px, uint32_t py, bool shadows, int32_t sfpa)
 {
     PixelShade s;
     const bool in = px < v.w && py < v.h;
@@ -350,13 +352,15 @@ __device__ __forceinline__ ShadowFrames shadow_frames(const FrameCfg &c)
 }
 
 // Whether colorFromShadow blends shadow levels for view v (src/renderer.cu:277).
-__device__ __forceinline__ bool shadows_on(const ShadowFrames &sf, const FrameCfg &c, const DevView &v)
+template <class V>
+__device__ __forceinline__ bool shadows_on(const ShadowFrames &sf, const FrameCfg &c, const V &v)
 {
     return !(c.no_shadows || sf.sfx >= (uint32_t)c.sfpa || sf.sfy == 0 || v.sha == nullptr);
 }
 
 // colorFromShadow (two sub-frame form), src/renderer.cu:270-295, on loaded inputs
-__device__ __forceinline__ uint32_t color_from_shadow(const ShadowFrames &sf, const FrameCfg &c, const DevView &v, bool on,
+template <class V>
+__device__ __forceinline__ uint32_t color_from_shadow(const ShadowFrames &sf, const FrameCfg &c, const V &v, bool on,
                                                       const PixelShade &s)
 {
     if (!on)
@@ -364,11 +368,13 @@ __device__ __forceinline__ uint32_t color_from_shadow(const ShadowFrames &sf, co
     const int32_t sfpa = c.sfpa;
     const uint32_t vx = (uint32_t)(v.forward ? (int32_t)sf.sfx : sfpa - (int32_t)sf.sfx);
     const uint32_t vy = (uint32_t)(v.forward ? (int32_t)sf.sfy : sfpa - (int32_t)sf.sfy);
-    if (vx == vy || vy >= (uint32_t)sfpa)
-        return color_from_shadow_idx(vx, sfpa, s);
-    if (vx >= (uint32_t)sfpa)
-        return color_from_shadow_idx(vy, sfpa, s);
-    const uint32_t a = color_from_shadow_idx(vx, sfpa, s);
+    // single-index cases: vx when vx == vy or vy is out of range, else vy when vx is; one
+    // code path for every lane (forward and backward views differ within a warp)
+    const bool only_x = vx == vy || vy >= (uint32_t)sfpa;
+    const bool single = only_x || vx >= (uint32_t)sfpa;
+    const uint32_t a = color_from_shadow_idx(only_x || !single ? vx : vy, sfpa, s);
+    if (single)
+        return a;
     const uint32_t b = color_from_shadow_idx(vy, sfpa, s);
     return lerp_color_u8(a, b, sf.sft);
 }
@@ -377,8 +383,9 @@ __device__ __forceinline__ uint32_t color_from_shadow(const ShadowFrames &sf, co
 // source pixel's flow, z and colour inputs together, then at the projected pixel in the
 // other keyframe its z, flow and colour inputs together (the colour is used only when the
 // round trip is consistent).
-__device__ uint32_t second_chance(float weight, const ShadowFrames &sf, const FrameCfg &c, uint32_t sx, uint32_t sy, const DevView &from,
-                                  const DevView &to, float eps2)
+template <class V>
+__device__ uint32_t second_chance(float weight, const ShadowFrames &sf, const FrameCfg &c, uint32_t sx, uint32_t sy, const V &from,
+                                  const V &to, float eps2)
 {
     const bool on_from = shadows_on(sf, c, from);
     const float4 m_ft = ld_f4(from.full_ff, sx, sy, from.w, from.h);
