@@ -136,7 +136,12 @@ class IstiQuality(C.Structure):
 METRICS_SIGNATURES = {
     "isti_quality_scratch_bytes": (C.c_size_t, [C.c_int32, C.c_int32]),
     "isti_quality_rgba8": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "isti_flip_scratch_bytes": (C.c_size_t, [C.c_int32, C.c_int32]),
+    "isti_flip_rgba8": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_void_p]),
 }
+
+FLIP_DEFAULT_PPD = 0.7 * 3840 / 0.7 * 3.141592653589793 / 180  # eval.py: 0.7 m wide 4K screen at 0.7 m
 
 ALL_SIGNATURES = {**SIGNATURES, **IO_SIGNATURES, **DATASET_SIGNATURES, **METRICS_SIGNATURES}
 

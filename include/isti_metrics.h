@@ -7,8 +7,8 @@
  *   PSNR = -10 log10(MSE)                         (eval.py:68, F.mse_loss)
  *   SSIM = mean of the SSIM map, 11x11 Gaussian window, sigma 1.5, zero
  *          padding, C1 = 0.01^2, C2 = 0.03^2, per channel (scripts/loss_utils.py:17-57)
- * for each frame against its ground truth.  FLIP (scripts/flip_loss.py) is not
- * provided.
+ * for each frame against its ground truth, and LDR-FLIP (scripts/flip_loss.py,
+ * isti_flip_rgba8 below).
  *
  * One fused kernel reads both RGBA8 images once: per 32x16 tile it stages the
  * tile and its 5-pixel halo in shared memory, filters the five SSIM moments
@@ -47,6 +47,22 @@ size_t isti_quality_scratch_bytes(int32_t width, int32_t height);
  * out: device pointer to one isti_quality. */
 isti_status isti_quality_rgba8(const void *a, const void *b, int32_t width, int32_t height, void *scratch,
                                isti_quality *out, void *stream);
+
+/* LDR-FLIP (scripts/flip_loss.py, LDRFLIPLoss; eval.py's flip_fn(render,
+ * ground_truth)): `test` is the rendered frame, `reference` the ground truth,
+ * both device RGBA8 (alpha ignored).  pixels_per_degree = the observer's
+ * pixels per degree of visual angle (eval.py: 0.7 m wide 4K screen at 0.7 m,
+ * 3840 * pi / 180 = 67.02); the filters must fit in ISTI_FLIP_MAX_RADIUS
+ * pixels (pixels_per_degree <= 118).  One tile kernel stages both images as
+ * YCxCz with a replicate-padded halo, applies the contrast-sensitivity filters
+ * and the edge / point detectors separably (the reference's 2-D kernels
+ * factor exactly), and reduces in a fixed order.  *out_mean (device double)
+ * receives the mean FLIP; out_map (device float, width*height) the per-pixel
+ * values, or NULL. */
+#define ISTI_FLIP_MAX_RADIUS 16
+size_t isti_flip_scratch_bytes(int32_t width, int32_t height);
+isti_status isti_flip_rgba8(const void *test, const void *reference, int32_t width, int32_t height, float pixels_per_degree,
+                            void *scratch, double *out_mean, float *out_map, void *stream);
 
 #ifdef __cplusplus
 }

@@ -161,9 +161,51 @@ def metrics_cases(reference="/root/reference"):
     print(f"metrics: {len(pairs)} pairs")
 
 
+def flip_cases(reference="/root/reference"):
+    """LDR-FLIP (eval.py's flip_fn(render, ground_truth)) of the metric pairs plus an
+    interpolated frame against its analytic ground truth, computed by the
+    reference's scripts/flip_loss.py.  That file places every tensor on 'cuda';
+    here it runs on the CPU with torch.Tensor.cuda and the device argument of
+    torch.zeros redirected for the duration of the call."""
+    import torch
+
+    sys.path.insert(0, os.path.join(reference, "scripts"))
+    pairs = dict(np.load(os.path.join(fixtures.GOLDEN_DIR, "metrics", "pairs.npz")))
+    names = [k[:-2] for k in pairs if k.endswith("_a")]
+    seq = Sequence(96, 54, 2, seed=21, aux_offsets=(-0.3, 0.3), shadows=True, max_speed=2.0)
+    render, _, _, _ = oracle.run_oracle(seq.frame(0), seq.client(0, 2), with_intermediates=False)
+    pairs["render_a"], pairs["render_b"] = render, seq.ground_truth(0, 2)
+    names.append("render")
+
+    orig_cuda, orig_zeros = torch.Tensor.cuda, torch.zeros
+    torch.Tensor.cuda = lambda self, *a, **k: self
+    torch.zeros = lambda *a, **k: orig_zeros(*a, **{kk: v for kk, v in k.items() if kk != "device"})
+    try:
+        from flip_loss import LDRFLIPLoss  # the reference's implementation
+        flip = LDRFLIPLoss()
+        out = {}
+        for n in names:
+            a, b = pairs[n + "_a"], pairs[n + "_b"]
+            ta = torch.from_numpy(np.ascontiguousarray(np.moveaxis(a[..., :3], -1, 0))).float().unsqueeze(0) / 255.0
+            tb = torch.from_numpy(np.ascontiguousarray(np.moveaxis(b[..., :3], -1, 0))).float().unsqueeze(0) / 255.0
+            m = flip(ta, tb)  # test = a (render), reference = b (ground truth)
+            out[f"{n}_a"], out[f"{n}_b"] = a, b
+            out[f"{n}_flip"] = np.float64(m.mean().item())
+            if n in ("odd", "render"):
+                out[f"{n}_map"] = m.squeeze().numpy().astype(np.float32)
+    finally:
+        torch.Tensor.cuda, torch.zeros = orig_cuda, orig_zeros
+    np.savez_compressed(os.path.join(fixtures.GOLDEN_DIR, "metrics", "flip.npz"), **out)
+    print(f"flip: {len(names)} pairs")
+
+
 def main():
     if sys.argv[1:] == ["metrics"]:
         metrics_cases()
+        return
+    if sys.argv[1:] == ["flip"]:
+        oracle.build()
+        flip_cases()
         return
     oracle.build()
     if not oracle.reference_available():
@@ -176,6 +218,7 @@ def main():
         return
     io_cases()
     metrics_cases()
+    flip_cases()
     timewarp_cases()
     c1 = Sequence(320, 180, 3, seed=11)
     case("c1_t050_mode0", c1, 0, 2, meta="main only, no shadows")
