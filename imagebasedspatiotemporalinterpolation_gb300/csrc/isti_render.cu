@@ -316,11 +316,26 @@ cudaError_t launch_reproj(isti::FrameParams &p, cudaStream_t stream)
     static thread_local isti::KeyMaps km; // 2 KiB, passed by value as a kernel parameter
     p.use_tma = make_key_maps<SW>(p, km) ? 1 : 0;
     const size_t smem = isti::reproj_smem<SW>(p.n_views, p.n_frames, fg);
+    // raise the kernel's dynamic shared-memory limit once to the largest size requested, so
+    // that calls inside a CUDA graph capture make no attribute calls after a first uncaptured
+    // call of the same shape
+    static std::mutex attr_mutex;
+    static int attr_set[64] = {}; // per device
     if (smem > 48 * 1024)
     {
-        cudaError_t e = cudaFuncSetAttribute(isti::reproj_kernel<SW, SI, MAV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
         if (e != cudaSuccess)
             return e;
+        std::lock_guard<std::mutex> lock(attr_mutex);
+        int &cur = attr_set[dev & 63];
+        if ((int)smem > cur)
+        {
+            e = cudaFuncSetAttribute(isti::reproj_kernel<SW, SI, MAV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess)
+                return e;
+            cur = (int)smem;
+        }
     }
     const dim3 gr((p.out_w + 31) / 32, (p.out_h + isti::ROWS - 1) / isti::ROWS);
     isti::reproj_kernel<SW, SI, MAV><<<gr, dim3(32, p.n_views), smem, stream>>>(p, km);
