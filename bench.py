@@ -321,13 +321,19 @@ def main_ours(args):
     if not args.no_e2e:
         e2e = run_e2e(args, seq, res, clients, r, dev, world)
 
-    # ---- roofline of the dominant kernel.  Algorithmic bytes of one batched call: every
-    # input byte of the 6 source views once (z + f16 motion for the splat launch; colour +
-    # shadow A/B/Info for the reprojection launch) and the 3 output frames once.
+    # ---- roofline of the dominant kernel.  Algorithmic bytes per interpolated output pixel
+    # (the per-unit figure of the path): every source view's inputs once and the output once,
+    # 6 views x (4 z + 6 f16 motion + 4 colour + 12 shadow A/B/Info) + 4 = 160 B.  Split by the
+    # kernel that reads them: splat z + motion (60 B), reprojection colour + shadows + output
+    # (100 B); one launch processes len(TS) frames of W x H output pixels.  The batched call
+    # reads each input once for all its frames, so "achieved" is the effective bandwidth of the
+    # per-frame data flow; the inputs-once figure is reported beside it.
     px = W * H
     n_views = 2 * n_cams
     calls = max(1, tim["kernel_launches"] // 3)  # init, splat, reprojection per call
-    alg = {"splat_kernel": n_views * (4 + 6) * px, "reproj_kernel": n_views * (4 + 12) * px + len(TS) * 4 * px}
+    out_px = len(TS) * px
+    alg = {"splat_kernel": n_views * (4 + 6) * out_px, "reproj_kernel": (n_views * (4 + 12) + 4) * out_px}
+    once = {"splat_kernel": n_views * (4 + 6) * px, "reproj_kernel": n_views * (4 + 12) * px + len(TS) * 4 * px}
     per_launch_ms = {"splat_kernel": tim["splat_ms"] / calls, "reproj_kernel": tim["reproj_ms"] / calls}
     dom = max(per_launch_ms, key=per_launch_ms.get)
     peak, peak_kind = peaks()
@@ -335,7 +341,9 @@ def main_ours(args):
     traffic = profile_traffic(dom)
     roof = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": traffic,
-            "algorithmic_bytes_per_launch": alg[dom]}
+            "algorithmic_bytes_per_launch": alg[dom], "bytes_per_output_px": alg[dom] // out_px,
+            "inputs_once_bytes_per_launch": once[dom],
+            "inputs_once_frac": round(once[dom] / (per_launch_ms[dom] / 1e3) / 1e9 / peak, 4)}
 
     # ---- quality of the interpolated frames of pair 0 against the analytic ray-cast of
     # the client camera at its own time (outside the timed region), by the GPU metric
