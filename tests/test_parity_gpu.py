@@ -237,3 +237,45 @@ def test_batch_limits(cuda):
     with pytest.raises(native.IstiError):
         r.render_batch(bufs[:2], mixed, frame)
     r.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1, 3])
+@pytest.mark.parametrize("size", [(1, 1), (1, 9), (9, 1), (2, 3), (36, 4), (37, 5), (38, 5), (40, 8), (4097, 3), (65535, 2)],
+                         ids=lambda s: f"{s[0]}x{s[1]}")
+def test_extreme_shapes_match_oracle(cuda, size, mode):
+    """Degenerate and extreme image shapes: single pixels, single rows/columns, exactly the
+    key-tile box (36x4, 40x8), widths whose row pitch forbids the TMA tile path (37), the
+    16-bit key field's largest width (65535)."""
+    w, h = size
+    seq = Sequence(w, h, 2, seed=w * 7 + h, n_spheres=24, max_speed=2.0)
+    frame, client = seq.frame(0), seq.client(0, 2, mode=mode)
+    prev = np.full((h, w, 4), 77, np.uint8)
+    assert_bit_exact(render_gpu(frame, client, prev), *oracle.run_oracle(frame, client, prev))
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4])
+def test_nonfinite_inputs_render_without_fault(cuda, mode):
+    """NaN / +-inf depth and motion (outside the parity claim: NaN bit patterns differ
+    between CPU and GPU) must neither fault nor stop the renderer: every splat key and
+    search step stays inside its view."""
+    import torch
+    seq = Sequence(160, 90, 2, seed=808, aux_offsets=(0.3,), shadows=True)
+    frame = seq.frame(0)
+    for v in frame.views():
+        v.z = v.z.copy()
+        v.z[10:20, 10:40] = np.nan
+        v.z[30:35, :] = np.inf
+        v.z[40:42, 50:90] = -np.inf
+        m = v.motion.astype(np.float32)
+        m[50:60, 0:30] = np.nan
+        m[60:62, :, 0] = np.inf
+        v.motion = m.astype(np.float16)
+    client = seq.client(0, 2, mode=mode)
+    dev = DeviceFrame.from_host(frame)
+    out = torch.zeros((90, 160, 4), dtype=torch.uint8, device="cuda")
+    r = Renderer()
+    for _ in range(2):
+        r.render(out, client, dev)
+    torch.cuda.synchronize()
+    assert r.device_status() == 0
+    r.close()
