@@ -148,6 +148,18 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value: float, world: int, device=None) -> float:
+    """The largest value over all ranks (the slowest replica's time); the only
+    collective of the benchmark: replicas share no data."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ------------------------------------------------------------------ CPU (oracle port)
 
 def cpu_frames(seq, pairs):
@@ -174,7 +186,7 @@ def time_cpu(frames, budget_s: float, max_frames: int):
         t_total += time.perf_counter() - t0
         n += 1
         i += 1
-    return n * W * H / 1e6 / t_total, n, t_total
+    return (n * W * H / 1e6 / t_total if n else 0.0), n, t_total
 
 
 def run_reference(args):
@@ -285,11 +297,7 @@ def main_ours(args):
     r.enable_timing(False)
     ms = t0.elapsed_time(t1)
     tim = r.timing()
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(ms, world, dev)
     step_ms = sorted(a.elapsed_time(b) for a, b in sev)
     n_frames = args.steps * len(TS)
     value = world * n_frames * W * H / 1e6 / (ms / 1e3)
@@ -514,12 +522,7 @@ def run_e2e(args, seq, res, clients, r, dev, world):
         down.wait_stream(st)
     t1.record(down)
     torch.cuda.synchronize()
-    ms = t0.elapsed_time(t1)
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(t0.elapsed_time(t1), world, dev)
     value = world * args.steps * len(TS) * W * H / 1e6 / (ms / 1e3)
     return {"value": round(value, 2), "unit": "Mpix/s", "h2d_bytes_per_step": counters["h2d"] // args.steps,
             "d2h_bytes_per_step": counters["d2h"] // args.steps, "ms_per_step": round(ms / args.steps, 4),
