@@ -270,6 +270,8 @@ bool inflate(const uint8_t *src, size_t n, std::vector<uint8_t> &out, size_t max
         if (pos + extra > out.size())
             out.resize(std::max(pos + extra, std::min(max_out, out.size() * 2 + 65536)));
     };
+    if (max_out <= (size_t(1) << 31)) // a known output size (PNG, EXR): one allocation up front
+        ensure(max_out - pos);
     Huffman lit, dist;
     bool final = false;
     while (!final)
@@ -386,8 +388,19 @@ bool inflate(const uint8_t *src, size_t n, std::vector<uint8_t> &out, size_t max
             ensure(len);
             uint8_t *o = out.data() + pos;
             const uint8_t *from = o - d;
-            for (uint32_t k = 0; k < len; k++)
-                o[k] = from[k];
+            if (d >= len)
+                std::memcpy(o, from, len); // no overlap
+            else if (d >= 8)
+            {
+                uint32_t k = 0; // overlapping, but every 8-byte chunk reads bytes already written
+                for (; k + 8 <= len; k += 8)
+                    std::memcpy(o + k, from + k, 8);
+                for (; k < len; k++)
+                    o[k] = from[k];
+            }
+            else
+                for (uint32_t k = 0; k < len; k++)
+                    o[k] = from[k];
             pos += len;
         }
         if (b.overrun())
@@ -499,6 +512,15 @@ void zlib_compress(const uint8_t *src, size_t n, std::vector<uint8_t> &out)
             {
                 const size_t maxlen = std::min<size_t>(258, n - i);
                 uint32_t l = 0;
+                while (l + 8 <= maxlen) // 8 bytes at a time, then the tail
+                {
+                    uint64_t p, q;
+                    std::memcpy(&p, src + size_t(cand) + l, 8);
+                    std::memcpy(&q, src + i + l, 8);
+                    if (p != q)
+                        break;
+                    l += 8;
+                }
                 while (l < maxlen && src[size_t(cand) + l] == src[i + l])
                     l++;
                 if (l >= 3)
@@ -613,6 +635,21 @@ void png_emit_row(const PngHeader &hd, const uint8_t *r, uint32_t n, uint8_t *ds
 {
     static const uint8_t depth_scale[9] = {0, 0xff, 0x55, 0, 0x11, 0, 0, 0, 0x01};
     const int ch = png_channels(hd.color);
+    if (hd.depth == 8 && dx == 1 && (hd.color == 6 || (hd.color == 2 && !hd.has_trns)))
+    {
+        // the common layouts: RGBA8 as it is, RGB8 with opaque alpha
+        if (hd.color == 6)
+            std::memcpy(dst, r, size_t(n) * 4);
+        else
+            for (uint32_t i = 0; i < n; i++, dst += 4, r += 3)
+            {
+                dst[0] = r[0];
+                dst[1] = r[1];
+                dst[2] = r[2];
+                dst[3] = 255;
+            }
+        return;
+    }
     auto sample = [&](uint32_t i, int c) -> uint32_t {
         const uint32_t idx = i * uint32_t(ch) + uint32_t(c);
         if (hd.depth == 16)
@@ -849,42 +886,39 @@ void png_encode(uint32_t w, uint32_t h, int ch, const uint8_t *px, std::vector<u
 {
     const size_t row_bytes = size_t(w) * ch;
     std::vector<uint8_t> filtered(size_t(h) * (row_bytes + 1));
-    std::vector<uint8_t> cand(row_bytes);
     std::vector<uint8_t> zero(row_bytes, 0);
+    auto mag = [](uint8_t v) { return uint32_t(v < 128 ? v : 256 - v); };
     for (uint32_t y = 0; y < h; y++)
     {
         const uint8_t *r = px + size_t(y) * row_bytes;
         const uint8_t *up = y ? r - row_bytes : zero.data();
         uint8_t *dst = filtered.data() + size_t(y) * (row_bytes + 1);
-        // pick the filter with the smallest sum of |residual| (signed bytes)
-        uint64_t best_cost = UINT64_MAX;
-        for (int f = 0; f < 5; f++)
+        // the filter with the smallest sum of |residual| (signed bytes), all five costs in one pass
+        uint64_t cost[5] = {0, 0, 0, 0, 0};
+        for (size_t i = 0; i < row_bytes; i++)
         {
-            uint64_t cost = 0;
-            for (size_t i = 0; i < row_bytes; i++)
-            {
-                const int a = i >= size_t(ch) ? r[i - ch] : 0;
-                const int b = up[i];
-                const int c = i >= size_t(ch) ? up[i - ch] : 0;
-                int pred = 0;
-                switch (f)
-                {
-                case 1: pred = a; break;
-                case 2: pred = b; break;
-                case 3: pred = (a + b) >> 1; break;
-                case 4: pred = paeth(a, b, c); break;
-                default: break;
-                }
-                const uint8_t v = uint8_t(r[i] - pred);
-                cand[i] = v;
-                cost += uint64_t(v < 128 ? v : 256 - v);
-            }
-            if (cost < best_cost)
-            {
-                best_cost = cost;
-                dst[0] = uint8_t(f);
-                std::memcpy(dst + 1, cand.data(), row_bytes);
-            }
+            const int a = i >= size_t(ch) ? r[i - ch] : 0;
+            const int b = up[i];
+            const int c = i >= size_t(ch) ? up[i - ch] : 0;
+            const int x = r[i];
+            cost[0] += mag(uint8_t(x));
+            cost[1] += mag(uint8_t(x - a));
+            cost[2] += mag(uint8_t(x - b));
+            cost[3] += mag(uint8_t(x - ((a + b) >> 1)));
+            cost[4] += mag(uint8_t(x - paeth(a, b, c)));
+        }
+        int f = 0;
+        for (int k = 1; k < 5; k++)
+            if (cost[k] < cost[f])
+                f = k;
+        dst[0] = uint8_t(f);
+        for (size_t i = 0; i < row_bytes; i++)
+        {
+            const int a = i >= size_t(ch) ? r[i - ch] : 0;
+            const int b = up[i];
+            const int c = i >= size_t(ch) ? up[i - ch] : 0;
+            const int pred = f == 0 ? 0 : f == 1 ? a : f == 2 ? b : f == 3 ? (a + b) >> 1 : paeth(a, b, c);
+            dst[1 + i] = uint8_t(r[i] - pred);
         }
     }
     std::vector<uint8_t> z;

@@ -20,15 +20,20 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
+#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <filesystem>
 #include <iomanip>
 #include <iostream>
+#include <mutex>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace fs = std::filesystem;
@@ -161,6 +166,82 @@ mat4 mat_of(const float *v)
     return m;
 }
 
+// Encodes and writes the PNG files on worker threads, so that encoding overlaps the
+// rendering of the next frames (the reference encodes on the render thread).  At most
+// `max_queued` frames wait; submit() blocks beyond that.
+class PngWriterPool
+{
+public:
+    PngWriterPool(unsigned n_threads, size_t max_queued) : max_queued_(max_queued)
+    {
+        for (unsigned i = 0; i < n_threads; i++)
+            threads_.emplace_back([this] { work(); });
+    }
+    ~PngWriterPool()
+    {
+        std::string ignored;
+        finish(ignored);
+    }
+    void submit(std::string path, std::vector<uint8_t> rgba, int32_t w, int32_t h)
+    {
+        std::unique_lock<std::mutex> lock(m_);
+        room_.wait(lock, [&] { return queue_.size() < max_queued_; });
+        queue_.push_back(Job{std::move(path), std::move(rgba), w, h});
+        ready_.notify_one();
+    }
+    // waits for every submitted frame; false (with the first error) if one failed
+    bool finish(std::string &err)
+    {
+        {
+            std::lock_guard<std::mutex> lock(m_);
+            stop_ = true;
+        }
+        ready_.notify_all();
+        for (std::thread &t : threads_)
+            if (t.joinable())
+                t.join();
+        err = error_;
+        return error_.empty();
+    }
+
+private:
+    struct Job
+    {
+        std::string path;
+        std::vector<uint8_t> rgba;
+        int32_t w, h;
+    };
+    void work()
+    {
+        for (;;)
+        {
+            Job job;
+            {
+                std::unique_lock<std::mutex> lock(m_);
+                ready_.wait(lock, [&] { return stop_ || !queue_.empty(); });
+                if (queue_.empty())
+                    return;
+                job = std::move(queue_.front());
+                queue_.pop_front();
+                room_.notify_one();
+            }
+            if (isti_png_encode_file(job.path.c_str(), job.w, job.h, 4, job.rgba.data()) != ISTI_OK)
+            {
+                std::lock_guard<std::mutex> lock(m_);
+                if (error_.empty())
+                    error_ = isti_last_error();
+            }
+        }
+    }
+    size_t max_queued_;
+    std::vector<std::thread> threads_;
+    std::deque<Job> queue_;
+    std::mutex m_;
+    std::condition_variable ready_, room_;
+    bool stop_ = false;
+    std::string error_;
+};
+
 int fail(const std::string &what)
 {
     std::cout << std::endl << "Error - " << what << std::endl;
@@ -233,7 +314,8 @@ int main(int argc, char **argv)
     const size_t out_bytes = size_t(w) * h * 4;
     if (cudaMalloc(&d_out, out_bytes) != cudaSuccess || cudaMemsetAsync(d_out, 0, out_bytes, stream) != cudaSuccess)
         return fail("cannot allocate the output image");
-    std::vector<uint8_t> host_img(args.write_images ? out_bytes : 0);
+    const unsigned n_writers = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    PngWriterPool writers(args.write_images ? n_writers : 0, 2 * n_writers);
     isti_renderer *renderer = nullptr;
     if (isti_renderer_create(&renderer) != ISTI_OK)
         return fail(isti_last_error());
@@ -314,6 +396,7 @@ int main(int argc, char **argv)
             }
             if (args.write_images)
             {
+                std::vector<uint8_t> host_img(out_bytes);
                 if (cudaMemcpyAsync(host_img.data(), d_out, out_bytes, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
                     cudaStreamSynchronize(stream) != cudaSuccess)
                     return fail("cannot read the output image");
@@ -321,9 +404,7 @@ int main(int argc, char **argv)
                 const auto t1 = std::chrono::steady_clock::now();
                 std::ostringstream name;
                 name << std::setfill('0') << std::setw(4) << (frame_number - 1) << ".png";
-                if (isti_png_encode_file((fs::path(args.output) / name.str()).string().c_str(), int32_t(w), int32_t(h), 4,
-                                         host_img.data()) != ISTI_OK)
-                    return fail(isti_last_error());
+                writers.submit((fs::path(args.output) / name.str()).string(), std::move(host_img), int32_t(w), int32_t(h));
                 write_s += seconds_since(t1);
             }
             else
@@ -337,6 +418,13 @@ int main(int argc, char **argv)
         }
     }
     std::cout << std::endl;
+    {
+        const auto t1 = std::chrono::steady_clock::now();
+        std::string werr;
+        if (!writers.finish(werr))
+            return fail(werr);
+        write_s += seconds_since(t1);
+    }
 
     int32_t dev_status = 0;
     isti_renderer_device_status(renderer, &dev_status);
