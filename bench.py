@@ -425,10 +425,15 @@ def main_ours(args):
 
 def run_e2e(args, seq, res, clients, r, dev, world):
     """Streams keyframes from pinned host memory through the C ABI.  Per step the
-    newly arrived keyframe's data goes up (3 cameras: colour, z; the pair's motion
-    and shadow images), the 3 frames are rendered, the 3 frames come back.  Three
-    streams overlap the upload of step s + 1 and the read-back of step s - 1 with
-    the rendering of step s; the timed region spans all of them."""
+    newly arrived keyframe's data goes up (3 cameras: colour, z, backward motion
+    and shadows; plus the earlier keyframe's forward motion and shadows), the 3
+    frames are rendered, the 3 frames come back.  Each keyframe's images sit in
+    one pinned host slab and one device slab, ordered so that what a step needs
+    of it is one contiguous range: 2 large copies per step.  Every keyframe of
+    the cycle has its own device slab, so when the steps wrap around to the
+    first pair its earlier keyframe is still resident, as in an endless stream.
+    Three streams overlap the upload of step s + 1 and the read-back of step
+    s - 1 with the rendering of step s; the timed region spans all of them."""
     import numpy as np
     import torch
 
@@ -436,61 +441,88 @@ def run_e2e(args, seq, res, clients, r, dev, world):
 
     P = args.pairs
     n_cams = 1 + len(AUX)
+    # slab layout of one keyframe: [arrival part of camera 0..n-1 | forward part of camera 0..n-1]
+    # arrival = colour, z, backward motion, backward shadow A/B/Info; forward = forward motion, shadows
+    rgba, zb, mot = H * W * 4, H * W * 4, H * W * 6   # each a multiple of 256 bytes
+    arr_parts = [("color", rgba), ("z", zb), ("mb", mot), ("sb0", rgba), ("sb1", rgba), ("sb2", rgba)]
+    fwd_parts = [("mf", mot), ("sf0", rgba), ("sf1", rgba), ("sf2", rgba)]
+    arr_bytes, fwd_bytes = sum(n for _, n in arr_parts), sum(n for _, n in fwd_parts)
+    slab_bytes = n_cams * (arr_bytes + fwd_bytes)
 
-    def pin(a):
-        return torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+    def offsets():
+        off, out = 0, [dict() for _ in range(n_cams)]
+        for parts in (arr_parts, fwd_parts):
+            for c in range(n_cams):
+                for name, n in parts:
+                    out[c][name] = (off, n)
+                    off += n
+        return out
+    offs = offsets()
 
-    host = {}
+    def fields(slab, c):
+        """Tensor views of camera c's images inside one slab (host or device)."""
+        o = offs[c]
+        sl = lambda name: slab[o[name][0]:o[name][0] + o[name][1]]
+        img = lambda name: sl(name).view(H, W, 4)
+        return dict(color=img("color"), z=sl("z").view(torch.float32).view(H, W),
+                    mf=sl("mf").view(torch.float16).view(H, W, 3), mb=sl("mb").view(torch.float16).view(H, W, 3),
+                    sf=[img(f"sf{i}") for i in range(3)], sb=[img(f"sb{i}") for i in range(3)])
+
+    host = []
     for k in range(P + 1):
+        slab = torch.empty(slab_bytes, dtype=torch.uint8).pin_memory()
         for c in range(n_cams):
-            kf = seq.keyframe(k, c)
-            host[(k, c)] = dict(color=pin(kf.color), z=pin(kf.z), mf=pin(kf.motion_fwd), mb=pin(kf.motion_bwd),
-                                sf=[pin(a) for a in kf.shadow_fwd], sb=[pin(a) for a in kf.shadow_bwd])
-    like = lambda t: torch.empty_like(t, device=dev)
-    h0 = host[(0, 0)]
-    ring = [[dict(color=like(h0["color"]), z=like(h0["z"])) for _ in range(n_cams)] for _ in range(3)]   # keyframe colour/z
-    pair = [[dict(mf=like(h0["mf"]), mb=like(h0["mb"]), sf=[like(a) for a in h0["sf"]], sb=[like(a) for a in h0["sb"]])
-             for _ in range(n_cams)] for _ in range(2)]                                                  # per-pair data
+            kf, f = seq.keyframe(k, c), fields(slab, c)
+            f["color"].copy_(torch.from_numpy(np.ascontiguousarray(kf.color)))
+            f["z"].copy_(torch.from_numpy(np.ascontiguousarray(kf.z, np.float32)))
+            f["mf"].copy_(torch.from_numpy(np.ascontiguousarray(kf.motion_fwd, np.float16)))
+            f["mb"].copy_(torch.from_numpy(np.ascontiguousarray(kf.motion_bwd, np.float16)))
+            for i in range(3):
+                f["sf"][i].copy_(torch.from_numpy(np.ascontiguousarray(kf.shadow_fwd[i])))
+                f["sb"][i].copy_(torch.from_numpy(np.ascontiguousarray(kf.shadow_bwd[i])))
+        host.append(slab)
+    ring = [torch.empty(slab_bytes, dtype=torch.uint8, device=dev) for _ in range(P + 1)]
+    ring_fields = [[fields(s, c) for c in range(n_cams)] for s in ring]
+    A = n_cams * arr_bytes   # arrival part = [0, A), forward part = [A, slab_bytes)
     outs_dev = [[torch.zeros((H, W, 4), dtype=torch.uint8, device=dev) for _ in TS] for _ in range(2)]
     outs_host = [[torch.empty((H, W, 4), dtype=torch.uint8).pin_memory() for _ in TS] for _ in range(2)]
-    n_up = 4  # uploads spread over several streams (several copy engines)
-    ups = [torch.cuda.Stream(dev) for _ in range(n_up)]
-    up, comp, down = ups[0], torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    up, comp, down = torch.cuda.Stream(dev), torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    ups = [up]
     ev = lambda: torch.cuda.Event()
     up_done, comp_done, down_done = {}, {}, {}
     counters = {"h2d": 0, "d2h": 0}
-    resident = {}  # ring slot -> keyframe index held
+    resident = {}  # ring slot -> keyframe index whose arrival part it holds
+
+    last_use = {}  # (ring slot, "arr" | "fwd") -> last step that read that part
 
     def step(s, count):
         p = s % P
         k0, k1 = p, p + 1
-        ps = pair[s % 2]
-        if s - 2 in comp_done:
-            for u in ups:
-                u.wait_event(comp_done[s - 2])    # ring slot of keyframe k1 and pair slot s % 2 are free
-        if True:
-            copies = []
-            for c in range(n_cams):
-                hk0, hk1 = host[(k0, c)], host[(k1, c)]
-                if resident.get(k0 % 3) != k0:   # first step, or the pairs wrapped around
-                    copies += [(ring[k0 % 3][c]["color"], hk0["color"]), (ring[k0 % 3][c]["z"], hk0["z"])]
-                copies += [(ring[k1 % 3][c]["color"], hk1["color"]), (ring[k1 % 3][c]["z"], hk1["z"]),
-                           (ps[c]["mb"], hk1["mb"]), (ps[c]["mf"], hk0["mf"])]
-                copies += list(zip(ps[c]["sb"], hk1["sb"])) + list(zip(ps[c]["sf"], hk0["sf"]))
-            for i, (d, h) in enumerate(copies):
-                with torch.cuda.stream(ups[i % n_up]):
-                    d.copy_(h, non_blocking=True)
+        s0, s1 = k0, k1
+        copies = []  # (slot, part, keyframe): the arrival part of k1, the forward part of k0
+        if resident.get(s0) != k0:   # first step only: keyframe 0 is never a newly arrived one
+            copies.append((s0, "arr", k0))
+        copies += [(s0, "fwd", k0), (s1, "arr", k1)]
+        for slot, part, _ in copies:   # wait until no earlier step still reads the range
+            if (slot, part) in last_use:
+                up.wait_event(comp_done[last_use[(slot, part)]])
+        with torch.cuda.stream(up):
+            for slot, part, k in copies:
+                lo, hi = (0, A) if part == "arr" else (A, slab_bytes)
+                ring[slot][lo:hi].copy_(host[k][lo:hi], non_blocking=True)
                 if count:
-                    counters["h2d"] += h.numel() * h.element_size()
-            resident[k0 % 3], resident[k1 % 3] = k0, k1
-            up_done[s] = [ev() for _ in ups]
-            for e_, u in zip(up_done[s], ups):
-                e_.record(u)
+                    counters["h2d"] += hi - lo
+        resident[s0], resident[s1] = k0, k1
+        up_done[s] = [ev()]
+        up_done[s][0].record(up)
+        for key in ((s0, "arr"), (s0, "fwd"), (s1, "arr")):
+            last_use[key] = s
         views = []
         for c in range(n_cams):
             d0, d1 = res[(k0, c)], res[(k1, c)]
-            views.append((DeviceView(ring[k0 % 3][c]["color"], ring[k0 % 3][c]["z"], ps[c]["mf"], *ps[c]["sf"], d0["vp"], d0["ivp"]),
-                          DeviceView(ring[k1 % 3][c]["color"], ring[k1 % 3][c]["z"], ps[c]["mb"], *ps[c]["sb"], d1["vp"], d1["ivp"])))
+            f0, f1 = ring_fields[s0][c], ring_fields[s1][c]
+            views.append((DeviceView(f0["color"], f0["z"], f0["mf"], *f0["sf"], d0["vp"], d0["ivp"]),
+                          DeviceView(f1["color"], f1["z"], f1["mb"], *f1["sb"], d1["vp"], d1["ivp"])))
         fr = DeviceFrame(views[0][0], views[0][1], [v[0] for v in views[1:]], [v[1] for v in views[1:]], [3] * (n_cams - 1))
         od = outs_dev[s % 2]
         for e_ in up_done[s]:
@@ -526,7 +558,7 @@ def run_e2e(args, seq, res, clients, r, dev, world):
     value = world * args.steps * len(TS) * W * H / 1e6 / (ms / 1e3)
     return {"value": round(value, 2), "unit": "Mpix/s", "h2d_bytes_per_step": counters["h2d"] // args.steps,
             "d2h_bytes_per_step": counters["d2h"] // args.steps, "ms_per_step": round(ms / args.steps, 4),
-            "pipeline": "uploads on 4 streams / render / read-back overlapped"}
+            "pipeline": "one contiguous slab per keyframe, 2 uploads per step / render / read-back overlapped"}
 
 
 def main():
