@@ -8,7 +8,7 @@
 //   PNG      ISO/IEC 15948 (W3C PNG specification), converted to RGBA8 with
 //            the rules stb_image applies for 4 requested channels;
 //   OpenEXR  scan-line files (OpenEXR file layout document), NONE / RLE /
-//            ZIPS / ZIP compression, with the channel mapping of LoadEXR.
+//            ZIPS / ZIP / PIZ compression, with the channel mapping of LoadEXR.
 #include "isti_io.h"
 #include "isti_error.hpp"
 
@@ -1013,6 +1013,373 @@ void exr_unpredict(std::vector<uint8_t> &t, uint8_t *out)
         out[i] = (i & 1) ? t[half + i / 2] : t[i / 2];
 }
 
+// ---- PIZ (OpenEXR compression 4), restated from the published OpenEXR format:
+// a block of 32 scan lines is split into 16-bit words (a HALF sample is one
+// word, a FLOAT or UINT sample two, per channel plane), the words present are
+// remapped to a dense range through a 65536-bit presence bitmap, each plane is
+// transformed by a 2-D Haar-like wavelet, and the words are Huffman coded
+// with a run-length symbol.  Block layout: u16 first and last non-zero bitmap
+// byte, those bitmap bytes, i32 Huffman stream length, the Huffman stream.
+namespace piz
+{
+constexpr int kEncSize = 65537;   // code-length table entries (symbols 0..65535, plus one)
+constexpr int kDecBits = 14;      // bits of the direct decoding table
+constexpr int kDecSize = 1 << kDecBits;
+constexpr int kShortZeroRun = 59; // code lengths 59..62 encode 2..5 zero lengths
+constexpr int kLongZeroRun = 63;  // followed by 8 bits: 6..261 zero lengths
+constexpr int kShortestLongRun = 2 + kLongZeroRun - kShortZeroRun;
+
+struct Bits
+{
+    const uint8_t *p, *end;
+    uint64_t c = 0;
+    int lc = 0;
+    bool more() const { return p < end; }
+    bool fill(int nb) // at least nb (<= 56) bits buffered
+    {
+        while (lc < nb)
+        {
+            if (p >= end)
+                return false;
+            c = (c << 8) | *p++;
+            lc += 8;
+        }
+        return true;
+    }
+    bool get(int nb, uint64_t &v)
+    {
+        if (!fill(nb))
+            return false;
+        lc -= nb;
+        v = (c >> lc) & ((uint64_t(1) << nb) - 1);
+        return true;
+    }
+};
+
+struct DecEntry
+{
+    int len = 0;               // > 0: a code of at most kDecBits bits for symbol `sym`
+    uint32_t sym = 0;
+    std::vector<uint32_t> lng; // symbols of the longer codes sharing this kDecBits-bit prefix
+};
+
+// Code lengths of symbols lo..hi (6 bits each, with zero-run escapes), then the
+// canonical code of every symbol: entry = length | code << 6.  Codes are given
+// from the longest length down, each length's codes in symbol order.
+bool read_code_table(Bits &in, int lo, int hi, std::vector<uint64_t> &code)
+{
+    code.assign(kEncSize, 0);
+    for (int s = lo; s <= hi; s++)
+    {
+        uint64_t l;
+        if (!in.get(6, l))
+            return false;
+        int run = 0;
+        if (l == uint64_t(kLongZeroRun))
+        {
+            uint64_t r;
+            if (!in.get(8, r))
+                return false;
+            run = int(r) + kShortestLongRun;
+        }
+        else if (l >= uint64_t(kShortZeroRun))
+            run = int(l) - kShortZeroRun + 2;
+        if (run)
+        {
+            if (s + run > hi + 1)
+                return false;
+            s += run - 1; // entries are already zero
+        }
+        else
+            code[size_t(s)] = l;
+    }
+    uint64_t count[59] = {};
+    for (int s = 0; s < kEncSize; s++)
+        count[code[size_t(s)]]++;
+    uint64_t next = 0;
+    for (int l = 58; l > 0; l--)
+    {
+        const uint64_t start = next;
+        next = (next + count[l]) >> 1;
+        count[l] = start;
+    }
+    for (int s = 0; s < kEncSize; s++)
+    {
+        const uint64_t l = code[size_t(s)];
+        if (l > 0)
+            code[size_t(s)] = l | (count[l]++ << 6);
+    }
+    return true;
+}
+
+bool build_decoder(const std::vector<uint64_t> &code, int lo, int hi, std::vector<DecEntry> &dec)
+{
+    dec.assign(kDecSize, DecEntry());
+    for (int s = lo; s <= hi; s++)
+    {
+        const uint64_t c = code[size_t(s)] >> 6;
+        const int l = int(code[size_t(s)] & 63);
+        if (l == 0)
+            continue;
+        if (c >> l)
+            return false; // more code bits than its length
+        if (l > kDecBits)
+        {
+            DecEntry &e = dec[size_t(c >> (l - kDecBits))];
+            if (e.len)
+                return false;
+            e.lng.push_back(uint32_t(s));
+        }
+        else
+        {
+            const size_t first = size_t(c << (kDecBits - l)), cnt = size_t(1) << (kDecBits - l);
+            for (size_t i = first; i < first + cnt; i++)
+            {
+                if (dec[i].len || !dec[i].lng.empty())
+                    return false;
+                dec[i].len = l;
+                dec[i].sym = uint32_t(s);
+            }
+        }
+    }
+    return true;
+}
+
+// One decoded symbol: a literal word, or (the highest symbol) 8 bits of run length
+// repeating the previous word.
+inline bool emit(uint32_t sym, uint32_t run_sym, Bits &in, uint16_t *out, size_t &o, size_t no)
+{
+    if (sym == run_sym)
+    {
+        uint64_t cnt;
+        if (!in.get(8, cnt) || o == 0 || o + cnt > no)
+            return false;
+        const uint16_t prev = out[o - 1];
+        for (uint64_t i = 0; i < cnt; i++)
+            out[o++] = prev;
+        return true;
+    }
+    if (o >= no)
+        return false;
+    out[o++] = uint16_t(sym);
+    return true;
+}
+
+bool huffman_decode(const uint8_t *src, size_t n, uint16_t *out, size_t no)
+{
+    if (n == 0)
+        return no == 0;
+    if (n < 20)
+        return false;
+    const uint32_t lo = le32(src), hi = le32(src + 4), n_bits = le32(src + 12);
+    if (lo >= uint32_t(kEncSize) || hi >= uint32_t(kEncSize) || lo > hi)
+        return false;
+    Bits tab{src + 20, src + n};
+    std::vector<uint64_t> code;
+    if (!read_code_table(tab, int(lo), int(hi), code))
+        return false;
+    const size_t avail = size_t(src + n - tab.p);
+    if (uint64_t(n_bits) > 8 * uint64_t(avail))
+        return false;
+    std::vector<DecEntry> dec;
+    if (!build_decoder(code, int(lo), int(hi), dec))
+        return false;
+
+    Bits in{tab.p, tab.p + (size_t(n_bits) + 7) / 8};
+    size_t o = 0;
+    while (in.more())
+    {
+        in.c = (in.c << 8) | *in.p++;
+        in.lc += 8;
+        while (in.lc >= kDecBits)
+        {
+            const DecEntry &e = dec[size_t((in.c >> (in.lc - kDecBits)) & (kDecSize - 1))];
+            if (e.len)
+            {
+                in.lc -= e.len;
+                if (!emit(e.sym, hi, in, out, o, no))
+                    return false;
+                continue;
+            }
+            if (e.lng.empty())
+                return false;
+            bool found = false;
+            for (uint32_t s : e.lng)
+            {
+                const int l = int(code[s] & 63);
+                while (in.lc < l && in.more())
+                {
+                    in.c = (in.c << 8) | *in.p++;
+                    in.lc += 8;
+                }
+                if (in.lc >= l && (code[s] >> 6) == ((in.c >> (in.lc - l)) & ((uint64_t(1) << l) - 1)))
+                {
+                    in.lc -= l;
+                    if (!emit(s, hi, in, out, o, no))
+                        return false;
+                    found = true;
+                    break;
+                }
+            }
+            if (!found)
+                return false;
+        }
+    }
+    // the codes in the last partial byte: drop its padding bits, then decode short codes
+    const int pad = int((8 - n_bits) & 7);
+    in.c >>= pad;
+    in.lc -= pad;
+    while (in.lc > 0)
+    {
+        const DecEntry &e = dec[size_t((in.c << (kDecBits - in.lc)) & (kDecSize - 1))];
+        if (!e.len || e.len > in.lc)
+            return false;
+        in.lc -= e.len;
+        if (!emit(e.sym, hi, in, out, o, no))
+            return false;
+    }
+    return o == no;
+}
+
+// inverse of the 14-bit wavelet step (values below 1 << 14, signed arithmetic)
+inline void wdec14(uint16_t l, uint16_t h, uint16_t &a, uint16_t &b)
+{
+    const int ls = int16_t(l), hs = int16_t(h);
+    const int ai = ls + (hs & 1) + (hs >> 1);
+    a = uint16_t(int16_t(ai));
+    b = uint16_t(int16_t(ai - hs));
+}
+
+// inverse of the 16-bit wavelet step (modulo 2^16)
+inline void wdec16(uint16_t l, uint16_t h, uint16_t &a, uint16_t &b)
+{
+    const int m = l, d = h;
+    const int bb = (m - (d >> 1)) & 0xffff;
+    const int aa = (d + bb - 0x8000) & 0xffff;
+    a = uint16_t(aa);
+    b = uint16_t(bb);
+}
+
+// Inverse 2-D wavelet of an nx x ny plane of words at stride ox (x) and oy (y),
+// from the coarsest level to the finest.
+void wavelet_decode(uint16_t *in, int nx, int ox, int ny, int oy, uint16_t max_value)
+{
+    const bool w14 = max_value < (1 << 14);
+    auto dec = [w14](uint16_t l, uint16_t h, uint16_t &a, uint16_t &b) { w14 ? wdec14(l, h, a, b) : wdec16(l, h, a, b); };
+    const int n = nx > ny ? ny : nx;
+    int p = 1;
+    while (p <= n)
+        p <<= 1;
+    p >>= 1;
+    int p2 = p;
+    p >>= 1;
+    while (p >= 1)
+    {
+        const ptrdiff_t oy1 = ptrdiff_t(oy) * p, oy2 = ptrdiff_t(oy) * p2, ox1 = ptrdiff_t(ox) * p, ox2 = ptrdiff_t(ox) * p2;
+        const ptrdiff_t ey = ptrdiff_t(oy) * (ny - p2);
+        ptrdiff_t py = 0;
+        for (; py <= ey; py += oy2)
+        {
+            ptrdiff_t px = py;
+            const ptrdiff_t ex = py + ptrdiff_t(ox) * (nx - p2);
+            for (; px <= ex; px += ox2)
+            {
+                uint16_t *q00 = in + px, *q01 = q00 + ox1, *q10 = q00 + oy1, *q11 = q10 + ox1;
+                uint16_t i00, i01, i10, i11;
+                dec(*q00, *q10, i00, i10);
+                dec(*q01, *q11, i01, i11);
+                dec(i00, i01, *q00, *q01);
+                dec(i10, i11, *q10, *q11);
+            }
+            if (nx & p) // odd column: 1-D in y
+            {
+                uint16_t *q00 = in + px, *q10 = q00 + oy1, i00;
+                dec(*q00, *q10, i00, *q10);
+                *q00 = i00;
+            }
+        }
+        if (ny & p) // odd line: 1-D in x
+        {
+            ptrdiff_t px = py;
+            const ptrdiff_t ex = py + ptrdiff_t(ox) * (nx - p2);
+            for (; px <= ex; px += ox2)
+            {
+                uint16_t *q00 = in + px, *q01 = q00 + ox1, i00;
+                dec(*q00, *q01, i00, *q01);
+                *q00 = i00;
+            }
+        }
+        p2 = p;
+        p >>= 1;
+    }
+}
+
+// One PIZ block of `lines` scan lines of width w -> the uncompressed block (per
+// line, per channel in header order, little-endian samples).
+bool decompress(const uint8_t *src, size_t n, const std::vector<int> &words_per_sample, int w, int lines, uint8_t *out)
+{
+    size_t total = 0;
+    for (int s : words_per_sample)
+        total += size_t(w) * size_t(lines) * size_t(s);
+    if (n < 4)
+        return false;
+    const uint16_t min_nz = uint16_t(src[0] | src[1] << 8), max_nz = uint16_t(src[2] | src[3] << 8);
+    size_t pos = 4;
+    if (max_nz >= 8192)
+        return false;
+    std::vector<uint8_t> bitmap(8192, 0);
+    if (min_nz <= max_nz)
+    {
+        const size_t cnt = size_t(max_nz) - min_nz + 1;
+        if (pos + cnt > n)
+            return false;
+        std::memcpy(bitmap.data() + min_nz, src + pos, cnt);
+        pos += cnt;
+    }
+    // dense index -> word: 0 always, then every word whose bitmap bit is set
+    std::vector<uint16_t> lut(65536, 0);
+    size_t k = 0;
+    for (uint32_t i = 0; i < 65536; i++)
+        if (i == 0 || (bitmap[i >> 3] >> (i & 7) & 1))
+            lut[k++] = uint16_t(i);
+    const uint16_t max_value = uint16_t(k - 1);
+    if (pos + 4 > n)
+        return false;
+    const int32_t length = int32_t(le32(src + pos));
+    pos += 4;
+    if (length < 0 || size_t(length) > n - pos)
+        return false;
+    std::vector<uint16_t> words(total);
+    if (!huffman_decode(src + pos, size_t(length), words.data(), total))
+        return false;
+    size_t start = 0;
+    std::vector<size_t> plane(words_per_sample.size());
+    for (size_t c = 0; c < words_per_sample.size(); c++)
+    {
+        const int s = words_per_sample[c];
+        plane[c] = start;
+        for (int j = 0; j < s; j++)
+            wavelet_decode(words.data() + start + j, w, s, lines, w * s, max_value);
+        start += size_t(w) * size_t(lines) * size_t(s);
+    }
+    for (uint16_t &v : words)
+        v = lut[v];
+    uint8_t *o = out;
+    for (int y = 0; y < lines; y++)
+        for (size_t c = 0; c < words_per_sample.size(); c++)
+        {
+            const size_t cnt = size_t(w) * size_t(words_per_sample[c]);
+            const uint16_t *s = words.data() + plane[c] + size_t(y) * cnt;
+            for (size_t i = 0; i < cnt; i++)
+            {
+                *o++ = uint8_t(s[i]);
+                *o++ = uint8_t(s[i] >> 8);
+            }
+        }
+    return true;
+}
+} // namespace piz
+
 bool exr_decode(const uint8_t *d, size_t n, int &width, int &height, int &channels, std::vector<float> &result,
                 isti_status &status, std::string &err)
 {
@@ -1100,6 +1467,7 @@ bool exr_decode(const uint8_t *d, size_t n, int &width, int &height, int &channe
     case 1:
     case 2: lines_per_block = 1; break;
     case 3: lines_per_block = 16; break;
+    case 4: lines_per_block = 32; break;
     default: return status = ISTI_ERR_UNSUPPORTED, err = "exr: compression " + std::to_string(compression) + " is not supported", false;
     }
     const int64_t w64 = int64_t(box[2]) - box[0] + 1, h64 = int64_t(box[3]) - box[1] + 1;
@@ -1152,6 +1520,9 @@ bool exr_decode(const uint8_t *d, size_t n, int &width, int &height, int &channe
         ch_off[c] = line_bytes;
         line_bytes += size_t(w) * (chans[c].type == EXR_HALF ? 2 : 4);
     }
+    std::vector<int> piz_words(chans.size()); // 16-bit words per sample, for PIZ
+    for (size_t c = 0; c < chans.size(); c++)
+        piz_words[c] = chans[c].type == EXR_HALF ? 1 : 2;
     const int n_blocks = (h + lines_per_block - 1) / lines_per_block;
     if (pos + size_t(n_blocks) * 8 > n)
         return err = "exr: truncated offset table", false;
@@ -1188,6 +1559,11 @@ bool exr_decode(const uint8_t *d, size_t n, int &width, int &height, int &channe
             if (!exr_unrle(src, size, tmp.data(), raw))
                 return err = "exr: corrupt RLE chunk", false;
             exr_unpredict(tmp, block.data());
+        }
+        else if (compression == 4)
+        {
+            if (!piz::decompress(src, size, piz_words, w, lines, block.data()))
+                return err = "exr: corrupt PIZ chunk", false;
         }
         else
         {

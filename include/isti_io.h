@@ -19,11 +19,11 @@
  *                            and B must be among its first four channels and
  *                            the result is RGBA float (A = 1 when absent).
  *                            HALF samples are widened exactly; scan-line files
- *                            with NONE, RLE, ZIPS or ZIP compression.
+ *                            with NONE, RLE, ZIPS, ZIP or PIZ compression.
  *   isti_png_encode_file  <- fpng_encode_image_to_file (image_buffer.cu:185).
  *
  * Differences from the reference's libraries: tiled, multi-part, deep and
- * PIZ/PXR24/B44/DWA-compressed EXR files return ISTI_ERR_UNSUPPORTED, and the
+ * PXR24/B44/DWA-compressed EXR files return ISTI_ERR_UNSUPPORTED, and the
  * zlib checksum of PNG and EXR data is verified (stb_image skips it).
  * Decoded buffers are allocated with malloc; release them with
  * isti_image_free.  Errors set isti_last_error().

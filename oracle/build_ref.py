@@ -59,6 +59,9 @@ def build(reference: str, verbose: bool = False) -> str | None:
         os.path.join(HERE, "ref_host", "ref_driver.cpp"),
         os.path.join(HERE, "ref_host", "ref_runtime.cpp"),
         "-o", lib,
+        # the emulated cudaMalloc & co. must bind inside this library even when a real CUDA
+        # runtime is loaded globally into the process (torch loads one RTLD_GLOBAL)
+        "-Wl,-Bsymbolic",
     ]
     if verbose:
         print(" ".join(cmd))

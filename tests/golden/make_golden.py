@@ -123,6 +123,16 @@ def io_cases():
                 path = os.path.join(IO_DIR, name)
                 ref_io.exr_save(path, planes, names, pt, comp)
                 expected[name] = ref_io.exr_load(path)
+    # PIZ over three 32-line blocks (the last one partial), smooth and noisy planes
+    prng = np.random.default_rng(4242)  # own stream: the files above do not change
+    yy, xx = np.mgrid[0:70, 0:45].astype(np.float32)
+    for pt_name, pt in (("half", 1), ("float", 2)):
+        planes = np.stack([xx * 0.37 - yy, np.sin(xx * 0.2) * 40 + yy, prng.standard_normal((70, 45)) * 3000,
+                           prng.integers(0, 4, (70, 45)).astype(np.float32)]).astype(np.float32)
+        name = f"piz_blocks_{pt_name}_ABGR.exr"
+        path = os.path.join(IO_DIR, name)
+        ref_io.exr_save(path, planes, ["A", "B", "G", "R"], pt, 4)
+        expected[name] = ref_io.exr_load(path)
     np.savez_compressed(os.path.join(IO_DIR, "expected.npz"),
                         **{k: (np.array(v) if isinstance(v, str) else v) for k, v in expected.items()})
     print(f"io: {len(expected)} files")

@@ -44,11 +44,6 @@ def test_codec_fixtures_match_reference_decoders(built, kind):
             with pytest.raises(native.IstiError):
                 read(path)
             continue
-        if name.startswith("piz_"):  # PIZ is not implemented: a clear error, never wrong pixels
-            with pytest.raises(native.IstiError) as e:
-                read(path)
-            assert e.value.status == native.ISTI_ERR_UNSUPPORTED
-            continue
         got = read(path)
         assert got.shape == want.shape, name
         assert (_bits(got) == _bits(want)).all(), name
@@ -73,12 +68,25 @@ def test_codecs_against_live_reference(built, tmp_path):
         with open(p, "wb") as f:
             f.write(png_writer.make_png(s, depth, color, palette=pal, interlace=i % 2))
         assert (files.read_png(p) == ref_io.png_load(p)).all()
-    for comp in (0, 1, 2, 3):
+    for comp in (0, 1, 2, 3, 4):
         for pt in (1, 2):
             planes = (rng.standard_normal((4, 21, 30)) * 9).astype(np.float32)
             p = str(tmp_path / f"x{comp}{pt}.exr")
             ref_io.exr_save(p, planes, ["A", "B", "G", "R"], pt, comp)
             assert (_bits(files.read_exr(p)) == _bits(ref_io.exr_load(p))).all()
+    # PIZ over several 32-line blocks and odd sizes: few distinct words (14-bit wavelet
+    # path), smooth ramps, and random bits over the whole 16-bit range (16-bit path)
+    yy, xx = np.mgrid[0:77, 0:101].astype(np.float32)
+    cases = {"few": rng.integers(0, 5, (4, 77, 101)).astype(np.float32) * 0.25,
+             "ramp": np.stack([xx * 0.01 + yy, yy * 0.5 - xx, np.sin(xx * 0.1) * yy, xx * yy]),
+             "wide": rng.integers(0, 1 << 32, (4, 77, 101), dtype=np.uint64).astype(np.uint32).view(np.float32)}
+    for name, planes in cases.items():
+        planes = np.nan_to_num(planes, nan=1.0, posinf=2.0, neginf=-2.0)
+        for pt in (1, 2):
+            for names in (["A", "B", "G", "R"], ["Y"]):
+                p = str(tmp_path / f"piz_{name}{pt}{len(names)}.exr")
+                ref_io.exr_save(p, planes[:len(names)], names, pt, 4)
+                assert (_bits(files.read_exr(p)) == _bits(ref_io.exr_load(p))).all(), (name, pt, names)
     for ch in (1, 4):
         for zip_c in (False, True):
             img = (rng.standard_normal((19, 33) if ch == 1 else (19, 33, 4)) * 3).astype(np.float32)
