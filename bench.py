@@ -338,7 +338,7 @@ def main_ours(args):
     # per-frame data flow; the inputs-once figure is reported beside it.
     px = W * H
     n_views = 2 * n_cams
-    calls = max(1, tim["kernel_launches"] // 3)  # init, splat, reprojection per call
+    calls = max(1, tim["frames"] // len(TS))  # one batched call per step
     out_px = len(TS) * px
     alg = {"splat_kernel": n_views * (4 + 6) * out_px, "reproj_kernel": (n_views * (4 + 12) + 4) * out_px}
     once = {"splat_kernel": n_views * (4 + 6) * px, "reproj_kernel": n_views * (4 + 12) * px + len(TS) * 4 * px}

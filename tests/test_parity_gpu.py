@@ -140,6 +140,37 @@ def test_repeated_runs_bit_identical(cuda):
     r.close()
 
 
+def test_one_renderer_across_shapes_and_modes(cuda):
+    """One renderer, calls whose view sizes, aux cameras and modes change from call to call
+    (the arena is reused or regrown, timewarp uses it differently): every call matches the
+    oracle, keys included."""
+    import torch
+    seq_a = Sequence(320, 180, 2, seed=4101, aux_offsets=(-0.3, 0.3), shadows=True, max_speed=3.0)
+    seq_b = Sequence(320, 180, 2, seed=4102, aux_offsets=(0.3,), aux_size=(160, 90), shadows=True, max_speed=3.0)
+    seq_c = Sequence(200, 120, 2, seed=4103)
+    frames = {"a": seq_a.frame(0), "b": seq_b.frame(0), "c": seq_c.frame(0)}
+    seqs = {"a": seq_a, "b": seq_b, "c": seq_c}
+    devs = {k: DeviceFrame.from_host(f) for k, f in frames.items()}
+    r = Renderer()
+    plan = [("c", 1, 0), ("a", 2, 0), ("a", 3, 1), ("b", 1, 0), ("b", 2, 3), ("a", 2, 0), ("a", 2, 4), ("a", 1, 0),
+            ("a", 3, 2), ("c", 2, 0), ("c", 1, 4), ("a", 0, 0)]
+    for i, (name, b, mode) in enumerate(plan):
+        frame, client = frames[name], seqs[name].client(0, b, mode=mode)
+        h, w = client.height, client.width
+        prev = np.full((h, w, 4), i, np.uint8)
+        out = torch.from_numpy(prev.copy()).cuda()
+        r.render(out, client, devs[name])
+        torch.cuda.synchronize()
+        assert r.device_status() == 0
+        exp = oracle.run_oracle(frame, client, prev, with_intermediates=mode != native.MODE_TIMEWARP)
+        assert np.array_equal(out.cpu().numpy(), exp[0]), f"call {i} ({name}, mode {mode}) differs"
+        if mode != native.MODE_TIMEWARP:
+            for v in range(len(frame.views())):
+                keys = r.view_buffers(v)[0].cpu().numpy().view(np.uint64)
+                assert np.array_equal(keys, exp[1][v]), f"call {i} view {v} keys differ"
+    r.close()
+
+
 def test_temporal_hole_filling_keeps_previous_output(cuda):
     seq = Sequence(320, 180, 2, seed=505)
     frame, client = seq.frame(0), seq.client(0, 2)
