@@ -19,8 +19,9 @@ value: device-resident throughput (CUDA events on the rendering stream).
 e2e:   the same metric through the C ABI with host buffers: each step
        uploads the newly arrived keyframe data from pinned host memory
        (colour, z, motion and shadow images of the new keyframe for the 3
-       cameras, plus the earlier keyframe's forward motion and shadows) and
-       reads the 3 output frames back.
+       cameras, plus the earlier keyframe's forward motion and shadows; the
+       shadow images as RGB, expanded to RGBA on the device, since their alpha
+       is never read) and reads the 3 output frames back.
 
 --impl reference times the reference's per-frame algorithm on the host
 cores (the C oracle, OpenMP over all threads: the reference has no CPU
@@ -434,39 +435,38 @@ def run_e2e(args, seq, res, clients, r, dev, world):
     first pair its earlier keyframe is still resident, as in an endless stream.
     Three streams overlap the upload of step s + 1 and the read-back of step
     s - 1 with the rendering of step s; the timed region spans all of them."""
+    import ctypes as C
+
     import numpy as np
     import torch
 
+    from imagebasedspatiotemporalinterpolation_gb300 import native
     from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame, DeviceView
 
     P = args.pairs
     n_cams = 1 + len(AUX)
-    # slab layout of one keyframe: [arrival part of camera 0..n-1 | forward part of camera 0..n-1]
-    # arrival = colour, z, backward motion, backward shadow A/B/Info; forward = forward motion, shadows
-    rgba, zb, mot = H * W * 4, H * W * 4, H * W * 6   # each a multiple of 256 bytes
-    arr_parts = [("color", rgba), ("z", zb), ("mb", mot), ("sb0", rgba), ("sb1", rgba), ("sb2", rgba)]
-    fwd_parts = [("mf", mot), ("sf0", rgba), ("sf1", rgba), ("sf2", rgba)]
-    arr_bytes, fwd_bytes = sum(n for _, n in arr_parts), sum(n for _, n in fwd_parts)
-    slab_bytes = n_cams * (arr_bytes + fwd_bytes)
-
-    def offsets():
-        off, out = 0, [dict() for _ in range(n_cams)]
-        for parts in (arr_parts, fwd_parts):
-            for c in range(n_cams):
-                for name, n in parts:
-                    out[c][name] = (off, n)
-                    off += n
-        return out
-    offs = offsets()
+    # Slab layout of one keyframe: [arrival part | forward part], each grouped by image kind
+    # over the cameras.  arrival = colour, z, backward motion, backward shadow A/B/Info;
+    # forward = forward motion, forward shadows.  Shadow images travel as packed RGB (the
+    # renderer never reads their alpha) and are expanded to RGBA on the device after upload
+    # (isti_rgb8_to_rgba8), one launch per part.
+    rgba, zb, mot, rgb = H * W * 4, H * W * 4, H * W * 6, H * W * 3   # each a multiple of 256 bytes
+    layout, off = {}, 0
+    for kind, n in (("color", rgba), ("z", zb), ("mb", mot), ("sb", 3 * rgb), ("mf", mot), ("sf", 3 * rgb)):
+        for c in range(n_cams):
+            layout[(kind, c)] = (off, n)
+            off += n
+    slab_bytes = off
+    A = layout[("mf", 0)][0]            # arrival part = [0, A), forward part = [A, slab_bytes)
+    sb_lo, sf_lo = layout[("sb", 0)][0], layout[("sf", 0)][0]
+    n_shadow = n_cams * 3               # shadow images per part
 
     def fields(slab, c):
         """Tensor views of camera c's images inside one slab (host or device)."""
-        o = offs[c]
-        sl = lambda name: slab[o[name][0]:o[name][0] + o[name][1]]
-        img = lambda name: sl(name).view(H, W, 4)
-        return dict(color=img("color"), z=sl("z").view(torch.float32).view(H, W),
+        sl = lambda kind: slab[layout[(kind, c)][0]:layout[(kind, c)][0] + layout[(kind, c)][1]]
+        return dict(color=sl("color").view(H, W, 4), z=sl("z").view(torch.float32).view(H, W),
                     mf=sl("mf").view(torch.float16).view(H, W, 3), mb=sl("mb").view(torch.float16).view(H, W, 3),
-                    sf=[img(f"sf{i}") for i in range(3)], sb=[img(f"sb{i}") for i in range(3)])
+                    sf=sl("sf").view(3, H, W, 3), sb=sl("sb").view(3, H, W, 3))
 
     host = []
     for k in range(P + 1):
@@ -478,22 +478,33 @@ def run_e2e(args, seq, res, clients, r, dev, world):
             f["mf"].copy_(torch.from_numpy(np.ascontiguousarray(kf.motion_fwd, np.float16)))
             f["mb"].copy_(torch.from_numpy(np.ascontiguousarray(kf.motion_bwd, np.float16)))
             for i in range(3):
-                f["sf"][i].copy_(torch.from_numpy(np.ascontiguousarray(kf.shadow_fwd[i])))
-                f["sb"][i].copy_(torch.from_numpy(np.ascontiguousarray(kf.shadow_bwd[i])))
+                f["sf"][i].copy_(torch.from_numpy(np.ascontiguousarray(kf.shadow_fwd[i][..., :3])))
+                f["sb"][i].copy_(torch.from_numpy(np.ascontiguousarray(kf.shadow_bwd[i][..., :3])))
         host.append(slab)
     ring = [torch.empty(slab_bytes, dtype=torch.uint8, device=dev) for _ in range(P + 1)]
-    ring_fields = [[fields(s, c) for c in range(n_cams)] for s in ring]
-    A = n_cams * arr_bytes   # arrival part = [0, A), forward part = [A, slab_bytes)
+    # RGBA shadow images the renderer reads, per slot: [backward | forward][camera][A, B, Info]
+    shadow = [torch.empty((2, n_cams, 3, H, W, 4), dtype=torch.uint8, device=dev) for _ in range(P + 1)]
+    ring_fields = []
+    for s_, sh in zip(ring, shadow):
+        per_cam = []
+        for c in range(n_cams):
+            f = fields(s_, c)
+            f["sb"], f["sf"] = [sh[0, c, i] for i in range(3)], [sh[1, c, i] for i in range(3)]
+            per_cam.append(f)
+        ring_fields.append(per_cam)
+    lib = native.load()
     outs_dev = [[torch.zeros((H, W, 4), dtype=torch.uint8, device=dev) for _ in TS] for _ in range(2)]
     outs_host = [[torch.empty((H, W, 4), dtype=torch.uint8).pin_memory() for _ in TS] for _ in range(2)]
     up, comp, down = torch.cuda.Stream(dev), torch.cuda.Stream(dev), torch.cuda.Stream(dev)
-    ups = [up]
+    xp = torch.cuda.Stream(dev, priority=-1)   # RGB -> RGBA expansion of the uploaded shadow images
+    ups = [up, xp]
     ev = lambda: torch.cuda.Event()
     up_done, comp_done, down_done = {}, {}, {}
-    counters = {"h2d": 0, "d2h": 0}
+    counters = {"h2d": 0, "d2h": 0, "launches": 0}
     resident = {}  # ring slot -> keyframe index whose arrival part it holds
 
     last_use = {}  # (ring slot, "arr" | "fwd") -> last step that read that part
+    last_frame = []  # [pair, DeviceFrame] of the latest step
 
     def step(s, count):
         p = s % P
@@ -506,15 +517,23 @@ def run_e2e(args, seq, res, clients, r, dev, world):
         for slot, part, _ in copies:   # wait until no earlier step still reads the range
             if (slot, part) in last_use:
                 up.wait_event(comp_done[last_use[(slot, part)]])
-        with torch.cuda.stream(up):
-            for slot, part, k in copies:
-                lo, hi = (0, A) if part == "arr" else (A, slab_bytes)
+        for slot, part, k in copies:
+            lo, hi = (0, A) if part == "arr" else (A, slab_bytes)
+            with torch.cuda.stream(up):
                 ring[slot][lo:hi].copy_(host[k][lo:hi], non_blocking=True)
-                if count:
-                    counters["h2d"] += hi - lo
+            # the expansion runs on its own high-priority stream, so the link keeps copying
+            copied = ev()
+            copied.record(up)
+            xp.wait_event(copied)
+            src = ring[slot][sb_lo if part == "arr" else sf_lo:][:n_shadow * rgb]
+            dst = shadow[slot][0 if part == "arr" else 1]
+            native.check(lib.isti_rgb8_to_rgba8(dst.data_ptr(), src.data_ptr(), n_shadow * H * W, C.c_void_p(xp.cuda_stream)))
+            if count:
+                counters["h2d"] += hi - lo
+                counters["launches"] += 1
         resident[s0], resident[s1] = k0, k1
         up_done[s] = [ev()]
-        up_done[s][0].record(up)
+        up_done[s][0].record(xp)
         for key in ((s0, "arr"), (s0, "fwd"), (s1, "arr")):
             last_use[key] = s
         views = []
@@ -524,6 +543,7 @@ def run_e2e(args, seq, res, clients, r, dev, world):
             views.append((DeviceView(f0["color"], f0["z"], f0["mf"], *f0["sf"], d0["vp"], d0["ivp"]),
                           DeviceView(f1["color"], f1["z"], f1["mb"], *f1["sb"], d1["vp"], d1["ivp"])))
         fr = DeviceFrame(views[0][0], views[0][1], [v[0] for v in views[1:]], [v[1] for v in views[1:]], [3] * (n_cams - 1))
+        last_frame[:] = [p, fr]
         od = outs_dev[s % 2]
         for e_ in up_done[s]:
             comp.wait_event(e_)
@@ -556,9 +576,28 @@ def run_e2e(args, seq, res, clients, r, dev, world):
     torch.cuda.synchronize()
     ms = max_over_ranks(t0.elapsed_time(t1), world, dev)
     value = world * args.steps * len(TS) * W * H / 1e6 / (ms / 1e3)
+
+    # outside the timed region: the streamed views of the last step render what the
+    # resident keyframes of the same pair render (slab layout and RGB expansion checked)
+    p, fr = last_frame
+    d_views = [(DeviceView(res[(p, c)]["color"], res[(p, c)]["z"], res[(p, c)]["mf"], *res[(p, c)]["sf"], res[(p, c)]["vp"],
+                           res[(p, c)]["ivp"]),
+                DeviceView(res[(p + 1, c)]["color"], res[(p + 1, c)]["z"], res[(p + 1, c)]["mb"], *res[(p + 1, c)]["sb"],
+                           res[(p + 1, c)]["vp"], res[(p + 1, c)]["ivp"])) for c in range(n_cams)]
+    resident_fr = DeviceFrame(d_views[0][0], d_views[0][1], [v[0] for v in d_views[1:]], [v[1] for v in d_views[1:]],
+                              [3] * (n_cams - 1))
+    got = [torch.zeros((H, W, 4), dtype=torch.uint8, device=dev) for _ in TS]
+    want = [torch.zeros_like(g) for g in got]
+    r.render_batch(got, clients[p], fr, chain=True, stream=comp)
+    r.render_batch(want, clients[p], resident_fr, chain=True, stream=comp)
+    comp.synchronize()
+    if not all(torch.equal(a, b) for a, b in zip(got, want)):
+        raise RuntimeError("e2e: frames rendered from the streamed keyframes differ from the resident ones")
     return {"value": round(value, 2), "unit": "Mpix/s", "h2d_bytes_per_step": counters["h2d"] // args.steps,
             "d2h_bytes_per_step": counters["d2h"] // args.steps, "ms_per_step": round(ms / args.steps, 4),
-            "pipeline": "one contiguous slab per keyframe, 2 uploads per step / render / read-back overlapped"}
+            "expand_launches_per_step": counters["launches"] / args.steps,
+            "pipeline": "one contiguous slab per keyframe, 2 uploads per step (shadow images as RGB, "
+                        "expanded to RGBA on the device) / render / read-back overlapped"}
 
 
 def main():

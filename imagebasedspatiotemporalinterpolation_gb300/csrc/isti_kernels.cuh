@@ -960,6 +960,29 @@ __global__ void depth_to_z_kernel(float *__restrict__ z, size_t n)
         z[tail] = unity_depth_to_z(z[tail]);
 }
 
+// Packed RGB8 -> RGBA8 with alpha 255.  VEC (src 4-byte and dst 16-byte aligned): a thread
+// turns 3 source words (4 pixels, byte 0 = R of the first) into one 16-byte store.
+template <bool VEC>
+__global__ void rgb8_to_rgba8_kernel(uint32_t *__restrict__ dst, const uint8_t *__restrict__ src, size_t n)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t groups = VEC ? n / 4 : 0;
+    const uint32_t *s32 = reinterpret_cast<const uint32_t *>(src);
+    for (size_t g = t; g < groups; g += stride)
+    {
+        const uint32_t w0 = __ldg(s32 + 3 * g), w1 = __ldg(s32 + 3 * g + 1), w2 = __ldg(s32 + 3 * g + 2);
+        uint4 o;
+        o.x = (w0 & 0xffffffu) | 0xff000000u;
+        o.y = (w0 >> 24) | ((w1 & 0xffffu) << 8) | 0xff000000u;
+        o.z = (w1 >> 16) | ((w2 & 0xffu) << 16) | 0xff000000u;
+        o.w = (w2 >> 8) | 0xff000000u;
+        reinterpret_cast<uint4 *>(dst)[g] = o;
+    }
+    for (size_t i = groups * 4 + t; i < n; i += stride)
+        dst[i] = (uint32_t)__ldg(src + 3 * i) | (uint32_t)__ldg(src + 3 * i + 1) << 8 | (uint32_t)__ldg(src + 3 * i + 2) << 16 | 0xff000000u;
+}
+
 // Dynamic shared memory of one reprojection block.
 template <int SW>
 constexpr size_t reproj_smem(int n_views, int n_frames, int frames_per_group)

@@ -665,6 +665,30 @@ extern "C" isti_status isti_render_noalloc(void *out_rgba, const isti_render_inf
     return ISTI_OK;
 }
 
+// RGB8 upload format -> RGBA8, declared in include/isti_dataset.h.
+extern "C" isti_status isti_rgb8_to_rgba8(void *dst_rgba, const void *src_rgb, size_t n_pixels, void *stream_ptr)
+{
+    if (n_pixels == 0)
+        return ISTI_OK;
+    if (!dst_rgba || !src_rgb || ((uintptr_t)dst_rgba & 3u))
+        return fail(ISTI_ERR_INVALID_ARG, "isti_rgb8_to_rgba8: NULL or unaligned buffer");
+    const uintptr_t d = (uintptr_t)dst_rgba, s = (uintptr_t)src_rgb;
+    if (d < s + 3 * n_pixels && s < d + 4 * n_pixels)
+        return fail(ISTI_ERR_INVALID_ARG, "isti_rgb8_to_rgba8: buffers overlap");
+    const bool vec = (d & 15u) == 0 && (s & 3u) == 0;
+    const size_t work = vec ? n_pixels / 4 + 3 : n_pixels;
+    const unsigned blocks = (unsigned)std::min<size_t>((work + 255) / 256, 152 * 16);
+    cudaStream_t st = static_cast<cudaStream_t>(stream_ptr);
+    uint32_t *dst = static_cast<uint32_t *>(dst_rgba);
+    const uint8_t *src = static_cast<const uint8_t *>(src_rgb);
+    if (vec)
+        isti::rgb8_to_rgba8_kernel<true><<<blocks, 256, 0, st>>>(dst, src, n_pixels);
+    else
+        isti::rgb8_to_rgba8_kernel<false><<<blocks, 256, 0, st>>>(dst, src, n_pixels);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? ISTI_OK : cuda_fail(e, "isti_rgb8_to_rgba8");
+}
+
 // convertDepthToZ_kernel (src/file_reader.cu:17-37), declared in include/isti_dataset.h.
 extern "C" isti_status isti_depth_to_z(float *depth, int32_t width, int32_t height, void *stream_ptr)
 {

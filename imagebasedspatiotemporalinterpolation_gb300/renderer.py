@@ -239,3 +239,16 @@ def render_noalloc(render_buffer, info, frame_data: DeviceFrame, stream=None) ->
         raise ValueError("render_buffer must be a (H, W, 4) uint8 tensor of the render resolution")
     s = (stream or torch.cuda.current_stream()).cuda_stream
     check(lib.isti_render_noalloc(_dptr(render_buffer), C.byref(ri), C.byref(frame_data.to_c()), C.c_void_p(s)))
+
+
+def rgb8_to_rgba8(dst, src, stream=None) -> None:
+    """isti_rgb8_to_rgba8: a packed RGB8 device tensor (..., 3) uint8 -> the RGBA8 tensor
+    (..., 4) uint8 the renderer reads, alpha 255.  For images whose alpha the renderer
+    never reads (shadow colour A/B, shadow info): uploading them as RGB moves 3/4 of the
+    bytes over the host link."""
+    torch = _torch()
+    if src.dtype != torch.uint8 or dst.dtype != torch.uint8 or src.shape[-1] != 3 or dst.shape[-1] != 4 \
+            or src.shape[:-1] != dst.shape[:-1] or not src.is_contiguous() or not dst.is_contiguous():
+        raise ValueError("rgb8_to_rgba8 expects contiguous uint8 (..., 3) -> (..., 4) tensors of the same pixel count")
+    s = (stream or torch.cuda.current_stream()).cuda_stream
+    check(native.load().isti_rgb8_to_rgba8(_dptr(dst), _dptr(src), C.c_size_t(src.numel() // 3), C.c_void_p(s)))

@@ -94,6 +94,14 @@ void isti_dataset_close(isti_dataset *d);
 isti_status isti_depth_to_z(float *depth, int32_t width, int32_t height, void *stream);
 isti_status isti_normalize_proj(const float proj[16], float out[16]);
 
+/* Packed RGB8 (3 bytes per pixel, device) -> the RGBA8 image the renderer reads
+ * (device, 4-byte aligned), alpha 255 (stb_image's fill for images without
+ * alpha).  No counterpart in the reference, which uploads RGBA: the renderer
+ * never reads the alpha bytes of shadow colour A/B and shadow info images, so a
+ * caller bound by the host link can upload those as RGB (3/4 of the bytes) and
+ * expand them on the device.  dst and src must not overlap. */
+isti_status isti_rgb8_to_rgba8(void *dst_rgba, const void *src_rgb, size_t n_pixels, void *stream);
+
 /* Host matrix helpers of the frame loop (src/main.cu:26-28,161,176), the glm
  * operations the reference applies: out = a * b, out = inverse(m), and
  * glm::interpolate(m1, m2, t). */

@@ -206,3 +206,37 @@ def test_dataset_loader_buffers(aux_dataset):
     info = ds.camera(-1)
     assert (info["width"], info["height"], info["server_fps"], info["n_frames"]) == (96, 54, 30, 3)
     ds.close()
+
+
+def test_rgb8_to_rgba8_upload_format(cuda):
+    """isti_rgb8_to_rgba8: packed RGB8 -> RGBA8 with alpha 255, on the vector path (aligned
+    buffers, 4 pixels per thread) and the byte path (unaligned), any pixel count."""
+    import torch
+
+    from imagebasedspatiotemporalinterpolation_gb300 import native
+    from imagebasedspatiotemporalinterpolation_gb300.renderer import rgb8_to_rgba8
+
+    rng = np.random.default_rng(5)
+    lib = native.load()
+    for n in (0, 1, 3, 4, 5, 7, 1023, 1920 * 1080 + 3):
+        rgb = rng.integers(0, 256, (n, 3), dtype=np.uint8)
+        want = np.concatenate([rgb, np.full((n, 1), 255, np.uint8)], 1)
+        for src_off, dst_off in ((0, 0), (1, 0), (0, 1), (3, 2)):
+            src_buf = torch.zeros(3 * n + 16, dtype=torch.uint8, device="cuda")
+            dst_buf = torch.zeros(4 * n + 64, dtype=torch.uint8, device="cuda")
+            src = src_buf[src_off:src_off + 3 * n]
+            src.copy_(torch.from_numpy(rgb.reshape(-1)))
+            dst = dst_buf[4 * dst_off:4 * dst_off + 4 * n]
+            native.check(lib.isti_rgb8_to_rgba8(dst.data_ptr(), src.data_ptr(), n, None))
+            torch.cuda.synchronize()
+            assert np.array_equal(dst.cpu().numpy().reshape(n, 4), want), (n, src_off, dst_off)
+            assert not dst_buf[:4 * dst_off].any() and not dst_buf[4 * dst_off + 4 * n:].any()  # nothing outside
+    img = torch.from_numpy(rng.integers(0, 256, (37, 53, 3), dtype=np.uint8)).cuda()
+    out = torch.empty((37, 53, 4), dtype=torch.uint8, device="cuda")
+    rgb8_to_rgba8(out, img)
+    assert torch.equal(out[..., :3], img) and bool((out[..., 3] == 255).all())
+    buf = torch.zeros(4096, dtype=torch.uint8, device="cuda")
+    with pytest.raises(native.IstiError):   # overlapping buffers
+        native.check(lib.isti_rgb8_to_rgba8(buf.data_ptr(), buf.data_ptr() + 8, 100, None))
+    with pytest.raises(native.IstiError):   # destination not 4-byte aligned
+        native.check(lib.isti_rgb8_to_rgba8(buf.data_ptr() + 2, buf.data_ptr() + 2048, 10, None))
