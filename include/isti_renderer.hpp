@@ -10,7 +10,13 @@
 // texture objects (reads outside an image return zero in both); matrices are
 // isti::Mat4 (column-major, m[column][row] like glm::mat4, and constructible
 // from a glm::mat4); Renderer::render takes an optional stream and does not
-// block the host; errors throw isti::Error carrying the isti_status.
+// block the host.
+// Errors as in the reference: a failing CUDA call or render is printed to
+// stdout and execution continues (CUDA_CHECK_THROW,
+// include/util/cuda_helper_host.h:19-29); Renderer::last_status() holds the
+// isti_status of the last render.  What the reference throws (a resize to
+// another size, an unreadable image file, a size mismatch) throws here too, as
+// isti::Error, a std::runtime_error.
 // Header-only; link libisti.so and the CUDA runtime.
 #pragma once
 
@@ -22,6 +28,7 @@
 #include <cstdint>
 #include <cstring>
 #include <filesystem>
+#include <iostream>
 #include <memory>
 #include <optional>
 #include <stdexcept>
@@ -45,10 +52,13 @@ inline void check(isti_status s)
         throw Error(s, isti_last_error());
 }
 
-inline void check_cuda(cudaError_t e, const char *what)
+// Prints a failed CUDA call and carries on, like the reference's CUDA_CHECK_THROW.
+inline bool check_cuda(cudaError_t e, const char *what)
 {
-    if (e != cudaSuccess)
-        throw Error(ISTI_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    if (e == cudaSuccess)
+        return true;
+    std::cout << "CUDA | " << what << " failed with error: " << cudaGetErrorString(e) << std::endl;
+    return false;
 }
 
 // 4x4 float matrix, column-major: m[c][r] is row r of column c (glm::mat4's layout).
@@ -120,9 +130,9 @@ public:
             return;
         if (_resolution.x != 0 || _resolution.y != 0)
             throw std::runtime_error("Resizing of ImageBuffer currently not supported");
-        check_cuda(cudaMalloc(&_ptr, bytes_for(resolution)), "ImageBuffer::resize");
         _resolution = resolution;
-        check_cuda(cudaMemset(_ptr, 0, bytes()), "ImageBuffer::resize");
+        if (check_cuda(cudaMalloc(&_ptr, bytes()), "cudaMalloc (ImageBuffer::resize)"))
+            check_cuda(cudaMemset(_ptr, 0, bytes()), "cudaMemset (ImageBuffer::resize)");
     }
 
     void memsetBuffer(T val)
@@ -130,8 +140,11 @@ public:
         std::vector<T> tmp(size_t(_resolution.x) * _resolution.y, val);
         upload(tmp.data());
     }
-    void download(T *h_buffer) const { check_cuda(cudaMemcpy(h_buffer, _ptr, bytes(), cudaMemcpyDeviceToHost), "ImageBuffer::download"); }
-    void upload(const T *h_buffer) { check_cuda(cudaMemcpy(_ptr, h_buffer, bytes(), cudaMemcpyHostToDevice), "ImageBuffer::upload"); }
+    void download(T *h_buffer) const
+    {
+        check_cuda(cudaMemcpy(h_buffer, _ptr, bytes(), cudaMemcpyDeviceToHost), "cudaMemcpy (ImageBuffer::download)");
+    }
+    void upload(const T *h_buffer) { check_cuda(cudaMemcpy(_ptr, h_buffer, bytes(), cudaMemcpyHostToDevice), "cudaMemcpy (ImageBuffer::upload)"); }
 
     // PNG into uchar4 images, EXR into float (one channel) or float4 (RGBA) images
     // (ImageBuffer::readFromFile, src/util/image_buffer.cu:103-178)
@@ -141,7 +154,9 @@ public:
         if (filename.extension() == ".exr")
         {
             float *px = nullptr;
-            check(isti_exr_decode_file(filename.string().c_str(), &w, &h, &ch, &px));
+            const isti_status s = isti_exr_decode_file(filename.string().c_str(), &w, &h, &ch, &px);
+            if (s != ISTI_OK)
+                throw Error(s, "Error loading EXR file " + filename.string() + ": " + isti_last_error());
             std::unique_ptr<void, decltype(&isti_image_free)> guard(px, isti_image_free);
             if (ch * (int)sizeof(float) != (int)sizeof(T))
                 throw std::runtime_error("EXR channel count does not match the image type: " + filename.string());
@@ -151,7 +166,9 @@ public:
         else
         {
             uint8_t *px = nullptr;
-            check(isti_png_decode_file(filename.string().c_str(), &w, &h, &px));
+            const isti_status s = isti_png_decode_file(filename.string().c_str(), &w, &h, &px);
+            if (s != ISTI_OK)
+                throw Error(s, "Could not load image " + filename.string() + " (" + isti_last_error() + ")");
             std::unique_ptr<void, decltype(&isti_image_free)> guard(px, isti_image_free);
             if (sizeof(T) != 4)
                 throw std::runtime_error("PNG files load into 4-byte RGBA images: " + filename.string());
@@ -325,7 +342,7 @@ struct FrameData
 class Renderer
 {
 public:
-    Renderer() { check(isti_renderer_create(&_r)); }
+    Renderer() { report(isti_renderer_create(&_r), "isti_renderer_create"); }
     ~Renderer() { isti_renderer_destroy(_r); }
     Renderer(const Renderer &) = delete;
     Renderer &operator=(const Renderer &) = delete;
@@ -360,12 +377,23 @@ public:
         fd.aux_curr = n_aux ? _curr.data() : nullptr;
         fd.aux_next = n_aux ? _next.data() : nullptr;
         fd.aux_priority = n_aux ? _prio.data() : nullptr;
-        check(isti_render(_r, render_buffer.ptr(), &info, &fd, stream));
+        if (_r)
+            report(isti_render(_r, render_buffer.ptr(), &info, &fd, stream), "Renderer::render");
+        else
+            report(ISTI_ERR_INVALID_ARG, "Renderer::render", "the renderer was not created");
     }
 
+    // isti_status of the last render (or of the construction, before the first render)
+    isti_status last_status() const { return _status; }
     isti_renderer *handle() { return _r; }
 
 private:
+    void report(isti_status s, const char *what, const char *msg = nullptr)
+    {
+        _status = s;
+        if (s != ISTI_OK)
+            std::cout << "isti | " << what << " failed with error: " << (msg ? msg : isti_last_error()) << std::endl;
+    }
     template <class B>
     static const void *ptr_of(const std::optional<B> &b)
     {
@@ -390,6 +418,7 @@ private:
         return v;
     }
     isti_renderer *_r = nullptr;
+    isti_status _status = ISTI_OK;
     std::vector<isti_view> _curr, _next;
     std::vector<int32_t> _prio;
 };

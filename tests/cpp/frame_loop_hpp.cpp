@@ -118,6 +118,8 @@ int main(int argc, char **argv)
                 if (!in)
                     throw std::runtime_error("case.txt is truncated");
                 renderer.render(render_buffer, info, frame_data);
+                if (renderer.last_status() != ISTI_OK) // printed by render, like the reference
+                    return 1;
                 char name[32];
                 std::snprintf(name, sizeof name, "%04d.png", frame_idx++);
                 render_buffer.writeToFile(out_dir / name);

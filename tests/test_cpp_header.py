@@ -21,9 +21,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(ROOT, "tests", "cpp", "frame_loop_hpp.cpp")
 
 
-def compile_frame_loop(out_dir: str) -> str:
-    exe = os.path.join(out_dir, "frame_loop_hpp")
-    cmd = [_build._nvcc(), "-std=c++20", "-O2", _build.CUDA_ARCH, "-I", _build.INCLUDE, SRC, "-o", exe,
+def compile_program(src: str, out_dir: str) -> str:
+    exe = os.path.join(out_dir, os.path.splitext(os.path.basename(src))[0])
+    cmd = [_build._nvcc(), "-std=c++20", "-O2", _build.CUDA_ARCH, "-I", _build.INCLUDE, src, "-o", exe,
            "-L", _build.LIB_DIR, "-listi", "-Xlinker", "-rpath," + _build.LIB_DIR,
            "-Xcompiler", "-Wall,-Wextra,-Werror"]
     res = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
@@ -33,11 +33,25 @@ def compile_frame_loop(out_dir: str) -> str:
 
 @pytest.fixture(scope="module")
 def frame_loop_exe(built, tmp_path_factory):
-    return compile_frame_loop(str(tmp_path_factory.mktemp("hpp_build")))
+    return compile_program(SRC, str(tmp_path_factory.mktemp("hpp_build")))
 
 
 def test_header_compiles_and_links(frame_loop_exe):
     assert os.access(frame_loop_exe, os.X_OK)
+
+
+def test_header_error_behaviour(built, tmp_path):
+    """Render failures are printed and execution continues (the reference's
+    CUDA_CHECK_THROW); resize to another size and unreadable files throw."""
+    exe = compile_program(os.path.join(ROOT, "tests", "cpp", "errors_hpp.cpp"), str(tmp_path))
+    res = subprocess.run([exe], capture_output=True, text=True, timeout=120, cwd=str(tmp_path))
+    assert res.returncode == 0, res.stdout + res.stderr
+    out = res.stdout
+    assert "isti | Renderer::render failed with error:" in out
+    assert "render status 0" not in out
+    assert "resize threw: Resizing of ImageBuffer currently not supported" in out
+    assert "read threw: Could not load image does_not_exist.png" in out
+    assert "exr read threw: Error loading EXR file does_not_exist.exr" in out
 
 
 def test_header_is_self_contained(tmp_path):
