@@ -65,6 +65,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-per-frame", action="store_true", help="skip the single-frame-call comparison")
     ap.add_argument("--no-quality", action="store_true", help="skip PSNR / SSIM against the analytic ground truth")
+    ap.add_argument("--no-graph-batch", action="store_true", help="skip the mixed-resolution batch under a CUDA graph")
     return ap.parse_args()
 
 
@@ -330,6 +331,11 @@ def main_ours(args):
     if not args.no_e2e:
         e2e = run_e2e(args, seq, res, clients, r, dev, world)
 
+    # ---- the batched mixed-resolution workload under one CUDA graph (reported beside the line)
+    graph_batch = None
+    if not args.no_graph_batch:
+        graph_batch = run_graph_batch(args, dev, rank)
+
     # ---- roofline of the dominant kernel.  Algorithmic bytes per interpolated output pixel
     # (the per-unit figure of the path): every source view's inputs once and the output once,
     # 6 views x (4 z + 6 f16 motion + 4 colour + 12 shadow A/B/Info) + 4 = 160 B.  Split by the
@@ -410,6 +416,7 @@ def main_ours(args):
                                     "splat_kernel": round(per_launch_ms["splat_kernel"], 4),
                                     "reproj_kernel": round(per_launch_ms["reproj_kernel"], 4)},
             "per_frame_api": per_frame,
+            "graph_batch_mixed": graph_batch,
             "gpu_launches": tim["kernel_launches"],
             "clocks": clk,
             "e2e": e2e,
@@ -422,6 +429,92 @@ def main_ours(args):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+GB_RES = ((1280, 720), (1920, 1080), (2064, 2208))
+GB_PAIRS = 16
+GB_EYES = (-0.032, 0.032)  # half the interpupillary distance, metres
+
+
+def run_graph_batch(args, dev, rank):
+    """The batched workload of the benchmark list: 16 keyframe pairs x 3 t values x 2 eyes,
+    the pairs at 1280x720, 1920x1080 and 2064x2208 in turn (6, 5, 5 pairs: 241.7 Mpix per
+    batch), main-camera buffers only (no aux cameras, no shadows), plain method.  Each
+    pair's 6 frames are one isti_render_batch call; the 16 calls are captured once into a
+    CUDA graph, replayed `warmup` times untimed and `steps` times timed (keyframes
+    resident; inputs and intermediates of a replay far larger than L2).  Afterwards one
+    pair per resolution is checked against per-frame isti_render calls."""
+    import numpy as np
+    import torch
+
+    from imagebasedspatiotemporalinterpolation_gb300 import scene
+    from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame, Renderer, render_info
+
+    def eye_client(seq, k, b, offset):
+        t = b / seq.fpa
+        pose = seq.poses[k].lerp(seq.poses[k + 1], t)
+        eye = pose.eye + scene.right_vector(pose.yaw, pose.pitch) * offset
+        vp = seq.proj_main @ scene.view_matrix(eye, pose.yaw, pose.pitch)
+        return scene.Client(seq.width, seq.height, float(np.float32(t)), vp.astype(np.float32),
+                            np.linalg.inv(vp).astype(np.float32), seq.fpa, seq.sfpa, False, 0)
+
+    jobs, first_of_res = [], []
+    for j, (w, h) in enumerate(GB_RES):
+        n_pairs = len(range(j, GB_PAIRS, len(GB_RES)))
+        seq = scene.Sequence(w, h, n_pairs + 1, seed=args.seed + 101 * (j + 1) + rank)
+        first_of_res.append(len(jobs))
+        for k in range(n_pairs):
+            infos = [render_info(eye_client(seq, k, b, e)) for b in TS for e in GB_EYES]
+            jobs.append((w, h, DeviceFrame.from_host(seq.frame(k), dev), infos))
+    mpix = sum(w * h * len(infos) for w, h, _, infos in jobs) / 1e6
+    r = Renderer()
+    stream = torch.cuda.Stream(dev)
+    outs = [[torch.zeros((h, w, 4), dtype=torch.uint8, device=dev) for _ in infos] for w, h, _, infos in jobs]
+    with torch.cuda.stream(stream):
+        for (w, h, frame, infos), o in zip(jobs, outs):   # sizes the arena before the capture
+            r.render_batch(o, infos, frame, chain=False, stream=stream)
+    stream.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        with torch.cuda.graph(graph, stream=stream):
+            for (w, h, frame, infos), o in zip(jobs, outs):
+                r.render_batch(o, infos, frame, chain=False, stream=stream)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            graph.replay()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        stream.synchronize()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for e0, e1 in ev:
+            e0.record(stream)
+            graph.replay()
+            e1.record(stream)
+        t1.record(stream)
+    stream.synchronize()
+    ms = t0.elapsed_time(t1) / args.steps
+    batch_ms = sorted(a.elapsed_time(b) for a, b in ev)
+    # outside the timed region: the replayed frames equal per-frame calls (one pair per resolution)
+    single = Renderer()
+    for idx in first_of_res:
+        w, h, frame, infos = jobs[idx]
+        o = outs[idx]
+        for k, info in enumerate(infos):
+            ref = torch.zeros((h, w, 4), dtype=torch.uint8, device=dev)
+            single.render(ref, info, frame, stream)
+            stream.synchronize()
+            if not torch.equal(ref, o[k]):
+                raise RuntimeError(f"graph batch: {w}x{h} frame {k} differs from the per-frame call")
+    single.close()
+    r.close()
+    return {"value": round(mpix / (ms / 1e3), 2), "unit": "Mpix/s", "mpix_per_batch": round(mpix, 2),
+            "frames_per_batch": sum(len(infos) for _, _, _, infos in jobs), "ms_per_batch": round(ms, 4),
+            "p50_batch_ms": round(batch_ms[len(batch_ms) // 2], 4),
+            "p99_batch_ms": round(batch_ms[min(len(batch_ms) - 1, int(0.99 * len(batch_ms)))], 4),
+            "launches_per_batch": 3 * len(jobs),
+            "workload": "16 pairs x 3 t x 2 eyes at 1280x720 / 1920x1080 / 2064x2208, main camera only, "
+                        "no shadows, mode 0, one CUDA graph per batch"}
 
 
 def run_e2e(args, seq, res, clients, r, dev, world):
