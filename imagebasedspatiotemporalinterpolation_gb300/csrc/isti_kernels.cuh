@@ -40,6 +40,10 @@ namespace isti
 constexpr int MAX_VIEWS = 2 + 2 * ISTI_MAX_AUX_CAMS;
 constexpr int MAX_FRAMES = ISTI_MAX_BATCH_FRAMES;
 constexpr int ROWS = 2; // output rows searched together by one reprojection thread
+// Registers per reprojection thread.  The kernel waits on dependent gathers, so resident
+// warps matter more than registers: at 48 (no spills) a 6-view block of 192 threads
+// fits 7 times into the register file, against 5 times at its natural 62.
+constexpr int REPROJ_MAX_REGS = 48;
 constexpr float FLT_MAX_F = 3.402823466e+38f;
 
 struct DevView
@@ -416,13 +420,22 @@ __device__ uint32_t second_chance(float weight, const ShadowFrames &sf, const Fr
 // ---- bidirectional reprojection, src/renderer.cu:148-465 ----
 
 // One direction of one camera for one output pixel: window init + search + error.
+// 12 bytes in shared memory: the error is never negative, so its sign bit carries
+// visible_in_main.
 struct DirRes
 {
-    float error;  // FLT_MAX when not searched
-    float depth;  // searched depth, else the window-initialisation depth
-    uint32_t src; // source pixel, x << 16 | y
-    uint32_t vis; // visible_in_main
+    float error_vis; // error (FLT_MAX when not searched); sign bit = visible_in_main
+    float depth;     // searched depth, else the window-initialisation depth
+    uint32_t src;    // source pixel, x << 16 | y
 };
+
+// (a NaN error loses its sign, which no comparison sees)
+__device__ __forceinline__ float pack_error_vis(float error, bool vis)
+{
+    return __uint_as_float((__float_as_uint(error) & 0x7fffffffu) | (vis ? 0x80000000u : 0u));
+}
+__device__ __forceinline__ float dir_error(const DirRes &d) { return __uint_as_float(__float_as_uint(d.error_vis) & 0x7fffffffu); }
+__device__ __forceinline__ bool dir_vis(const DirRes &d) { return (__float_as_uint(d.error_vis) >> 31) != 0u; }
 
 // Result of bidirectionalReprojection for one camera (src/renderer.cu:366-397), without its colour.
 struct CamRes
@@ -463,26 +476,28 @@ __device__ __forceinline__ CamRes cam_result(const DirRes &f, const DirRes &b, c
     r.depth = 0.0f;
     r.dir = 0;
     r.src = 0;
-    if (f.error < eps1 || b.error < eps1)
+    const float fe = dir_error(f), be = dir_error(b);
+    const bool fvis = dir_vis(f), bvis = dir_vis(b);
+    if (fe < eps1 || be < eps1)
     {
-        const bool both = f.error < eps1 && b.error < eps1;
+        const bool both = fe < eps1 && be < eps1;
         const bool similar = fabsf(__fsub_rn(depth_to_z(f.depth), depth_to_z(b.depth))) < eps2;
-        const bool choose_fwd = (both && !similar && f.depth < b.depth) || ((!both || similar) && f.error < b.error);
+        const bool choose_fwd = (both && !similar && f.depth < b.depth) || ((!both || similar) && fe < be);
         r.valid = true;
         if (choose_fwd)
         {
-            r.vis = f.vis || (both && similar && b.vis);
+            r.vis = fvis || (both && similar && bvis);
             r.priority = vf.priority;
-            r.error = f.error;
+            r.error = fe;
             r.depth = f.depth;
             r.dir = 0;
             r.src = f.src;
         }
         else
         {
-            r.vis = b.vis || (both && similar && f.vis);
+            r.vis = bvis || (both && similar && fvis);
             r.priority = vb.priority;
-            r.error = b.error;
+            r.error = be;
             r.depth = b.depth;
             r.dir = 1;
             r.src = b.src;
@@ -609,7 +624,7 @@ __device__ __forceinline__ unsigned long long window_key(const unsigned long lon
 // bidirectionalReprojection_kernel<SW, SI, MAIN_ALWAYS_VALID>, src/renderer.cu:400-465
 // block = (32, n_views): output rows ROWS * blockIdx.y + {0, 1}, 32 pixels each, one warp per source view.
 template <int SW, int SI, bool MAV>
-__global__ void __launch_bounds__(32 * MAX_VIEWS) reproj_kernel(const __grid_constant__ FrameParams p, const __grid_constant__ KeyMaps km)
+__global__ void __maxnreg__(REPROJ_MAX_REGS) reproj_kernel(const __grid_constant__ FrameParams p, const __grid_constant__ KeyMaps km)
 {
     using T = Tile<SW>;
     // dynamic shared memory only (no static __shared__ in front of it): the key tiles start at
@@ -752,16 +767,14 @@ __global__ void __launch_bounds__(32 * MAX_VIEWS) reproj_kernel(const __grid_con
                 for (int r = 0; r < ROWS; r++)
                 {
                     DirRes d;
-                    d.error = FLT_MAX_F;
+                    d.error_vis = FLT_MAX_F;
                     d.depth = d_init[r];
-                    d.vis = 0;
                     if (s[r])
                     {
                         d.depth = z_to_depth(__fadd_rn(zz[r], m[r].z));
                         const float ex = __fmul_rn(__fsub_rn(__fadd_rn(fx[r], m[r].x), pcx), v.err_sx);
                         const float ey = __fmul_rn(__fsub_rn(__fadd_rn(fy[r], m[r].y), pcy[r]), v.err_sy);
-                        d.error = __fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)));
-                        d.vis = m[r].w > 0.0f;
+                        d.error_vis = pack_error_vis(__fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey))), m[r].w > 0.0f);
                     }
                     d.src = (ax[r] << 16) | ay[r];
                     res[((k * ROWS + r) * nv + vw) * 32 + lane] = d;

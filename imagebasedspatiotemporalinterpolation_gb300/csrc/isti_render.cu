@@ -302,15 +302,44 @@ bool make_key_maps(const isti::FrameParams &p, isti::KeyMaps &km)
     return true;
 }
 
-constexpr size_t SMEM_LIMIT = 200 * 1024;
+// Shared memory per SM and reserved per block of device `dev` (cached).
+struct SmemInfo
+{
+    int per_sm = 0, reserved = 0;
+};
+SmemInfo smem_info(int dev)
+{
+    static std::mutex m;
+    static SmemInfo cache[64];
+    std::lock_guard<std::mutex> lock(m);
+    SmemInfo &s = cache[dev & 63];
+    if (s.per_sm == 0)
+    {
+        if (cudaDeviceGetAttribute(&s.per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&s.reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess)
+            s = SmemInfo{228 * 1024, 1024};
+    }
+    return s;
+}
 
 template <int SW, int SI, bool MAV>
 cudaError_t launch_reproj(isti::FrameParams &p, cudaStream_t stream)
 {
     using T = isti::Tile<SW>;
-    // key tiles of as many frames as fit beside the per-frame results
+    // Key tiles of as many frames per TMA round as fit beside the per-frame results without
+    // costing a resident block: the register budget allows `blocks` blocks per SM, and the
+    // shared memory of one block is kept within 1 / blocks of the SM's (at least one frame).
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    const SmemInfo si = smem_info(dev);
+    const int threads = 32 * p.n_views;
+    int blocks = 65536 / (isti::REPROJ_MAX_REGS * threads);
+    blocks = blocks < 1 ? 1 : (blocks > 32 ? 32 : blocks);
+    const size_t budget = (size_t)si.per_sm / (size_t)blocks - (size_t)si.reserved;
     const size_t res_bytes = isti::reproj_smem<SW>(p.n_views, p.n_frames, 0);
-    int fg = (int)((SMEM_LIMIT - res_bytes) / ((size_t)p.n_views * T::BYTES));
+    int fg = budget > res_bytes ? (int)((budget - res_bytes) / ((size_t)p.n_views * T::BYTES)) : 1;
     fg = fg < 1 ? 1 : (fg > p.n_frames ? p.n_frames : fg);
     p.frames_per_group = fg;
     static thread_local isti::KeyMaps km; // 2 KiB, passed by value as a kernel parameter
@@ -323,10 +352,6 @@ cudaError_t launch_reproj(isti::FrameParams &p, cudaStream_t stream)
     static int attr_set[64] = {}; // per device
     if (smem > 48 * 1024)
     {
-        int dev = 0;
-        cudaError_t e = cudaGetDevice(&dev);
-        if (e != cudaSuccess)
-            return e;
         std::lock_guard<std::mutex> lock(attr_mutex);
         int &cur = attr_set[dev & 63];
         if ((int)smem > cur)
