@@ -40,10 +40,17 @@ namespace isti
 constexpr int MAX_VIEWS = 2 + 2 * ISTI_MAX_AUX_CAMS;
 constexpr int MAX_FRAMES = ISTI_MAX_BATCH_FRAMES;
 constexpr int ROWS = 2; // output rows searched together by one reprojection thread
-// Registers per reprojection thread.  The kernel waits on dependent gathers, so resident
-// warps matter more than registers: at 48 (no spills) a 6-view block of 192 threads
-// fits 7 times into the register file, against 5 times at its natural 62.
-constexpr int REPROJ_MAX_REGS = 48;
+// Registers per reprojection thread (the kernel's register cap, a template argument).
+// The kernel waits on dependent gathers, so resident warps matter more than registers:
+// at 48 (no spills) a 6-view block of 192 threads fits 7 times into the register file
+// (5 times at its natural 62), at 40 (a few spilled words) 8 times.  Measured at 1080p,
+// 3 frames: for the 3x3 window 40 is faster with 4 or more views (4 views 0.441 -> 0.425
+// ms, 6 views 0.590 -> 0.564 ms) and 48 with 2 (0.240 -> 0.239 ms, 56: 0.252); the 7x7
+// window (mode 1) spills more and runs best at 56 (6 views: 40 1.203, 48 1.164, 56 1.153 ms).
+constexpr int REPROJ_REGS = 48;
+constexpr int REPROJ_REGS_MANY_VIEWS = 40;
+constexpr int REPROJ_MANY_VIEWS = 4;
+constexpr int REPROJ_REGS_WIDE_WINDOW = 56;
 constexpr float FLT_MAX_F = 3.402823466e+38f;
 
 struct DevView
@@ -211,7 +218,9 @@ __global__ void __launch_bounds__(256) init_kernel(const __grid_constant__ Frame
 
 // ---- computeFlowFields_sortedSplatting_kernel, src/renderer.cu:76-146 ----
 
-__global__ void __launch_bounds__(256) splat_kernel(const __grid_constant__ FrameParams p)
+// 8 blocks of 256 threads per SM (32 registers, a few spilled words): 64 resident warps
+// instead of 56 at the natural 36 registers, 3-8 % faster (1080p, 3 frames, 2-6 views).
+__global__ void __launch_bounds__(256, 8) splat_kernel(const __grid_constant__ FrameParams p)
 {
     const DevView &v = p.v[blockIdx.z];
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -623,8 +632,8 @@ __device__ __forceinline__ unsigned long long window_key(const unsigned long lon
 
 // bidirectionalReprojection_kernel<SW, SI, MAIN_ALWAYS_VALID>, src/renderer.cu:400-465
 // block = (32, n_views): output rows ROWS * blockIdx.y + {0, 1}, 32 pixels each, one warp per source view.
-template <int SW, int SI, bool MAV>
-__global__ void __maxnreg__(REPROJ_MAX_REGS) reproj_kernel(const __grid_constant__ FrameParams p, const __grid_constant__ KeyMaps km)
+template <int SW, int SI, bool MAV, int REGS>
+__global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FrameParams p, const __grid_constant__ KeyMaps km)
 {
     using T = Tile<SW>;
     // dynamic shared memory only (no static __shared__ in front of it): the key tiles start at
@@ -980,17 +989,21 @@ __global__ void rgb8_to_rgba8_kernel(uint32_t *__restrict__ dst, const uint8_t *
 {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const size_t groups = VEC ? n / 4 : 0;
-    const uint32_t *s32 = reinterpret_cast<const uint32_t *>(src);
-    for (size_t g = t; g < groups; g += stride)
+    size_t groups = 0;
+    if constexpr (VEC)
     {
-        const uint32_t w0 = __ldg(s32 + 3 * g), w1 = __ldg(s32 + 3 * g + 1), w2 = __ldg(s32 + 3 * g + 2);
-        uint4 o;
-        o.x = (w0 & 0xffffffu) | 0xff000000u;
-        o.y = (w0 >> 24) | ((w1 & 0xffffu) << 8) | 0xff000000u;
-        o.z = (w1 >> 16) | ((w2 & 0xffu) << 16) | 0xff000000u;
-        o.w = (w2 >> 8) | 0xff000000u;
-        reinterpret_cast<uint4 *>(dst)[g] = o;
+        groups = n / 4;
+        const uint32_t *s32 = reinterpret_cast<const uint32_t *>(src);
+        for (size_t g = t; g < groups; g += stride)
+        {
+            const uint32_t w0 = __ldg(s32 + 3 * g), w1 = __ldg(s32 + 3 * g + 1), w2 = __ldg(s32 + 3 * g + 2);
+            uint4 o;
+            o.x = (w0 & 0xffffffu) | 0xff000000u;
+            o.y = (w0 >> 24) | ((w1 & 0xffffu) << 8) | 0xff000000u;
+            o.z = (w1 >> 16) | ((w2 & 0xffu) << 16) | 0xff000000u;
+            o.w = (w2 >> 8) | 0xff000000u;
+            reinterpret_cast<uint4 *>(dst)[g] = o;
+        }
     }
     for (size_t i = groups * 4 + t; i < n; i += stride)
         dst[i] = (uint32_t)__ldg(src + 3 * i) | (uint32_t)__ldg(src + 3 * i + 1) << 8 | (uint32_t)__ldg(src + 3 * i + 2) << 16 | 0xff000000u;

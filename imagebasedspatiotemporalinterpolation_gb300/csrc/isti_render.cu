@@ -322,21 +322,22 @@ SmemInfo smem_info(int dev)
     return s;
 }
 
-template <int SW, int SI, bool MAV>
-cudaError_t launch_reproj(isti::FrameParams &p, cudaStream_t stream)
+template <int SW, int SI, bool MAV, int REGS>
+cudaError_t launch_reproj_regs(isti::FrameParams &p, cudaStream_t stream)
 {
     using T = isti::Tile<SW>;
     // Key tiles of as many frames per TMA round as fit beside the per-frame results without
-    // costing a resident block: the register budget allows `blocks` blocks per SM, and the
-    // shared memory of one block is kept within 1 / blocks of the SM's (at least one frame).
+    // costing a resident block: the register budget allows `blocks` blocks per SM (at most
+    // 64 warps and 32 blocks), and the shared memory of one block is kept within 1 / blocks
+    // of the SM's (at least one frame).
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess)
         return e;
     const SmemInfo si = smem_info(dev);
     const int threads = 32 * p.n_views;
-    int blocks = 65536 / (isti::REPROJ_MAX_REGS * threads);
-    blocks = blocks < 1 ? 1 : (blocks > 32 ? 32 : blocks);
+    int blocks = std::min(65536 / (REGS * threads), std::min(64 / p.n_views, 32));
+    blocks = blocks < 1 ? 1 : blocks;
     const size_t budget = (size_t)si.per_sm / (size_t)blocks - (size_t)si.reserved;
     const size_t res_bytes = isti::reproj_smem<SW>(p.n_views, p.n_frames, 0);
     int fg = budget > res_bytes ? (int)((budget - res_bytes) / ((size_t)p.n_views * T::BYTES)) : 1;
@@ -356,15 +357,28 @@ cudaError_t launch_reproj(isti::FrameParams &p, cudaStream_t stream)
         int &cur = attr_set[dev & 63];
         if ((int)smem > cur)
         {
-            e = cudaFuncSetAttribute(isti::reproj_kernel<SW, SI, MAV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            e = cudaFuncSetAttribute(isti::reproj_kernel<SW, SI, MAV, REGS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess)
                 return e;
             cur = (int)smem;
         }
     }
     const dim3 gr((p.out_w + 31) / 32, (p.out_h + isti::ROWS - 1) / isti::ROWS);
-    isti::reproj_kernel<SW, SI, MAV><<<gr, dim3(32, p.n_views), smem, stream>>>(p, km);
+    isti::reproj_kernel<SW, SI, MAV, REGS><<<gr, dim3(32, p.n_views), smem, stream>>>(p, km);
     return cudaGetLastError();
+}
+
+template <int SW, int SI, bool MAV>
+cudaError_t launch_reproj(isti::FrameParams &p, cudaStream_t stream)
+{
+    if constexpr (SW == 1)
+    {
+        if (p.n_views >= isti::REPROJ_MANY_VIEWS)
+            return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS_MANY_VIEWS>(p, stream);
+        return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS>(p, stream);
+    }
+    else
+        return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS_WIDE_WINDOW>(p, stream);
 }
 
 // Enqueues the three kernels of one batch; events (optional) are recorded after init and splat.
