@@ -473,6 +473,17 @@ struct Tile
 
 __device__ __forceinline__ int tile_x0(uint32_t tx0, int sw) { return ((int)tx0 - sw) & ~1; }
 
+// Bytes at the start of a reprojection block's shared memory: the key tiles of one frame
+// group in phase 1, then (the tiles are dead by then) the chained colours and flags of
+// phases 2-3.  A multiple of 128, so the results that follow stay aligned.
+template <int SW>
+__host__ __device__ constexpr size_t reproj_tile_region(int n_views, int n_frames, int frames_per_group)
+{
+    const size_t tiles = (size_t)frames_per_group * n_views * Tile<SW>::BYTES;
+    const size_t chain = (size_t)n_frames * ROWS * 32 * sizeof(uint32_t) * 2;
+    return tiles > chain ? tiles : chain;
+}
+
 __device__ __forceinline__ CamRes cam_result(const DirRes &f, const DirRes &b, const DevView &vf, const DevView &vb, float eps1, float eps2,
                                              bool always_valid)
 {
@@ -640,11 +651,12 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
     // the 1 KiB-aligned window base, so every TMA destination is 128-byte aligned
     extern __shared__ __align__(1024) unsigned char smem[];
     const int nv = p.n_views, nf = p.n_frames, fg = p.frames_per_group;
+    // [key tiles, phase 1 | chained colours and flags, phases 2-3 (same bytes)][results][barrier]
     unsigned long long *tiles = reinterpret_cast<unsigned long long *>(smem);                 // [fg][nv][H][W]
-    DirRes *res = reinterpret_cast<DirRes *>(smem + (size_t)fg * nv * T::BYTES);             // [nf][ROWS][nv][32]
-    uint32_t *cols = reinterpret_cast<uint32_t *>(res + nf * ROWS * nv * 32);                 // [nf][ROWS][32]
+    uint32_t *cols = reinterpret_cast<uint32_t *>(smem);                                      // [nf][ROWS][32]
     uint32_t *valid = cols + nf * ROWS * 32;                                                 // [nf][ROWS][32]
-    unsigned long long &bar = *reinterpret_cast<unsigned long long *>(valid + nf * ROWS * 32); // TMA completion barrier
+    DirRes *res = reinterpret_cast<DirRes *>(smem + reproj_tile_region<SW>(nv, nf, fg));     // [nf][ROWS][nv][32]
+    unsigned long long &bar = *reinterpret_cast<unsigned long long *>(res + nf * ROWS * nv * 32); // TMA completion barrier
 
     const int lane = threadIdx.x, vw = threadIdx.y;
     const uint32_t x0 = blockIdx.x * 32, x = x0 + lane, y0 = blockIdx.y * ROWS;
@@ -1013,7 +1025,7 @@ __global__ void rgb8_to_rgba8_kernel(uint32_t *__restrict__ dst, const uint8_t *
 template <int SW>
 constexpr size_t reproj_smem(int n_views, int n_frames, int frames_per_group)
 {
-    return (size_t)frames_per_group * n_views * Tile<SW>::BYTES +
-           (size_t)n_frames * ROWS * (n_views * 32 * sizeof(DirRes) + 2 * 32 * sizeof(uint32_t)) + 16; // + mbarrier
+    return reproj_tile_region<SW>(n_views, n_frames, frames_per_group) + (size_t)n_frames * ROWS * n_views * 32 * sizeof(DirRes) +
+           16; // + mbarrier
 }
 } // namespace isti

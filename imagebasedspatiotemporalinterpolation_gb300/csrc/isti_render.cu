@@ -302,46 +302,17 @@ bool make_key_maps(const isti::FrameParams &p, isti::KeyMaps &km)
     return true;
 }
 
-// Shared memory per SM and reserved per block of device `dev` (cached).
-struct SmemInfo
-{
-    int per_sm = 0, reserved = 0;
-};
-SmemInfo smem_info(int dev)
-{
-    static std::mutex m;
-    static SmemInfo cache[64];
-    std::lock_guard<std::mutex> lock(m);
-    SmemInfo &s = cache[dev & 63];
-    if (s.per_sm == 0)
-    {
-        if (cudaDeviceGetAttribute(&s.per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&s.reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess)
-            s = SmemInfo{228 * 1024, 1024};
-    }
-    return s;
-}
-
 template <int SW, int SI, bool MAV, int REGS>
 cudaError_t launch_reproj_regs(isti::FrameParams &p, cudaStream_t stream)
 {
-    using T = isti::Tile<SW>;
-    // Key tiles of as many frames per TMA round as fit beside the per-frame results without
-    // costing a resident block: the register budget allows `blocks` blocks per SM (at most
-    // 64 warps and 32 blocks), and the shared memory of one block is kept within 1 / blocks
-    // of the SM's (at least one frame).
+    // One frame's key tiles per TMA round: the least shared memory per block, so the most
+    // resident blocks and the largest L1 (1080p, 6 views, 3 frames, 8 blocks per SM: one
+    // frame per round 0.569 ms, two 0.581 ms; at 7 blocks two frames 0.590, three 0.594).
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess)
         return e;
-    const SmemInfo si = smem_info(dev);
-    const int threads = 32 * p.n_views;
-    int blocks = std::min(65536 / (REGS * threads), std::min(64 / p.n_views, 32));
-    blocks = blocks < 1 ? 1 : blocks;
-    const size_t budget = (size_t)si.per_sm / (size_t)blocks - (size_t)si.reserved;
-    const size_t res_bytes = isti::reproj_smem<SW>(p.n_views, p.n_frames, 0);
-    int fg = budget > res_bytes ? (int)((budget - res_bytes) / ((size_t)p.n_views * T::BYTES)) : 1;
-    fg = fg < 1 ? 1 : (fg > p.n_frames ? p.n_frames : fg);
+    const int fg = 1;
     p.frames_per_group = fg;
     static thread_local isti::KeyMaps km; // 2 KiB, passed by value as a kernel parameter
     p.use_tma = make_key_maps<SW>(p, km) ? 1 : 0;
