@@ -228,8 +228,11 @@ struct isti_dataset
         const size_t n_threads = std::min<size_t>(jobs.size(), std::min(hw, 16u));
         std::atomic<size_t> next_job{0};
         auto worker = [&]() {
+            // the files are decoded side by side: one thread per file (restored for the caller's thread)
+            isti::set_decode_threads(n_threads > 1 ? 1 : 0);
             for (size_t k; (k = next_job.fetch_add(1)) < jobs.size();)
                 decode(jobs[k]);
+            isti::set_decode_threads(0);
         };
         std::vector<std::thread> threads;
         for (size_t t = 1; t < n_threads; t++)

@@ -13,16 +13,30 @@
 #include "isti_error.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace
 {
 using isti::set_error;
+
+thread_local int t_decode_threads = 0;
+
+// Threads for a decode of `units` independent pieces: one per 4 pieces, at most 8 and
+// the hardware's, unless the caller set a budget (isti::set_decode_threads).
+int decode_threads(int units)
+{
+    int n = t_decode_threads;
+    if (n <= 0)
+        n = std::min<int>(8, std::max(1u, std::thread::hardware_concurrency()));
+    return std::max(1, std::min(n, units / 4));
+}
 
 // ------------------------------------------------------------------ files
 
@@ -187,6 +201,17 @@ struct BitReader
 
     void refill()
     {
+        if (end - p >= 8) // whole bytes up to 56..63 buffered bits, from one 8-byte load
+        {
+            uint64_t v = 0;
+            for (int k = 0; k < 8; k++) // little-endian assembly (the compiler folds it to one load)
+                v |= uint64_t(p[k]) << (8 * k);
+            const int take = (63 - cnt) >> 3; // 1..7 bytes: the bits above cnt stay zero
+            buf |= (v & ((uint64_t(1) << (8 * take)) - 1)) << cnt;
+            p += take;
+            cnt += take * 8;
+            return;
+        }
         while (cnt <= 56)
         {
             uint64_t byte = 0;
@@ -399,8 +424,18 @@ bool inflate(const uint8_t *src, size_t n, std::vector<uint8_t> &out, size_t max
                     o[k] = from[k];
             }
             else
-                for (uint32_t k = 0; k < len; k++)
+            {
+                // a pattern of period d < 8: copy the first bytes one at a time, then 8-byte
+                // chunks from a multiple of d back (>= 8), which repeats the same pattern
+                const uint32_t d8 = d * ((8 + d - 1) / d);
+                uint32_t k = 0;
+                for (; k < len && k < d8; k++)
                     o[k] = from[k];
+                for (; k + 8 <= len; k += 8)
+                    std::memcpy(o + k, o + k - d8, 8);
+                for (; k < len; k++)
+                    o[k] = o[k - d];
+            }
             pos += len;
         }
         if (b.overrun())
@@ -598,20 +633,23 @@ bool png_unfilter(uint8_t *data, uint32_t rows, size_t row_bytes, int bpp, std::
                 r[i] = uint8_t(r[i] + prior[i]);
             break;
         case 3:
-            for (size_t i = 0; i < row_bytes; i++)
-            {
-                const int left = i >= size_t(bpp) ? r[i - bpp] : 0;
-                r[i] = uint8_t(r[i] + ((left + prior[i]) >> 1));
-            }
+        {
+            const size_t first = std::min(size_t(bpp), row_bytes); // no left neighbour
+            for (size_t i = 0; i < first; i++)
+                r[i] = uint8_t(r[i] + (prior[i] >> 1));
+            for (size_t i = first; i < row_bytes; i++)
+                r[i] = uint8_t(r[i] + ((int(r[i - bpp]) + prior[i]) >> 1));
             break;
+        }
         case 4:
-            for (size_t i = 0; i < row_bytes; i++)
-            {
-                const int left = i >= size_t(bpp) ? r[i - bpp] : 0;
-                const int upleft = i >= size_t(bpp) ? prior[i - bpp] : 0;
-                r[i] = uint8_t(r[i] + paeth(left, prior[i], upleft));
-            }
+        {
+            const size_t first = std::min(size_t(bpp), row_bytes); // paeth(0, up, 0) = up
+            for (size_t i = 0; i < first; i++)
+                r[i] = uint8_t(r[i] + prior[i]);
+            for (size_t i = first; i < row_bytes; i++)
+                r[i] = uint8_t(r[i] + paeth(r[i - bpp], prior[i], prior[i - bpp]));
             break;
+        }
         default: return err = "png: bad filter type", false;
         }
         prior = r;
@@ -1530,7 +1568,20 @@ bool exr_decode(const uint8_t *d, size_t n, int &width, int &height, int &channe
     if (!grey && sel[3] < 0)
         for (size_t i = 0; i < size_t(w) * h; i++)
             result[4 * i + 3] = 1.0f;
-    std::vector<uint8_t> block, tmp;
+
+    // chunk table first (in file order, the first bad entry is the error), then the chunks,
+    // on several threads when there are many and no two chunks claim the same lines
+    struct Chunk
+    {
+        const uint8_t *src;
+        uint32_t size;
+        int64_t row0;
+        int lines;
+    };
+    const size_t nb = size_t(n_blocks);
+    std::vector<Chunk> chunks(nb);
+    std::vector<uint8_t> claimed(nb, 0);
+    bool unique = true;
     for (int bi = 0; bi < n_blocks; bi++)
     {
         const uint64_t off = le64(d + pos + 8 * size_t(bi));
@@ -1543,38 +1594,49 @@ bool exr_decode(const uint8_t *d, size_t n, int &width, int &height, int &channe
         const int64_t row0 = int64_t(y) - box[1];
         if (row0 < 0 || row0 >= h || row0 % lines_per_block != 0)
             return err = "exr: bad chunk line number", false;
-        const int lines = int(std::min<int64_t>(lines_per_block, h - row0));
+        uint8_t &c = claimed[size_t(row0 / lines_per_block)];
+        unique = unique && !c;
+        c = 1;
+        chunks[size_t(bi)] = Chunk{d + off + 8, size, row0, int(std::min<int64_t>(lines_per_block, h - row0))};
+    }
+    std::vector<std::string> errors(nb);
+    auto decode_chunk = [&](int bi, std::vector<uint8_t> &block, std::vector<uint8_t> &tmp) -> bool {
+        const Chunk &ck = chunks[size_t(bi)];
+        std::string &e = errors[size_t(bi)];
+        const int lines = ck.lines;
         const size_t raw = line_bytes * size_t(lines);
-        const uint8_t *src = d + off + 8;
+        const uint8_t *src = ck.src;
+        const uint32_t size = ck.size;
         block.resize(raw);
         if (size == raw || compression == 0)
         {
             if (size != raw)
-                return err = "exr: uncompressed chunk has the wrong size", false;
+                return e = "exr: uncompressed chunk has the wrong size", false;
             std::memcpy(block.data(), src, raw);
         }
         else if (compression == 1)
         {
             tmp.resize(raw);
             if (!exr_unrle(src, size, tmp.data(), raw))
-                return err = "exr: corrupt RLE chunk", false;
+                return e = "exr: corrupt RLE chunk", false;
             exr_unpredict(tmp, block.data());
         }
         else if (compression == 4)
         {
             if (!piz::decompress(src, size, piz_words, w, lines, block.data()))
-                return err = "exr: corrupt PIZ chunk", false;
+                return e = "exr: corrupt PIZ chunk", false;
         }
         else
         {
             tmp.clear();
             tmp.reserve(raw);
-            if (!zlib_decompress(src, size, tmp, raw, err))
-                return err = "exr: " + err, false;
+            if (!zlib_decompress(src, size, tmp, raw, e))
+                return e = "exr: " + e, false;
             if (tmp.size() != raw)
-                return err = "exr: ZIP chunk has the wrong size", false;
+                return e = "exr: ZIP chunk has the wrong size", false;
             exr_unpredict(tmp, block.data());
         }
+        const int64_t row0 = ck.row0;
         for (int l = 0; l < lines; l++)
         {
             const uint8_t *line = block.data() + size_t(l) * line_bytes;
@@ -1596,7 +1658,27 @@ bool exr_decode(const uint8_t *d, size_t n, int &width, int &height, int &channe
                 }
             }
         }
-    }
+        return true;
+    };
+    const int n_threads = unique ? decode_threads(n_blocks) : 1;
+    std::atomic<int> next{0};
+    std::atomic<bool> failed{false};
+    auto worker = [&]() {
+        std::vector<uint8_t> block, tmp;
+        for (int bi; !failed.load(std::memory_order_relaxed) && (bi = next.fetch_add(1)) < n_blocks;)
+            if (!decode_chunk(bi, block, tmp))
+                failed = true;
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < n_threads; t++)
+        pool.emplace_back(worker);
+    worker();
+    for (std::thread &t : pool)
+        t.join();
+    if (failed)
+        for (const std::string &e : errors) // the first failing chunk in file order
+            if (!e.empty())
+                return err = e, false;
     width = w;
     height = h;
     status = ISTI_OK;
@@ -1827,3 +1909,5 @@ isti_status isti_exr_encode_file(const char *path, int32_t width, int32_t height
 void isti_image_free(void *p) { std::free(p); }
 
 } // extern "C"
+
+void isti::set_decode_threads(int n) { t_decode_threads = n; }
