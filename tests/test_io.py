@@ -80,6 +80,14 @@ def test_codecs_against_live_reference(built, tmp_path):
     cases = {"few": rng.integers(0, 5, (4, 77, 101)).astype(np.float32) * 0.25,
              "ramp": np.stack([xx * 0.01 + yy, yy * 0.5 - xx, np.sin(xx * 0.1) * yy, xx * yy]),
              "wide": rng.integers(0, 1 << 32, (4, 77, 101), dtype=np.uint64).astype(np.uint32).view(np.float32)}
+    # many chunks (decoded on several threads), every compression
+    tall = (rng.standard_normal((4, 300, 61)) * 9).astype(np.float32)
+    tall[:, ::5] = 0.25
+    for comp in (0, 1, 2, 3, 4):
+        for pt in (1, 2):
+            p = str(tmp_path / f"tall{comp}{pt}.exr")
+            ref_io.exr_save(p, tall, ["A", "B", "G", "R"], pt, comp)
+            assert (_bits(files.read_exr(p)) == _bits(ref_io.exr_load(p))).all(), (comp, pt)
     for name, planes in cases.items():
         planes = np.nan_to_num(planes, nan=1.0, posinf=2.0, neginf=-2.0)
         for pt in (1, 2):
@@ -115,6 +123,23 @@ def test_exr_encoder_round_trip(built, tmp_path):
         assert (_bits(files.read_exr(p)) == _bits(img)).all()
         files.write_exr(p, img[..., 0], zip_c)
         assert (_bits(files.read_exr(p)) == _bits(img[..., 0])).all()
+
+
+def test_exr_many_chunks_decode_in_parallel(built, tmp_path):
+    """Images with many chunks are decoded on several threads: same bits as written, and a
+    damaged chunk still fails cleanly."""
+    rng = np.random.default_rng(12)
+    img = (rng.standard_normal((701, 257, 4)) * 100).astype(np.float32)
+    img[::7] = 0.5  # some compressible rows
+    for zip_c in (False, True):  # 701 one-line chunks, 44 sixteen-line chunks
+        p = str(tmp_path / f"big{zip_c}.exr")
+        files.write_exr(p, img, zip_c)
+        assert (_bits(files.read_exr(p)) == _bits(img)).all()
+    data = bytearray(open(str(tmp_path / "bigTrue.exr"), "rb").read())
+    for k in range(len(data) // 3, len(data) // 3 + 64):  # garble the middle of the chunk data
+        data[k] ^= 0x5a
+    with pytest.raises(native.IstiError):
+        files.decode_exr(bytes(data))
 
 
 def test_zlib_streams(built):
