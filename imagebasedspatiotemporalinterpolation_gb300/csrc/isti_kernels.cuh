@@ -278,10 +278,10 @@ __global__ void __launch_bounds__(256, 8) splat_kernel(const __grid_constant__ F
 // ---- colour: colorFromShadow / secondChanceAndBlend_kernel, src/renderer.cu:217-327 ----
 
 // The colour inputs of one source pixel of one view: colour and, when soft shadows apply,
-// shadow info and the shadow colours A/B, fetched together (one round of loads; A/B are
-// fetched even when the levels end up not needing them) and the pixel's shadow levels
-// (min / max over the shadow sub-frames and the initial level) computed once for every
-// level index asked for.  Reads outside the view are zero (border addressing).
+// shadow info, then the shadow colours A/B where the levels need them, and the pixel's
+// shadow levels (min / max over the shadow sub-frames and the initial level) computed
+// once for every level index asked for.  Reads outside the view are zero (border
+// addressing).
 struct PixelShade
 {
     uint32_t color, sha, shb;
@@ -298,26 +298,27 @@ __device__ __forceinline__ PixelShade load_shade(const V &v, uint32_t px, uint32
     const uint32_t idx = py * v.w + px;
     s.color = in ? __ldg(v.color + idx) : 0u;
     s.sha = s.shb = 0u;
-    uint32_t si = 0u;
-    if (shadows && in)
-    {
-        si = __ldg(v.shi + idx);
-        s.sha = __ldg(v.sha + idx);
-        if (v.shb != nullptr)
-            s.shb = __ldg(v.shb + idx);
-    }
+    const uint32_t si = (shadows && in) ? __ldg(v.shi + idx) : 0u;
     s.bf = ((si & 255u) << 16) | (((si >> 8) & 255u) << 8) | ((si >> 16) & 255u);
     s.levels = shadows && v.shb != nullptr && s.bf != 0;
     s.init = (int32_t)(s.bf & SOFTSHADOW_VAL_MASK);
     s.mn = (int32_t)SOFTSHADOW_VAL_MASK;
     s.mx = 0;
     if (s.levels)
+    {
         for (int32_t i = 0; i < sfpa; i++)
         {
             const int32_t lv = (int32_t)((s.bf >> (SOFTSHADOW_BITS * (uint32_t)i)) & SOFTSHADOW_VAL_MASK);
             s.mn = min(s.mn, lv);
             s.mx = max(s.mx, lv);
         }
+        // colour A / B are read only where a level differs from the initial one
+        // (colorFromShadow uses the pixel's own colour otherwise)
+        if (s.mn != s.init)
+            s.sha = __ldg(v.sha + idx);
+        if (s.mx != s.init)
+            s.shb = __ldg(v.shb + idx);
+    }
     return s;
 }
 
