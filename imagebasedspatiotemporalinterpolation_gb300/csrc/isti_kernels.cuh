@@ -99,7 +99,7 @@ struct FrameParams
     uint32_t out_w, out_h;
     int32_t n_views, n_aux, n_frames, linear, chain;
     int32_t use_tma;          // key tiles fetched by TMA (every view's row pitch a multiple of 16 bytes)
-    int32_t frames_per_group; // frames whose key tiles are resident in shared memory together
+    int32_t row_pairs;        // pairs of output rows per reprojection block
 };
 
 // One 3-D tensor map per source view over its splat keys: (x, y, frame), u64 elements.
@@ -474,14 +474,15 @@ struct Tile
 
 __device__ __forceinline__ int tile_x0(uint32_t tx0, int sw) { return ((int)tx0 - sw) & ~1; }
 
-// Bytes at the start of a reprojection block's shared memory: the key tiles of one frame
-// group in phase 1, then (the tiles are dead by then) the chained colours and flags of
-// phases 2-3.  A multiple of 128, so the results that follow stay aligned.
+// A reprojection block works through units = (frame, pair of output rows): n_frames x
+// row_pairs of them.  Bytes at the start of its shared memory: the key tiles of one unit
+// (every view) in phase 1, then (the tiles are dead by then) the chained colours and flags
+// of phases 2-3.  A multiple of 128, so the results that follow stay aligned.
 template <int SW>
-__host__ __device__ constexpr size_t reproj_tile_region(int n_views, int n_frames, int frames_per_group)
+__host__ __device__ constexpr size_t reproj_tile_region(int n_views, int n_units)
 {
-    const size_t tiles = (size_t)frames_per_group * n_views * Tile<SW>::BYTES;
-    const size_t chain = (size_t)n_frames * ROWS * 32 * sizeof(uint32_t) * 2;
+    const size_t tiles = (size_t)n_views * Tile<SW>::BYTES;
+    const size_t chain = (size_t)n_units * ROWS * 32 * sizeof(uint32_t) * 2;
     return tiles > chain ? tiles : chain;
 }
 
@@ -643,7 +644,10 @@ __device__ __forceinline__ unsigned long long window_key(const unsigned long lon
 }
 
 // bidirectionalReprojection_kernel<SW, SI, MAIN_ALWAYS_VALID>, src/renderer.cu:400-465
-// block = (32, n_views): output rows ROWS * blockIdx.y + {0, 1}, 32 pixels each, one warp per source view.
+// block = (32, n_views): 32 output columns x (2 * row_pairs) output rows, one warp per source
+// view.  The block works through units (frame k, row pair): phase 1 runs one unit at a time
+// on every warp; phases 2-3 spread the units' rows over the warps.  More row pairs per block
+// (for single frames) keep every warp busy in phase 2.
 template <int SW, int SI, bool MAV, int REGS>
 __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FrameParams p, const __grid_constant__ KeyMaps km)
 {
@@ -651,16 +655,16 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
     // dynamic shared memory only (no static __shared__ in front of it): the key tiles start at
     // the 1 KiB-aligned window base, so every TMA destination is 128-byte aligned
     extern __shared__ __align__(1024) unsigned char smem[];
-    const int nv = p.n_views, nf = p.n_frames, fg = p.frames_per_group;
+    const int nv = p.n_views, nf = p.n_frames, np = p.row_pairs, nu = nf * np;
     // [key tiles, phase 1 | chained colours and flags, phases 2-3 (same bytes)][results][barrier]
-    unsigned long long *tiles = reinterpret_cast<unsigned long long *>(smem);                 // [fg][nv][H][W]
-    uint32_t *cols = reinterpret_cast<uint32_t *>(smem);                                      // [nf][ROWS][32]
-    uint32_t *valid = cols + nf * ROWS * 32;                                                 // [nf][ROWS][32]
-    DirRes *res = reinterpret_cast<DirRes *>(smem + reproj_tile_region<SW>(nv, nf, fg));     // [nf][ROWS][nv][32]
-    unsigned long long &bar = *reinterpret_cast<unsigned long long *>(res + nf * ROWS * nv * 32); // TMA completion barrier
+    unsigned long long *tiles = reinterpret_cast<unsigned long long *>(smem);                 // [nv][H][W]
+    uint32_t *cols = reinterpret_cast<uint32_t *>(smem);                                      // [nu][ROWS][32]
+    uint32_t *valid = cols + nu * ROWS * 32;                                                 // [nu][ROWS][32]
+    DirRes *res = reinterpret_cast<DirRes *>(smem + reproj_tile_region<SW>(nv, nu));         // [nu][ROWS][nv][32]
+    unsigned long long &bar = *reinterpret_cast<unsigned long long *>(res + nu * ROWS * nv * 32); // TMA completion barrier
 
     const int lane = threadIdx.x, vw = threadIdx.y;
-    const uint32_t x0 = blockIdx.x * 32, x = x0 + lane, y0 = blockIdx.y * ROWS;
+    const uint32_t x0 = blockIdx.x * 32, x = x0 + lane, yb = blockIdx.y * (ROWS * np);
     const bool xok = x < p.out_w;
     const bool leader = lane == 0 && vw == 0;
     if (p.use_tma)
@@ -672,68 +676,66 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
     {
         const DevView &v = p.v[vw];
         const uint32_t ix = v.sx == 1 ? x : x / v.sx, tx0 = v.sx == 1 ? x0 : x0 / v.sx;
-        const uint32_t iy0 = v.sy == 1 ? y0 : y0 / v.sy, iy1 = v.sy == 1 ? y0 + 1 : (y0 + 1) / v.sy;
-        const bool rok[ROWS] = {xok, xok && y0 + 1 < p.out_h};
         const bool fwd = (vw & 1) == 0;
         const int xs = tile_x0(tx0, SW);
         const int col = (int)ix - xs;
-        const int wrow[ROWS] = {SW, (int)(iy1 - iy0) + SW}; // tile row of each output row's window centre
         // pixel2CS of the output pixels in the main view (the search target) and in this view (the error)
         const DevView &v0 = p.v[0];
-        const uint32_t xc = min(x, p.out_w - 1), y1c = min(y0 + 1, p.out_h - 1);
+        const uint32_t xc = min(x, p.out_w - 1);
         const float qx = __ldg(v0.lut + xc);
-        const float qy[ROWS] = {__ldg(v0.lut + v0.w + y0), __ldg(v0.lut + v0.w + y1c)};
         const float pcx = __ldg(v.lut + min(ix, v.w - 1));
-        const float pcy[ROWS] = {__ldg(v.lut + v.w + iy0), __ldg(v.lut + v.w + min(iy1, v.h - 1))};
         const uint32_t vwid = v.w, vhei = v.h;
+        int round = 0; // TMA rounds so far (mbarrier phase parity)
 #pragma unroll 1
-        for (int k0 = 0, grp = 0; k0 < nf; k0 += fg, grp++)
+        for (int rp = 0; rp < np; rp++)
         {
-            const int ng = min(fg, nf - k0);
-            if (k0 > 0)
-                __syncthreads(); // every warp is done with the previous group's tiles
+            const uint32_t y0 = yb + (uint32_t)rp * ROWS; // the row pair's first output row
+            const uint32_t iy0 = v.sy == 1 ? y0 : y0 / v.sy, iy1 = v.sy == 1 ? y0 + 1 : (y0 + 1) / v.sy;
+            const bool rok[ROWS] = {xok && y0 < p.out_h, xok && y0 + 1 < p.out_h};
+            const int wrow[ROWS] = {SW, (int)(iy1 - iy0) + SW}; // tile row of each output row's window centre
+            const uint32_t y0c = min(y0, p.out_h - 1), y1c = min(y0 + 1, p.out_h - 1);
+            const float qy[ROWS] = {__ldg(v0.lut + v0.w + y0c), __ldg(v0.lut + v0.w + y1c)};
+            const float pcy[ROWS] = {__ldg(v.lut + v.w + min(iy0, vhei - 1)), __ldg(v.lut + v.w + min(iy1, vhei - 1))};
+#pragma unroll 1
+        for (int k = 0; k < nf; k++, round++)
+        {
+            const int u = k * np + rp;
+            if (round > 0)
+                __syncthreads(); // every warp is done with the previous unit's tiles
             if (p.use_tma)
             {
                 if (leader)
                 {
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    mbar_expect_tx(&bar, (uint32_t)(ng * nv * T::BYTES));
-                    for (int g = 0; g < ng; g++)
-                        for (int w = 0; w < nv; w++)
-                        {
-                            const DevView &vv = p.v[w];
-                            const uint32_t wx0 = vv.sx == 1 ? x0 : x0 / vv.sx, wy0 = vv.sy == 1 ? y0 : y0 / vv.sy;
-                            tma_load_3d(tiles + (size_t)(g * nv + w) * T::ELEMS, &km.m[w], tile_x0(wx0, SW), (int)wy0 - SW, k0 + g, &bar);
-                        }
+                    mbar_expect_tx(&bar, (uint32_t)(nv * T::BYTES));
+                    for (int w = 0; w < nv; w++)
+                    {
+                        const DevView &vv = p.v[w];
+                        const uint32_t wx0 = vv.sx == 1 ? x0 : x0 / vv.sx, wy0 = vv.sy == 1 ? y0 : y0 / vv.sy;
+                        tma_load_3d(tiles + (size_t)w * T::ELEMS, &km.m[w], tile_x0(wx0, SW), (int)wy0 - SW, k, &bar);
+                    }
                 }
-                mbar_wait_bounded(&bar, (uint32_t)(grp & 1), p.status);
+                mbar_wait_bounded(&bar, (uint32_t)(round & 1), p.status);
             }
             else
             {
-                for (int g = 0; g < ng; g++)
-                {
-                    const unsigned long long *keys = v.splat + (k0 + g) * p.key_stride;
-                    unsigned long long *tg = tiles + (size_t)(g * nv + vw) * T::ELEMS;
+                const unsigned long long *keys = v.splat + k * p.key_stride;
+                unsigned long long *tg = tiles + (size_t)vw * T::ELEMS;
 #pragma unroll
-                    for (int r = 0; r < T::H; r++)
+                for (int r = 0; r < T::H; r++)
+                {
+                    const uint32_t gy = iy0 - SW + r;
+                    const bool row_ok = gy < vhei;
+                    for (int c = lane; c < T::W; c += 32)
                     {
-                        const uint32_t gy = iy0 - SW + r;
-                        const bool row_ok = gy < vhei;
-                        for (int c = lane; c < T::W; c += 32)
-                        {
-                            const uint32_t gx = (uint32_t)(xs + c);
-                            tg[r * T::W + c] = (row_ok && gx < vwid) ? __ldg(keys + (gy * vwid + gx)) : 0ull;
-                        }
+                        const uint32_t gx = (uint32_t)(xs + c);
+                        tg[r * T::W + c] = (row_ok && gx < vwid) ? __ldg(keys + (gy * vwid + gx)) : 0ull;
                     }
                 }
                 __syncwarp();
             }
-
-#pragma unroll 1
-            for (int g = 0; g < ng; g++)
             {
-                const int k = k0 + g;
-                const unsigned long long *tg = tiles + (size_t)(g * nv + vw) * T::ELEMS;
+                const unsigned long long *tg = tiles + (size_t)vw * T::ELEMS;
                 const float4 *cam = v.cam_ff + k * p.cam_stride;
                 const bool search_ok = !fwd || p.f[k].alpha < 1.0f;
                 bool s[ROWS];
@@ -799,19 +801,22 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
                         d.error_vis = pack_error_vis(__fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey))), m[r].w > 0.0f);
                     }
                     d.src = (ax[r] << 16) | ay[r];
-                    res[((k * ROWS + r) * nv + vw) * 32 + lane] = d;
+                    res[((u * ROWS + r) * nv + vw) * 32 + lane] = d;
                 }
             }
+        }
         }
     }
     __syncthreads();
 
-    // phase 2: (frame, row) tasks over the warps
+    // phase 2: (unit, row) tasks over the warps
 #pragma unroll 1
-    for (int t = vw; t < nf * ROWS; t += nv)
+    for (int t = vw; t < nu * ROWS; t += nv)
     {
-        const int k = t / ROWS, r = t % ROWS;
-        const uint32_t y = y0 + r;
+        const int u = t / ROWS, r = t % ROWS;
+        // u = k * np + rp; np is 1..3 (the host's choice), so no general division
+        const int k = np == 1 ? u : (np == 2 ? (u >> 1) : (np == 3 ? u / 3 : u / np));
+        const uint32_t y = yb + (uint32_t)(u - k * np) * ROWS + r;
         uint32_t color = 0;
         const bool ok = xok && y < p.out_h && resolve_pixel<MAV>(res + t * nv * 32, lane, p, p.f[k], color);
         if (!p.chain)
@@ -829,16 +834,16 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
         return;
     __syncthreads();
     // phase 3: one persistent buffer per row, starting as out[0], copied to out[k] after frame k
-    if (vw >= ROWS)
+    if (vw >= np * ROWS)
         return;
-    const uint32_t y = y0 + vw;
+    const uint32_t y = yb + vw; // row vw of the block: row vw % ROWS of row pair vw / ROWS
     if (!xok || y >= p.out_h)
         return;
     uint32_t run = 0;
     for (int k = 0; k < nf; k++)
     {
         uint32_t *o = p.out[k] + (y * p.out_w + x);
-        const int t = k * ROWS + vw;
+        const int t = (k * np + vw / ROWS) * ROWS + vw % ROWS;
         if (k == 0)
             run = *o;
         if (valid[t * 32 + lane])
@@ -1022,11 +1027,10 @@ __global__ void rgb8_to_rgba8_kernel(uint32_t *__restrict__ dst, const uint8_t *
         dst[i] = (uint32_t)__ldg(src + 3 * i) | (uint32_t)__ldg(src + 3 * i + 1) << 8 | (uint32_t)__ldg(src + 3 * i + 2) << 16 | 0xff000000u;
 }
 
-// Dynamic shared memory of one reprojection block.
+// Dynamic shared memory of one reprojection block of `n_units` units.
 template <int SW>
-constexpr size_t reproj_smem(int n_views, int n_frames, int frames_per_group)
+constexpr size_t reproj_smem(int n_views, int n_units)
 {
-    return reproj_tile_region<SW>(n_views, n_frames, frames_per_group) + (size_t)n_frames * ROWS * n_views * 32 * sizeof(DirRes) +
-           16; // + mbarrier
+    return reproj_tile_region<SW>(n_views, n_units) + (size_t)n_units * ROWS * n_views * 32 * sizeof(DirRes) + 16; // + mbarrier
 }
 } // namespace isti

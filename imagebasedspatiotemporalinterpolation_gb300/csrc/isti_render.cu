@@ -305,18 +305,19 @@ bool make_key_maps(const isti::FrameParams &p, isti::KeyMaps &km)
 template <int SW, int SI, bool MAV, int REGS>
 cudaError_t launch_reproj_regs(isti::FrameParams &p, cudaStream_t stream)
 {
-    // One frame's key tiles per TMA round: the least shared memory per block, so the most
+    // One unit's key tiles per TMA round: the least shared memory per block, so the most
     // resident blocks and the largest L1 (1080p, 6 views, 3 frames, 8 blocks per SM: one
     // frame per round 0.569 ms, two 0.581 ms; at 7 blocks two frames 0.590, three 0.594).
+    // Row pairs per block: enough (frame, row) tasks for every warp in phase 2 when there
+    // are fewer frames than views need (a single frame of 6 views: 3 row pairs).
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess)
         return e;
-    const int fg = 1;
-    p.frames_per_group = fg;
+    p.row_pairs = std::max(1, std::min(3, p.n_views / (isti::ROWS * p.n_frames)));
     static thread_local isti::KeyMaps km; // 2 KiB, passed by value as a kernel parameter
     p.use_tma = make_key_maps<SW>(p, km) ? 1 : 0;
-    const size_t smem = isti::reproj_smem<SW>(p.n_views, p.n_frames, fg);
+    const size_t smem = isti::reproj_smem<SW>(p.n_views, p.n_frames * p.row_pairs);
     // raise the kernel's dynamic shared-memory limit once to the largest size requested, so
     // that calls inside a CUDA graph capture make no attribute calls after a first uncaptured
     // call of the same shape
@@ -334,7 +335,8 @@ cudaError_t launch_reproj_regs(isti::FrameParams &p, cudaStream_t stream)
             cur = (int)smem;
         }
     }
-    const dim3 gr((p.out_w + 31) / 32, (p.out_h + isti::ROWS - 1) / isti::ROWS);
+    const uint32_t block_rows = (uint32_t)(isti::ROWS * p.row_pairs);
+    const dim3 gr((p.out_w + 31) / 32, (p.out_h + block_rows - 1) / block_rows);
     isti::reproj_kernel<SW, SI, MAV, REGS><<<gr, dim3(32, p.n_views), smem, stream>>>(p, km);
     return cudaGetLastError();
 }
