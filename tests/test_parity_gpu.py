@@ -126,6 +126,22 @@ def test_oracle_parity_odd_sizes_and_half_res_aux(cuda):
         assert_bit_exact(render_gpu(frame, client, prev), *exp)
 
 
+@pytest.mark.parametrize("mode", [0, 1, 3])
+def test_row_pair_blocks_partial_last_block(cuda, mode):
+    """Single frames of 6 views run 3 row pairs per block (4 views: 2): heights that leave a
+    partial last block, full- and half-resolution aux cameras."""
+    for (w, h, aux_size) in ((250, 139, None), (250, 140, (125, 70)), (96, 7, None), (130, 4, (65, 2))):
+        seq = Sequence(w, h, 2, seed=w + h + mode, aux_offsets=(-0.3, 0.3), aux_size=aux_size, shadows=True,
+                       max_speed=3.0, n_spheres=40)
+        frame, client = seq.frame(0), seq.client(0, 1, mode=mode)
+        prev = np.full((h, w, 4), 31, np.uint8)
+        assert_bit_exact(render_gpu(frame, client, prev), *oracle.run_oracle(frame, client, prev))
+    seq = Sequence(161, 43, 2, seed=5, aux_offsets=(0.3,), shadows=True, max_speed=3.0)  # 4 views
+    frame, client = seq.frame(0), seq.client(0, 2, mode=mode)
+    prev = np.full((43, 161, 4), 3, np.uint8)
+    assert_bit_exact(render_gpu(frame, client, prev), *oracle.run_oracle(frame, client, prev))
+
+
 def test_repeated_runs_bit_identical(cuda):
     """atomicMin is order-independent: 10 renders give identical keys and images."""
     seq = Sequence(640, 360, 2, seed=404, aux_offsets=(-0.3, 0.3), shadows=True)
