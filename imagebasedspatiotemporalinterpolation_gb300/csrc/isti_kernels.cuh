@@ -29,6 +29,7 @@
 
 #include "isti.h"
 #include "isti_device.cuh"
+#include "isti_error_cmp.cuh"
 
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -51,7 +52,6 @@ constexpr int REPROJ_REGS = 48;
 constexpr int REPROJ_REGS_MANY_VIEWS = 40;
 constexpr int REPROJ_MANY_VIEWS = 4;
 constexpr int REPROJ_REGS_WIDE_WINDOW = 56;
-constexpr float FLT_MAX_F = 3.402823466e+38f;
 
 struct DevView
 {
@@ -430,22 +430,34 @@ __device__ uint32_t second_chance(float weight, const ShadowFrames &sf, const Fr
 // ---- bidirectional reprojection, src/renderer.cu:148-465 ----
 
 // One direction of one camera for one output pixel: window init + search + error.
-// 12 bytes in shared memory: the error is never negative, so its sign bit carries
+// 12 bytes in shared memory.  The error is stored as a pattern of isti_error_cmp.cuh:
+// squared (SQ, no square root per searched direction) or its rounded root; bit 31 carries
 // visible_in_main.
 struct DirRes
 {
-    float error_vis; // error (FLT_MAX when not searched); sign bit = visible_in_main
-    float depth;     // searched depth, else the window-initialisation depth
-    uint32_t src;    // source pixel, x << 16 | y
+    uint32_t error_vis; // err_pack<SQ>(squared error), ERR_UNSEARCHED_OF<SQ> when not searched; bit 31 = visible_in_main
+    float depth;        // searched depth, else the window-initialisation depth
+    uint32_t src;       // source pixel, x << 16 | y
 };
 
-// (a NaN error loses its sign, which no comparison sees)
-__device__ __forceinline__ float pack_error_vis(float error, bool vis)
+// Squared errors save the square root, but the freer schedule spills at 40 registers, where
+// the roots are faster (1080p, 3 frames, 6 views: 0.537 ms roots, 0.548 squared; 2 views at
+// 48 registers 0.238 -> 0.222 ms squared; 7x7 window at 56, 6 views 1.116 -> 1.092 ms).
+template <int REGS>
+constexpr bool SQUARED_ERRORS = REGS != REPROJ_REGS_MANY_VIEWS;
+
+template <bool SQ>
+constexpr uint32_t ERR_EPS_1_FULL_RES = err_eps<SQ>(EPS_1_FULL_RES); // error < EPS_1 <=> pattern < this
+template <bool SQ>
+constexpr uint32_t ERR_EPS_1_LOW_RES = err_eps<SQ>(EPS_1_LOW_RES);
+
+template <bool SQ>
+__device__ __forceinline__ uint32_t pack_error_vis(float error2, bool vis)
 {
-    return __uint_as_float((__float_as_uint(error) & 0x7fffffffu) | (vis ? 0x80000000u : 0u));
+    return err_pack<SQ>(error2) | (vis ? 0x80000000u : 0u);
 }
-__device__ __forceinline__ float dir_error(const DirRes &d) { return __uint_as_float(__float_as_uint(d.error_vis) & 0x7fffffffu); }
-__device__ __forceinline__ bool dir_vis(const DirRes &d) { return (__float_as_uint(d.error_vis) >> 31) != 0u; }
+__device__ __forceinline__ uint32_t dir_error(const DirRes &d) { return d.error_vis & 0x7fffffffu; }
+__device__ __forceinline__ bool dir_vis(const DirRes &d) { return (d.error_vis >> 31) != 0u; }
 
 // Result of bidirectionalReprojection for one camera (src/renderer.cu:366-397), without its colour.
 struct CamRes
@@ -454,7 +466,7 @@ struct CamRes
     bool vis;
     bool blend;      // always-valid 50/50 blend of both directions
     int32_t priority;
-    float error;     // indeterminate in the reference for the blend; 0 here
+    uint32_t error;  // squared error bits; indeterminate in the reference for the blend, 0 here
     float depth;
     int32_t dir;     // 0 forward keyframe, 1 backward keyframe
     uint32_t src;
@@ -486,7 +498,8 @@ __host__ __device__ constexpr size_t reproj_tile_region(int n_views, int n_units
     return tiles > chain ? tiles : chain;
 }
 
-__device__ __forceinline__ CamRes cam_result(const DirRes &f, const DirRes &b, const DevView &vf, const DevView &vb, float eps1, float eps2,
+template <bool SQ>
+__device__ __forceinline__ CamRes cam_result(const DirRes &f, const DirRes &b, const DevView &vf, const DevView &vb, uint32_t eps1, float eps2,
                                              bool always_valid)
 {
     CamRes r;
@@ -494,17 +507,18 @@ __device__ __forceinline__ CamRes cam_result(const DirRes &f, const DirRes &b, c
     r.vis = false;
     r.blend = false;
     r.priority = 0;
-    r.error = 0.0f;
+    r.error = 0u;
     r.depth = 0.0f;
     r.dir = 0;
     r.src = 0;
-    const float fe = dir_error(f), be = dir_error(b);
+    const uint32_t fe = dir_error(f), be = dir_error(b);
     const bool fvis = dir_vis(f), bvis = dir_vis(b);
-    if (fe < eps1 || be < eps1)
+    const bool fok = err_below<SQ>(fe, eps1), bok = err_below<SQ>(be, eps1);
+    if (fok || bok)
     {
-        const bool both = fe < eps1 && be < eps1;
+        const bool both = fok && bok;
         const bool similar = fabsf(__fsub_rn(depth_to_z(f.depth), depth_to_z(b.depth))) < eps2;
-        const bool choose_fwd = (both && !similar && f.depth < b.depth) || ((!both || similar) && fe < be);
+        const bool choose_fwd = (both && !similar && f.depth < b.depth) || ((!both || similar) && err_less<SQ>(fe, be));
         r.valid = true;
         if (choose_fwd)
         {
@@ -536,27 +550,27 @@ __device__ __forceinline__ CamRes cam_result(const DirRes &f, const DirRes &b, c
 // Chooses among the cameras of one output pixel and returns the colour to
 // write (false: keep the previous output), src/renderer.cu:400-465.
 // res points at the [n_views][32] results of this pixel's row and frame.
-template <bool MAV>
+template <bool MAV, bool SQ>
 __device__ __forceinline__ bool resolve_pixel(const DirRes *res, int lane, const FrameParams &p, const FrameCfg &c, uint32_t &color)
 {
-    const CamRes m = cam_result(res[lane], res[32 + lane], p.v[0], p.v[1], EPS_1_FULL_RES, EPS_2_FULL_RES, MAV);
+    const CamRes m = cam_result<SQ>(res[lane], res[32 + lane], p.v[0], p.v[1], ERR_EPS_1_FULL_RES<SQ>, EPS_2_FULL_RES, MAV);
     CamRes best;
     best.valid = false;
     best.vis = false;
     best.priority = 0;
-    best.error = 0.0f;
+    best.error = 0u;
     best.depth = 0.0f;
     int best_cam = 0;
     const int n_cams = p.n_views / 2;
     for (int cam = 1; cam < n_cams; cam++)
     {
-        const CamRes r = cam_result(res[(2 * cam) * 32 + lane], res[(2 * cam + 1) * 32 + lane], p.v[2 * cam], p.v[2 * cam + 1], EPS_1_LOW_RES,
-                                    EPS_2_LOW_RES, false);
+        const CamRes r = cam_result<SQ>(res[(2 * cam) * 32 + lane], res[(2 * cam + 1) * 32 + lane], p.v[2 * cam], p.v[2 * cam + 1],
+                                        ERR_EPS_1_LOW_RES<SQ>, EPS_2_LOW_RES, false);
         bool take = !best.valid;
         if (best.valid && r.valid)
         {
             const bool similar = fabsf(__fsub_rn(depth_to_z(best.depth), depth_to_z(r.depth))) < EPS_2_LOW_RES;
-            take = (!similar && r.depth < best.depth) || (similar && r.priority >= best.priority && r.error < best.error);
+            take = (!similar && r.depth < best.depth) || (similar && r.priority >= best.priority && err_less<SQ>(r.error, best.error));
         }
         if (take)
         {
@@ -791,14 +805,14 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
                 for (int r = 0; r < ROWS; r++)
                 {
                     DirRes d;
-                    d.error_vis = FLT_MAX_F;
+                    d.error_vis = ERR_UNSEARCHED_OF<SQUARED_ERRORS<REGS>>;
                     d.depth = d_init[r];
                     if (s[r])
                     {
                         d.depth = z_to_depth(__fadd_rn(zz[r], m[r].z));
                         const float ex = __fmul_rn(__fsub_rn(__fadd_rn(fx[r], m[r].x), pcx), v.err_sx);
                         const float ey = __fmul_rn(__fsub_rn(__fadd_rn(fy[r], m[r].y), pcy[r]), v.err_sy);
-                        d.error_vis = pack_error_vis(__fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey))), m[r].w > 0.0f);
+                        d.error_vis = pack_error_vis<SQUARED_ERRORS<REGS>>(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), m[r].w > 0.0f);
                     }
                     d.src = (ax[r] << 16) | ay[r];
                     res[((u * ROWS + r) * nv + vw) * 32 + lane] = d;
@@ -818,7 +832,7 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
         const int k = np == 1 ? u : (np == 2 ? (u >> 1) : (np == 3 ? u / 3 : u / np));
         const uint32_t y = yb + (uint32_t)(u - k * np) * ROWS + r;
         uint32_t color = 0;
-        const bool ok = xok && y < p.out_h && resolve_pixel<MAV>(res + t * nv * 32, lane, p, p.f[k], color);
+        const bool ok = xok && y < p.out_h && resolve_pixel<MAV, SQUARED_ERRORS<REGS>>(res + t * nv * 32, lane, p, p.f[k], color);
         if (!p.chain)
         {
             if (ok)
