@@ -250,9 +250,15 @@ __global__ void __launch_bounds__(256, 8) splat_kernel(const __grid_constant__ F
     const float4 d_ws = make_float4(__fsub_rn(ws_to.x, ws_from.x), __fsub_rn(ws_to.y, ws_from.y), __fsub_rn(ws_to.z, ws_from.z),
                                     __fsub_rn(ws_to.w, ws_from.w));
 
-    // client-camera part, per frame
-    for (int k = 0; k < p.n_frames; k++)
+    // client-camera part, per frame.  Unrolled over the batch limit, so the client matrix
+    // p.cam_vp[k] is read as constant operands rather than by indexed loads (1080p, 3
+    // frames, 6 views: 0.287 -> 0.270 ms; a switch on the view index for the same effect on
+    // the view's matrices spills at 32 registers and was slower, 0.280 ms).
+#pragma unroll
+    for (int k = 0; k < MAX_FRAMES; k++)
     {
+        if (k >= p.n_frames)
+            break;
         const float wg = v.forward ? p.f[k].alpha : __fsub_rn(1.0f, p.f[k].alpha);
         unsigned long long *keys = v.splat + k * p.key_stride;
         float4 *cam = v.cam_ff + k * p.cam_stride;

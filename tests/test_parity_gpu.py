@@ -276,8 +276,19 @@ def test_batch_limits(cuda):
     frame = DeviceFrame.from_host(seq.frame(0))
     r = Renderer()
     bufs = [torch.zeros((36, 64, 4), dtype=torch.uint8, device="cuda") for _ in range(9)]
-    clients = [seq.client(0, b % 4) for b in range(9)]
-    r.render_batch(bufs[:8], clients[:8], frame)
+    clients = [seq.client(0, b % 4, alpha=(b + 1) / 9) for b in range(9)]
+    # the largest batch equals frame-by-frame renders, outputs and splat keys
+    singles, keys = [], []
+    for c in clients[:8]:
+        single = torch.zeros((36, 64, 4), dtype=torch.uint8, device="cuda")
+        r.render(single, c, frame)
+        singles.append(single)
+        keys.append(r.view_buffers(0)[0].clone())
+    r.render_batch(bufs[:8], clients[:8], frame, chain=False)
+    torch.cuda.synchronize()
+    for k in range(8):
+        assert torch.equal(bufs[k], singles[k]), f"frame {k} of 8 differs"
+        assert torch.equal(r.view_buffers(k * len(frame.views()))[0], keys[k]), f"frame {k} of 8: keys differ"
     with pytest.raises(ValueError):
         r.render_batch(bufs, clients, frame)
     mixed = [seq.client(0, 1), seq.client(0, 2, mode=3)]
