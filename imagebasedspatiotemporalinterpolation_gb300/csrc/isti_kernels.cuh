@@ -769,6 +769,11 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
                     ax[r] = ((uint32_t)lo) >> 16;
                     ay[r] = (uint32_t)lo & 0xFFFFu;
                     s[r] = rok[r] && search_ok && d_init[r] > 0.0f;
+                    // the depth read after the search is mostly at or next to the start (a
+                    // splatted source pixel, in range): fetch its line into L1 during the search
+                    // (3x3 window, 6 views: 0.537 -> 0.533 ms; no gain for the 7x7 window)
+                    if (SW == 1 && s[r])
+                        asm volatile("prefetch.global.L1 [%0];" ::"l"(v.z + (ay[r] * vwid + ax[r])));
                 }
                 // iterativeSearch<SI>, src/renderer.cu:177-202, both rows interleaved.  The start is a
                 // splatted source pixel and every accepted step is in range: no border handling needed.
