@@ -66,6 +66,9 @@ def parse():
     ap.add_argument("--no-per-frame", action="store_true", help="skip the single-frame-call comparison")
     ap.add_argument("--no-quality", action="store_true", help="skip PSNR / SSIM against the analytic ground truth")
     ap.add_argument("--no-graph-batch", action="store_true", help="skip the mixed-resolution batch under a CUDA graph")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving loop with simulated clients")
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="real time of the serving loop (the config runs 60 s)")
+    ap.add_argument("--serve-slots", type=int, default=4, help="concurrent batches (streams) of the serving loop")
     return ap.parse_args()
 
 
@@ -336,6 +339,11 @@ def main_ours(args):
     if not args.no_graph_batch:
         graph_batch = run_graph_batch(args, dev, rank)
 
+    # ---- the serving loop: simulated clients in real time (reported beside the line)
+    serving = None
+    if not args.no_serving:
+        serving = run_serving(args, dev, rank)
+
     # ---- roofline of the dominant kernel.  Algorithmic bytes per interpolated output pixel
     # (the per-unit figure of the path): every source view's inputs once and the output once,
     # 6 views x (4 z + 6 f16 motion + 4 colour + 12 shadow A/B/Info) + 4 = 160 B.  Split by the
@@ -417,6 +425,7 @@ def main_ours(args):
                                     "reproj_kernel": round(per_launch_ms["reproj_kernel"], 4)},
             "per_frame_api": per_frame,
             "graph_batch_mixed": graph_batch,
+            "serving": serving,
             "gpu_launches": tim["kernel_launches"],
             "clocks": clk,
             "e2e": e2e,
@@ -434,6 +443,57 @@ def main_ours(args):
 GB_RES = ((1280, 720), (1920, 1080), (2064, 2208))
 GB_PAIRS = 16
 GB_EYES = (-0.032, 0.032)  # half the interpupillary distance, metres
+SV_CLIENTS = 16
+
+
+def run_serving(args, dev, rank):
+    """The serving workload of the benchmark list: 16 simulated clients, each sending stereo
+    frame requests as a Poisson process at a rate drawn from U[90, 120] Hz and receiving a
+    new keyframe pair every 1/30 s, at 1280x720 / 1920x1080 / 2064x2208 per eye in turn,
+    main camera only, no shadows, plain method; keyframes resident on the device, admission
+    against a 120 GB budget, 4 slots, batches of up to 8 frames.  Runs in real time for
+    --serve-seconds, then drains; latency is from a request's scheduled arrival to the loop
+    seeing its batch done.  Keyframe pairs are uploaded from pinned host memory as they
+    arrive (each client cycles through two pre-rendered pairs of its resolution)."""
+    import numpy as np
+    import torch
+
+    from imagebasedspatiotemporalinterpolation_gb300 import scene
+    from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame
+    from imagebasedspatiotemporalinterpolation_gb300.serving import CudaBackend, PinnedPair, Server, SimClient, eye_info, simulate
+
+    rng = np.random.default_rng(args.seed + 7 + rank)
+    seqs = {}
+    for j, (w, h) in enumerate(GB_RES):
+        seq = scene.Sequence(w, h, 3, seed=args.seed + 301 * (j + 1) + rank)
+        seqs[(w, h)] = (seq, [PinnedPair(seq.frame(p)) for p in range(2)])
+    max_w, max_h = max(GB_RES, key=lambda r: r[0] * r[1])
+    server = Server(CudaBackend(dev), hbm_budget=120 << 30, n_slots=args.serve_slots, max_batch=8,
+                    slot_pixels=max_w * max_h, slot_views=2)
+    # every slot's renderer sized once for the largest batch (no allocation while serving)
+    big_seq = seqs[(max_w, max_h)][0]
+    big = DeviceFrame.from_host(big_seq.frame(0), dev)
+    outs = [torch.zeros((max_h, max_w, 4), dtype=torch.uint8, device=dev) for _ in range(8)]
+    infos = [eye_info(big_seq, 0, b / 8, GB_EYES[0]) for b in range(8)]
+    for stream, renderer in server.slots:
+        renderer.render_batch(outs, infos, big, chain=True, stream=stream)
+    torch.cuda.synchronize()
+    del outs, big
+    sims = []
+    for c in range(SV_CLIENTS):
+        w, h = GB_RES[c % len(GB_RES)]
+        seq, pairs = seqs[(w, h)]
+        server.open_client(c, w, h, len(GB_EYES), pairs[0])
+        sims.append(SimClient(c, seq, pairs, rate_hz=float(rng.uniform(90.0, 120.0)), phase_s=float(rng.uniform(0.0, 1.0 / 30))))
+    st = simulate(server, sims, seconds=args.serve_seconds, eyes=GB_EYES, seed=args.seed + rank)
+    torch.cuda.synchronize()
+    return {"mpix_per_s": round(st["mpix_per_s"], 1), "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+            "requests": st["requests"], "offered_requests": st["offered_requests"], "refused_requests": st["refused_requests"],
+            "batches": st["batches"], "frames_per_batch": round(st["frames_per_batch"], 2), "keyframe_uploads": st["uploads"],
+            "clients": st["clients"], "admitted": st["admitted"], "seconds": args.serve_seconds,
+            "reserved_gb": round(st["peak_reserved_bytes"] / 2**30, 2), "budget_gb": 120, "slots": args.serve_slots,
+            "workload": "16 clients, stereo requests Poisson U[90,120] Hz, keyframe pairs 30 Hz, 1280x720 / 1920x1080 / "
+                        "2064x2208 per eye, main camera only, plain method, continuous batching"}
 
 
 def run_graph_batch(args, dev, rank):
