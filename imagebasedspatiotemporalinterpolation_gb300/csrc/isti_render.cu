@@ -39,6 +39,9 @@ struct isti_renderer
     std::vector<int32_t> event_frames;
     size_t events_used = 0;
     int32_t timed_launches = 0;
+    // autotuning of the reprojection launch: one entry per tuned shape class
+    bool autotune = false;
+    std::vector<isti_tuning> tuned;
 };
 
 namespace
@@ -302,8 +305,26 @@ bool make_key_maps(const isti::FrameParams &p, isti::KeyMaps &km)
     return true;
 }
 
+// A reprojection launch shape: register cap and output row pairs per block (0: the fixed rule).
+struct ReprojChoice
+{
+    int regs = 0;
+    int row_pairs = 0;
+};
+
+// The fixed rule: register cap by window size and view count (isti_kernels.cuh), row pairs
+// so that every warp has a colour task in phase 2.
+int rule_regs(int sw, int n_views)
+{
+    if (sw != 1)
+        return isti::REPROJ_REGS_WIDE_WINDOW;
+    return n_views >= isti::REPROJ_MANY_VIEWS ? isti::REPROJ_REGS_MANY_VIEWS : isti::REPROJ_REGS;
+}
+
+int rule_row_pairs(int n_views, int n_frames) { return std::max(1, std::min(3, n_views / (isti::ROWS * n_frames))); }
+
 template <int SW, int SI, bool MAV, int REGS>
-cudaError_t launch_reproj_regs(isti::FrameParams &p, cudaStream_t stream)
+cudaError_t launch_reproj_regs(isti::FrameParams &p, cudaStream_t stream, int row_pairs)
 {
     // One unit's key tiles per TMA round: the least shared memory per block, so the most
     // resident blocks and the largest L1 (1080p, 6 views, 3 frames, 8 blocks per SM: one
@@ -314,7 +335,7 @@ cudaError_t launch_reproj_regs(isti::FrameParams &p, cudaStream_t stream)
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess)
         return e;
-    p.row_pairs = std::max(1, std::min(3, p.n_views / (isti::ROWS * p.n_frames)));
+    p.row_pairs = row_pairs > 0 ? std::min(row_pairs, 3) : rule_row_pairs(p.n_views, p.n_frames);
     static thread_local isti::KeyMaps km; // 2 KiB, passed by value as a kernel parameter
     p.use_tma = make_key_maps<SW>(p, km) ? 1 : 0;
     const size_t smem = isti::reproj_smem<SW>(p.n_views, p.n_frames * p.row_pairs);
@@ -342,20 +363,48 @@ cudaError_t launch_reproj_regs(isti::FrameParams &p, cudaStream_t stream)
 }
 
 template <int SW, int SI, bool MAV>
-cudaError_t launch_reproj(isti::FrameParams &p, cudaStream_t stream)
+cudaError_t launch_reproj(isti::FrameParams &p, cudaStream_t stream, ReprojChoice c)
 {
+    const int regs = c.regs > 0 ? c.regs : rule_regs(SW, p.n_views);
     if constexpr (SW == 1)
     {
-        if (p.n_views >= isti::REPROJ_MANY_VIEWS)
-            return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS_MANY_VIEWS>(p, stream);
-        return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS>(p, stream);
+        if (regs == isti::REPROJ_REGS_MANY_VIEWS)
+            return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS_MANY_VIEWS>(p, stream, c.row_pairs);
+        return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS>(p, stream, c.row_pairs);
     }
     else
-        return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS_WIDE_WINDOW>(p, stream);
+        return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS_WIDE_WINDOW>(p, stream, c.row_pairs);
+}
+
+// window size of the reprojection of a render mode (src/renderer.cu:676-693)
+int mode_window(int mode) { return mode == ISTI_MODE_BACKWARD_BIDIRECTIONAL ? 3 : 1; }
+
+// register caps a mode's reprojection is built with (the autotuner's candidates)
+std::vector<int> mode_regs(int mode)
+{
+    if (mode_window(mode) == 1)
+        return {isti::REPROJ_REGS_MANY_VIEWS, isti::REPROJ_REGS};
+    return {isti::REPROJ_REGS_WIDE_WINDOW};
+}
+
+cudaError_t launch_reproj_mode(isti::FrameParams &p, int mode, cudaStream_t stream, ReprojChoice c)
+{
+    switch (mode)
+    {
+    case ISTI_MODE_OURS:
+    case ISTI_MODE_BACKWARD_UNIDIRECTIONAL:
+        return launch_reproj<1, 3, false>(p, stream, c);
+    case ISTI_MODE_SPLATTING:
+        return launch_reproj<1, 0, false>(p, stream, c);
+    case ISTI_MODE_BACKWARD_BIDIRECTIONAL:
+        return launch_reproj<3, 5, true>(p, stream, c);
+    }
+    return cudaGetLastError();
 }
 
 // Enqueues the three kernels of one batch; events (optional) are recorded after init and splat.
-cudaError_t launch_batch(isti::FrameParams &p, int mode, cudaStream_t stream, cudaEvent_t after_init, cudaEvent_t after_splat)
+cudaError_t launch_batch(isti::FrameParams &p, int mode, cudaStream_t stream, cudaEvent_t after_init, cudaEvent_t after_splat,
+                         ReprojChoice choice)
 {
     uint32_t max_w = 0, max_h = 0;
     for (int k = 0; k < p.n_views; k++)
@@ -376,17 +425,90 @@ cudaError_t launch_batch(isti::FrameParams &p, int mode, cudaStream_t stream, cu
     isti::splat_kernel<<<gs, dim3(32, 8), 0, stream>>>(p);
     if (after_splat)
         cudaEventRecord(after_splat, stream);
-    switch (mode)
+    return launch_reproj_mode(p, mode, stream, choice);
+}
+
+bool has_shadows(const isti::FrameParams &p)
+{
+    for (int k = 0; k < p.n_views; k++)
+        if (p.v[k].shi != nullptr)
+            return true;
+    return false;
+}
+
+isti_tuning *find_tuning(isti_renderer *r, int mode, const isti::FrameParams &p)
+{
+    const int32_t sh = has_shadows(p) ? 1 : 0;
+    for (isti_tuning &t : r->tuned)
+        if (t.mode == mode && t.n_views == p.n_views && t.n_frames == p.n_frames && t.shadows == sh && t.width == p.out_w &&
+            t.height == p.out_h)
+            return &t;
+    return nullptr;
+}
+
+// Times every candidate launch of the reprojection of the batch just enqueued (same inputs,
+// same outputs: each run rewrites them identically) and records the fastest for its shape
+// class.  One untimed launch per candidate first (module loading), then REPEAT timed ones.
+isti_status tune_reproj(isti_renderer *r, int mode, cudaStream_t stream)
+{
+    constexpr int REPEAT = 3;
+    isti::FrameParams &p = r->last;
+    std::vector<ReprojChoice> cands;
+    for (int regs : mode_regs(mode))
+        for (int np = 1; np <= 3; np++)
+            cands.push_back({regs, np});
+    const ReprojChoice rule{rule_regs(mode_window(mode), p.n_views), rule_row_pairs(p.n_views, p.n_frames)};
+    std::vector<cudaEvent_t> ev(2 * cands.size(), nullptr);
+    cudaError_t e = cudaSuccess;
+    for (cudaEvent_t &x : ev)
+        if (e == cudaSuccess)
+            e = cudaEventCreate(&x);
+    for (size_t i = 0; i < cands.size() && e == cudaSuccess; i++)
     {
-    case ISTI_MODE_OURS:
-    case ISTI_MODE_BACKWARD_UNIDIRECTIONAL:
-        return launch_reproj<1, 3, false>(p, stream);
-    case ISTI_MODE_SPLATTING:
-        return launch_reproj<1, 0, false>(p, stream);
-    case ISTI_MODE_BACKWARD_BIDIRECTIONAL:
-        return launch_reproj<3, 5, true>(p, stream);
+        e = launch_reproj_mode(p, mode, stream, cands[i]);
+        if (e == cudaSuccess)
+            e = cudaEventRecord(ev[2 * i], stream);
+        for (int k = 0; k < REPEAT && e == cudaSuccess; k++)
+            e = launch_reproj_mode(p, mode, stream, cands[i]);
+        if (e == cudaSuccess)
+            e = cudaEventRecord(ev[2 * i + 1], stream);
     }
-    return cudaGetLastError();
+    // leave the renderer's parameters as its chosen launch sets them
+    if (e == cudaSuccess)
+        e = cudaEventSynchronize(ev.back());
+    float best_ms = 0.0f, rule_ms = 0.0f;
+    size_t best = 0;
+    for (size_t i = 0; i < cands.size() && e == cudaSuccess; i++)
+    {
+        float ms = 0.0f;
+        e = cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]);
+        ms /= REPEAT;
+        if (i == 0 || ms < best_ms)
+        {
+            best_ms = ms;
+            best = i;
+        }
+        if (cands[i].regs == rule.regs && cands[i].row_pairs == rule.row_pairs)
+            rule_ms = ms;
+    }
+    for (cudaEvent_t x : ev)
+        if (x)
+            cudaEventDestroy(x);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "autotuning the reprojection");
+    isti_tuning t{};
+    t.mode = mode;
+    t.n_views = p.n_views;
+    t.n_frames = p.n_frames;
+    t.shadows = has_shadows(p) ? 1 : 0;
+    t.width = p.out_w;
+    t.height = p.out_h;
+    t.regs = cands[best].regs;
+    t.row_pairs = cands[best].row_pairs;
+    t.best_ms = best_ms;
+    t.rule_ms = rule_ms;
+    r->tuned.push_back(t);
+    return ISTI_OK;
 }
 
 isti_status render_batch(isti_renderer *r, int n_frames, void *const *outs, const isti_render_info *infos, const isti_frame_data *frame,
@@ -446,13 +568,26 @@ isti_status render_batch(isti_renderer *r, int n_frames, void *const *outs, cons
         r->timed_launches += 3;
         cudaEventRecord(ev[0], stream);
     }
+    ReprojChoice choice{};
+    const isti_tuning *tuned = timewarp ? nullptr : find_tuning(r, infos[0].mode, r->last);
+    if (tuned)
+        choice = {tuned->regs, tuned->row_pairs};
     e = timewarp ? launch_timewarp(r->last, base, stream, ev ? ev[1] : nullptr, ev ? ev[2] : nullptr)
-                 : launch_batch(r->last, infos[0].mode, stream, ev ? ev[1] : nullptr, ev ? ev[2] : nullptr);
+                 : launch_batch(r->last, infos[0].mode, stream, ev ? ev[1] : nullptr, ev ? ev[2] : nullptr, choice);
     if (ev)
         cudaEventRecord(ev[3], stream);
     if (e != cudaSuccess)
         return cuda_fail(e, "kernel launch");
     r->has_frame = true;
+    if (r->autotune && !timewarp && !tuned)
+    {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        e = cudaStreamIsCapturing(stream, &cs);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaStreamIsCapturing");
+        if (cs == cudaStreamCaptureStatusNone) // no tuning inside a capture: the class keeps the rule until an uncaptured call
+            return tune_reproj(r, infos[0].mode, stream);
+    }
     return ISTI_OK;
 }
 } // namespace
@@ -578,6 +713,32 @@ isti_status isti_renderer_timing(isti_renderer *r, isti_timing *out)
     return ISTI_OK;
 }
 
+isti_status isti_renderer_set_autotune(isti_renderer *r, int32_t on)
+{
+    if (!r)
+        return fail(ISTI_ERR_INVALID_ARG, "renderer is NULL");
+    r->autotune = on != 0;
+    return ISTI_OK;
+}
+
+isti_status isti_renderer_tuning_count(const isti_renderer *r, int32_t *count)
+{
+    if (!r || !count)
+        return fail(ISTI_ERR_INVALID_ARG, "NULL argument");
+    *count = (int32_t)r->tuned.size();
+    return ISTI_OK;
+}
+
+isti_status isti_renderer_tuning(const isti_renderer *r, int32_t index, isti_tuning *out)
+{
+    if (!r || !out)
+        return fail(ISTI_ERR_INVALID_ARG, "NULL argument");
+    if (index < 0 || (size_t)index >= r->tuned.size())
+        return fail(ISTI_ERR_INVALID_ARG, "no tuned shape class with this index");
+    *out = r->tuned[(size_t)index];
+    return ISTI_OK;
+}
+
 isti_status isti_renderer_view_buffers(const isti_renderer *r, int32_t view, const uint64_t **splat, const float **cam_ff,
                                        const float **full_ff, uint32_t *width, uint32_t *height)
 {
@@ -671,7 +832,7 @@ extern "C" isti_status isti_render_noalloc(void *out_rgba, const isti_render_inf
     // the reference's empty value (all bytes 0xfe), the tables and the status word; the
     // flow fields are fully rewritten by the splat kernel before the reprojection reads them.
     e = info->mode == ISTI_MODE_TIMEWARP ? launch_timewarp(p, base, static_cast<cudaStream_t>(stream_ptr), nullptr, nullptr)
-                                         : launch_batch(p, info->mode, static_cast<cudaStream_t>(stream_ptr), nullptr, nullptr);
+                                         : launch_batch(p, info->mode, static_cast<cudaStream_t>(stream_ptr), nullptr, nullptr, ReprojChoice{});
     if (e != cudaSuccess)
         return cuda_fail(e, "kernel launch");
     return ISTI_OK;

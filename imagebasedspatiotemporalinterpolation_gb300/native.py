@@ -64,6 +64,12 @@ class IstiTiming(C.Structure):
                 ("splat_ms", C.c_float), ("reproj_ms", C.c_float)]
 
 
+class IstiTuning(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("n_views", C.c_int32), ("n_frames", C.c_int32), ("shadows", C.c_int32),
+                ("width", C.c_uint32), ("height", C.c_uint32), ("regs", C.c_int32), ("row_pairs", C.c_int32),
+                ("best_ms", C.c_float), ("rule_ms", C.c_float)]
+
+
 # Every function include/isti.h declares: name -> (restype, argtypes)
 SIGNATURES = {
     "isti_abi_version": (C.c_int32, []),
@@ -77,6 +83,9 @@ SIGNATURES = {
     "isti_renderer_device_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "isti_renderer_enable_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "isti_renderer_timing": (C.c_int, [C.c_void_p, C.POINTER(IstiTiming)]),
+    "isti_renderer_set_autotune": (C.c_int, [C.c_void_p, C.c_int32]),
+    "isti_renderer_tuning_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "isti_renderer_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(IstiTuning)]),
     "isti_render_noalloc": (C.c_int, [C.c_void_p, C.POINTER(IstiRenderInfo), C.POINTER(IstiFrameData), C.c_void_p]),
     "isti_render_batch": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(IstiRenderInfo),
                                     C.POINTER(IstiFrameData), C.c_int32, C.c_void_p]),

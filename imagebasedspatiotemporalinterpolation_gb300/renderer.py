@@ -207,6 +207,22 @@ class Renderer:
         return {"frames": t.frames, "kernel_launches": t.kernel_launches, "init_ms": t.init_ms,
                 "splat_ms": t.splat_ms, "reproj_ms": t.reproj_ms}
 
+    def set_autotune(self, on: bool = True) -> None:
+        """isti_renderer_set_autotune: the first uncaptured render of each shape class times
+        the reprojection's candidate launches and later renders use the fastest."""
+        check(self._lib.isti_renderer_set_autotune(self._h, int(on)))
+
+    def tuning(self) -> list:
+        """The tuned shape classes and their chosen launches (isti_renderer_tuning)."""
+        n = C.c_int32()
+        check(self._lib.isti_renderer_tuning_count(self._h, C.byref(n)))
+        out = []
+        for i in range(n.value):
+            t = native.IstiTuning()
+            check(self._lib.isti_renderer_tuning(self._h, i, C.byref(t)))
+            out.append({k: getattr(t, k) for k, _ in native.IstiTuning._fields_})
+        return out
+
     def view_buffers(self, view: int):
         """(splat keys as int64 bit patterns (H, W), cam_ff f32 (H, W, 4), full_ff f32 (H, W, 4)) of the
         last render, as copies."""

@@ -182,6 +182,29 @@ isti_status isti_renderer_enable_timing(isti_renderer *r, int32_t on);
 /* Waits for the recorded events, returns the sums and resets them. */
 isti_status isti_renderer_timing(isti_renderer *r, isti_timing *out);
 
+/* Autotuning of the reprojection launch (no counterpart in the reference, which has one
+ * launch shape).  With autotuning on, the first uncaptured render of each shape class
+ * (mode, source views, frames per call, render size, shadows present) also times every
+ * candidate launch of its reprojection -- register cap x output row pairs per block --
+ * on the call's stream, waits for them (one host synchronisation per class), and the
+ * class's later renders, captured ones included, use the fastest.  Every candidate
+ * computes the same result and the reprojection rewrites its outputs identically when
+ * repeated, so the output does not depend on the choice.  Off (the default): a fixed
+ * rule measured on GB300 at 1080p. */
+isti_status isti_renderer_set_autotune(isti_renderer *r, int32_t on);
+
+typedef struct isti_tuning
+{
+    int32_t mode, n_views, n_frames, shadows; /* the shape class */
+    uint32_t width, height;
+    int32_t regs, row_pairs;                  /* the chosen launch: register cap, output row pairs per block */
+    float best_ms, rule_ms;                   /* reprojection time of the choice and of the fixed rule */
+} isti_tuning;
+
+/* Number of tuned shape classes, and the index-th of them (0-based, in tuning order). */
+isti_status isti_renderer_tuning_count(const isti_renderer *r, int32_t *count);
+isti_status isti_renderer_tuning(const isti_renderer *r, int32_t index, isti_tuning *out);
+
 /* Render without allocating (no counterpart in the reference, whose Renderer
  * always allocates its own buffers).
  *

@@ -337,3 +337,43 @@ def test_nonfinite_inputs_render_without_fault(cuda, mode):
     torch.cuda.synchronize()
     assert r.device_status() == 0
     r.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [(160, 90, (-0.3, 0.3), True, 0, 1), (160, 90, (), False, 0, 6), (128, 72, (0.3,), True, 1, 3),
+                                  (96, 54, (), False, 3, 2)], ids=["6v-shadows-1f", "2v-6f", "mode1-4v-3f", "mode3-2v-2f"])
+def test_autotuned_renders_equal_the_rule_and_the_oracle(cuda, case):
+    """With autotuning on, the first render of a shape class also times every candidate
+    reprojection launch (register cap x row pairs); that render and the later ones, with
+    the chosen launch, equal the fixed-rule renderer and the oracle bit for bit."""
+    import torch
+    w, h, aux, sh, mode, nf = case
+    seq = Sequence(w, h, 2, seed=4100 + w + nf, aux_offsets=aux, shadows=sh, max_speed=2.0)
+    frame = seq.frame(0)
+    dev = DeviceFrame.from_host(frame)
+    clients = [seq.client(0, b % 4, mode=mode, alpha=(b + 1) / (nf + 1)) for b in range(nf)]
+    g = torch.Generator().manual_seed(w * nf)
+    prev = torch.randint(0, 256, (h, w, 4), dtype=torch.uint8, generator=g).cuda()
+    tuned, rule = Renderer(), Renderer()
+    tuned.set_autotune(True)
+    for rep in range(2):   # the tuning call, then a call with the chosen launch
+        a = [prev.clone()] + [torch.zeros_like(prev) for _ in clients[1:]]
+        b = [prev.clone()] + [torch.zeros_like(prev) for _ in clients[1:]]
+        tuned.render_batch(a, clients, dev, chain=True)
+        rule.render_batch(b, clients, dev, chain=True)
+        torch.cuda.synchronize()
+        for k in range(nf):
+            assert torch.equal(a[k], b[k]), f"call {rep}, frame {k}: the tuned launch differs from the rule"
+        for v in range(len(dev.views())):
+            assert torch.equal(tuned.view_buffers(v)[0], rule.view_buffers(v)[0])
+    t = tuned.tuning()
+    assert len(t) == 1
+    t = t[0]
+    assert (t["mode"], t["n_views"], t["n_frames"], t["shadows"], t["width"], t["height"]) == (mode, len(dev.views()), nf, int(sh), w, h)
+    assert t["regs"] in ((40, 48) if mode != 1 else (56,)) and 1 <= t["row_pairs"] <= 3
+    assert 0 < t["best_ms"] <= t["rule_ms"]
+    # the first frame against the oracle
+    exp = oracle.run_oracle(frame, clients[0], prev.cpu().numpy(), with_intermediates=False)[0]
+    np.testing.assert_array_equal(a[0].cpu().numpy(), exp)
+    tuned.close()
+    rule.close()
