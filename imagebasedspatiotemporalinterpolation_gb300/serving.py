@@ -153,7 +153,7 @@ class Server:
         self._pair_refs: dict[tuple[int, int], int] = collections.Counter()  # (cid, seq) -> waiting requests
         self._rid = 0
         self._bid = 0
-        self.latencies: list[float] = []
+        self.latencies: collections.deque = collections.deque(maxlen=1 << 20)   # the latest requests' latencies (ms)
         self.pixels_done = 0
         self.requests_done = 0
         self.batches = 0
@@ -303,6 +303,8 @@ class Server:
             b.outs[-1].after = [consumed]   # the new chain head; freed by the eye's next batch
             eye.busy = False
             b.pair.running -= 1
+            if b.pair.last_use and b.done in b.pair.last_use:
+                b.pair.last_use.remove(b.done)   # finished: a later upload need not wait for it
             self.running[si] = None
             self.t_last = now
             n += 1

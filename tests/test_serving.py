@@ -281,3 +281,12 @@ def test_percentile():
     assert percentile([3.0], 99) == 3.0
     assert percentile([1.0, 2.0, 3.0, 4.0], 50) == 2.5
     assert percentile(list(range(101)), 99) == 99.0
+
+
+def test_pair_slot_keeps_only_running_readers():
+    """A client whose keyframes stop arriving: its pair slot remembers only the batches
+    still running on it (the events a later upload has to wait for), not every batch."""
+    server, _, _, _ = run_mix(11, n_clients=1, n_slots=2, push_p=0.0, submit_p=0.9, steps=300)
+    c = server.clients[0]
+    assert server.batches > 100
+    assert all(len(s.last_use or []) <= len(server.slots) for s in c.slots)
