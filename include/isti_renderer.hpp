@@ -387,6 +387,15 @@ public:
     isti_status last_status() const { return _status; }
     isti_renderer *handle() { return _r; }
 
+    // isti_renderer_set_autotune (no counterpart in the reference): the first uncaptured
+    // render of each shape class times the reprojection's candidate launches; the output
+    // does not depend on it.
+    void setAutotune(bool on)
+    {
+        if (_r)
+            report(isti_renderer_set_autotune(_r, on ? 1 : 0), "Renderer::setAutotune");
+    }
+
 private:
     void report(isti_status s, const char *what, const char *msg = nullptr)
     {

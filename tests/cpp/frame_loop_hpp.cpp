@@ -76,6 +76,7 @@ int main(int argc, char **argv)
         frame_data.resize(make_uint2(W, H), aux_res, aux_prio);
 
         Renderer renderer;
+        renderer.setAutotune(true); // the frames must not depend on it
         ImageBuffer<uchar4, 4> render_buffer(make_uint2(W, H));
         render_buffer.memsetBuffer(make_uchar4(uint8_t(fill[0]), uint8_t(fill[1]), uint8_t(fill[2]), uint8_t(fill[3])));
 
