@@ -46,7 +46,7 @@ def test_struct_layout_matches_header(built, tmp_path):
     structs = {"isti_view": native.IstiView, "isti_frame_data": native.IstiFrameData,
                "isti_render_info": native.IstiRenderInfo, "isti_timing": native.IstiTiming,
                "isti_camera_info": native.IstiCameraInfo, "isti_camera_frame": native.IstiCameraFrame,
-               "isti_quality": native.IstiQuality}
+               "isti_quality": native.IstiQuality, "isti_tuning": native.IstiTuning}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "isti.h"', '#include "isti_dataset.h"',
              '#include "isti_metrics.h"', "int main(void){"]
     for cname, cls in structs.items():
@@ -73,6 +73,9 @@ def test_argument_validation_without_device(built):
     assert b"NULL" in lib.isti_last_error()
     assert lib.isti_renderer_destroy(None) == native.ISTI_OK
     assert lib.isti_renderer_view_buffers(None, 0, None, None, None, None, None) == native.ISTI_ERR_INVALID_ARG
+    assert lib.isti_renderer_set_autotune(None, 1) == native.ISTI_ERR_INVALID_ARG
+    assert lib.isti_renderer_tuning_count(None, None) == native.ISTI_ERR_INVALID_ARG
+    assert lib.isti_renderer_tuning(None, 0, None) == native.ISTI_ERR_INVALID_ARG
 
 
 def test_missing_library_fails_loudly(tmp_path):
