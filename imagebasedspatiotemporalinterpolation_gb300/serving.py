@@ -23,8 +23,10 @@ Continuous batching: whenever a slot is free, the eye with the oldest waiting re
 (among eyes with no batch in flight whose pair is uploaded) takes it; up to `max_batch`
 of that eye's waiting requests on the same pair are rendered by one chained
 isti_render_batch call on the slot's stream, the first output starting as a copy of
-the eye's previous output.  Batches of different clients overlap on the device (one
-stream per slot).  A new keyframe pair is uploaded into the client's older pair slot
+the eye's previous output.  When several eyes of that client are ready on the same pair
+(a stereo request), their next frames share one unchained call instead, each output
+starting as a copy of its own eye's previous output: one splat of the keyframe pair for
+both eyes.  Batches of different clients overlap on the device (one stream per slot).  A new keyframe pair is uploaded into the client's older pair slot
 once no waiting or running request uses that slot's pair; the upload waits for the
 last batch that read the slot, and batches on the new pair wait for the upload (CUDA
 events, no host blocking).
@@ -106,10 +108,8 @@ class _Batch:
     bid: int
     slot: int
     client: _Client
-    eye: int
+    parts: list               # (eye index, its requests, its output buffers) in render order
     pair: _PairSlot
-    requests: list
-    outs: list
     done: object              # event
 
 
@@ -130,7 +130,8 @@ class Server:
     """Continuous-batching request loop over one backend (see the module docstring)."""
 
     def __init__(self, backend, hbm_budget: int, n_slots: int = 4, max_batch: int = 8, out_ring: int | None = None,
-                 slot_pixels: int = 2064 * 2208, slot_views: int = 2, clock=time.perf_counter, on_complete=None):
+                 slot_pixels: int = 2064 * 2208, slot_views: int = 2, clock=time.perf_counter, on_complete=None,
+                 multi_eye: bool = True):
         if n_slots < 1 or not 1 <= max_batch <= backend.max_batch:
             raise ValueError(f"need n_slots >= 1 and 1 <= max_batch <= {backend.max_batch}")
         self.be = backend
@@ -141,6 +142,7 @@ class Server:
             raise ValueError("out_ring must hold a full batch beside the eye's previous output")
         self.clock = clock
         self.on_complete = on_complete
+        self.multi_eye = multi_eye
         self.slot_bytes = backend.slot_bytes(slot_pixels, slot_views, max_batch)
         self.reserved = n_slots * self.slot_bytes
         if self.reserved > self.budget:
@@ -286,22 +288,24 @@ class Server:
                 continue
             now = self.clock()
             c = b.client
-            eye = c.eyes[b.eye]
-            for r, o in zip(b.requests, b.outs):
-                r.t_done = now
-                r.out = o.buf
-                if self.on_complete is not None:
-                    self.on_complete(r)
-                r.out = None
-                self.latencies.append(r.latency_ms)
-                self.pixels_done += r.pixels
-                self.requests_done += 1
+            for _, reqs, outs in b.parts:
+                for r, o in zip(reqs, outs):
+                    r.t_done = now
+                    r.out = o.buf
+                    if self.on_complete is not None:
+                        self.on_complete(r)
+                    r.out = None
+                    self.latencies.append(r.latency_ms)
+                    self.pixels_done += r.pixels
+                    self.requests_done += 1
             consumed = self.be.consumer_event()
-            for o in b.outs[:-1]:
-                o.after = [consumed]
-                eye.free.append(o)
-            b.outs[-1].after = [consumed]   # the new chain head; freed by the eye's next batch
-            eye.busy = False
+            for ei, _, outs in b.parts:
+                eye = c.eyes[ei]
+                for o in outs[:-1]:
+                    o.after = [consumed]
+                    eye.free.append(o)
+                outs[-1].after = [consumed]   # the eye's new chain head; freed by its next batch
+                eye.busy = False
             b.pair.running -= 1
             if b.pair.last_use and b.done in b.pair.last_use:
                 b.pair.last_use.remove(b.done)   # finished: a later upload need not wait for it
@@ -346,6 +350,10 @@ class Server:
                     best = (r, c, ei, slot)
         return best
 
+    def _ready_eyes(self, c: _Client, pslot: _PairSlot) -> list:
+        return [ei for ei, e in enumerate(c.eyes)
+                if not e.busy and e.free and e.waiting and e.waiting[0].pair_seq == pslot.seq]
+
     def _launch(self) -> int:
         n = 0
         for si in range(len(self.slots)):
@@ -355,35 +363,51 @@ class Server:
             if pick is None:
                 break
             _, c, ei, pslot = pick
-            e = c.eyes[ei]
-            k = min(self.max_batch, len(e.free))
-            reqs = []
-            while e.waiting and len(reqs) < k and e.waiting[0].pair_seq == pslot.seq:
-                reqs.append(e.waiting.popleft())
-            outs = [e.free.pop() for _ in reqs]
-            waits = [pslot.ready] + [ev for o in outs for ev in (o.after or [])]
-            head = e.head
-            if head is not None:
-                waits += head.after or []
-            done = self.be.launch(self.slots[si], [o.buf for o in outs], [r.info for r in reqs], pslot.dev,
-                                  head.buf if head is not None else None, waits)
-            for r in reqs:
-                self._pair_refs[(c.cid, r.pair_seq)] -= 1
-                if self._pair_refs[(c.cid, r.pair_seq)] == 0:
-                    del self._pair_refs[(c.cid, r.pair_seq)]
-            if head is not None:
-                head.after = (head.after or []) + [done]   # also read by this batch's chain copy
-                e.free.append(head)
-            e.head = outs[-1]
-            e.busy = True
+            ready = self._ready_eyes(c, pslot)[:self.max_batch] if self.multi_eye else [ei]
+            if len(ready) > 1:
+                # the next frame of every ready eye in one unchained call: each output
+                # starts as a copy of its own eye's previous output
+                takes, chain = [(x, 1) for x in ready], False
+            else:
+                e = c.eyes[ei]
+                k, m = min(self.max_batch, len(e.free)), 0
+                for r in e.waiting:
+                    if m >= k or r.pair_seq != pslot.seq:
+                        break
+                    m += 1
+                takes, chain = [(ei, m)], True
+            parts, infos, bufs, prefill, waits = [], [], [], [], [pslot.ready]
+            for x, m in takes:
+                e = c.eyes[x]
+                reqs = [e.waiting.popleft() for _ in range(m)]
+                outs = [e.free.pop() for _ in reqs]
+                for o in outs:
+                    waits += o.after or []
+                if e.head is not None:
+                    waits += e.head.after or []
+                    prefill.append((len(bufs), e.head.buf))
+                parts.append((x, reqs, outs))
+                infos += [r.info for r in reqs]
+                bufs += [o.buf for o in outs]
+            done = self.be.launch(self.slots[si], bufs, infos, pslot.dev, prefill, chain, waits)
+            self._bid += 1
+            for x, reqs, outs in parts:
+                e = c.eyes[x]
+                for r in reqs:
+                    r.batch = self._bid
+                    self._pair_refs[(c.cid, r.pair_seq)] -= 1
+                    if self._pair_refs[(c.cid, r.pair_seq)] == 0:
+                        del self._pair_refs[(c.cid, r.pair_seq)]
+                if e.head is not None:
+                    e.head.after = (e.head.after or []) + [done]   # also read by this batch's copy
+                    e.free.append(e.head)
+                e.head = outs[-1]
+                e.busy = True
             pslot.running += 1
             pslot.last_use = (pslot.last_use or []) + [done]
-            self._bid += 1
-            for r in reqs:
-                r.batch = self._bid
-            self.running[si] = _Batch(self._bid, si, c, ei, pslot, reqs, outs, done)
+            self.running[si] = _Batch(self._bid, si, c, parts, pslot, done)
             self.batches += 1
-            self.frames_in_batches += len(reqs)
+            self.frames_in_batches += len(bufs)
             n += 1
         return n
 
@@ -490,14 +514,16 @@ class CudaBackend:
         ev.record(s)
         return ev
 
-    def launch(self, slot, outs, infos, dev_pair, chain_from, waits):
+    def launch(self, slot, outs, infos, dev_pair, prefill, chain, waits):
+        """Renders infos into outs (chained or not) after copying each (index, buffer) of
+        `prefill` into outs[index]."""
         torch = self.torch
         stream, renderer = slot
         self._wait(stream, waits)
         with torch.cuda.stream(stream):
-            if chain_from is not None:
-                outs[0].copy_(chain_from, non_blocking=True)
-            renderer.render_batch(outs, infos, dev_pair, chain=True, stream=stream)
+            for i, src in prefill:
+                outs[i].copy_(src, non_blocking=True)
+            renderer.render_batch(outs, infos, dev_pair, chain=chain, stream=stream)
         ev = torch.cuda.Event()
         ev.record(stream)
         return ev

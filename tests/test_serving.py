@@ -99,20 +99,28 @@ class FakeBackend:
             dev.content = host.content
         return self._enqueue(self.upload_stream, waits, run)
 
-    def launch(self, slot, outs, infos, dev, chain_from, waits):
-        self.launch_log.append((len(outs), tuple(i[0] for i in infos), tuple(i[2] for i in infos)))
-        tag = infos[0][1]
-        assert self.in_flight[tag] == 0, "two batches of one eye in flight"
-        self.in_flight[tag] += 1
+    def launch(self, slot, outs, infos, dev, prefill, chain, waits):
+        self.launch_log.append((len(outs), tuple(i[0] for i in infos), tuple(i[2] for i in infos), chain,
+                                tuple(i[1] for i in infos)))
+        tags = set(i[1] for i in infos)
+        assert chain or len(tags) == len(infos), "an unchained batch holds two frames of one eye"
+        assert not chain or len(tags) == 1, "a chained batch mixes eyes"
+        for tag in tags:
+            assert self.in_flight[tag] == 0, "two batches of one eye in flight"
+            self.in_flight[tag] += 1
 
         def run():
             assert dev.content is not None, "batch ran before its pair was uploaded"
-            prev = chain_from.v if chain_from is not None else outs[0].v
+            for i, src in prefill:
+                outs[i].v = src.v
+            prev = outs[0].v
             for o, info in zip(outs, infos):
                 assert info[2] == dev.content, "batch ran on a pair slot that held another pair"
-                prev = fold(prev, info[0], dev.content)
+                base = prev if chain else o.v
+                prev = fold(base, info[0], dev.content)
                 o.v = prev
-            self.in_flight[tag] -= 1
+            for tag in tags:
+                self.in_flight[tag] -= 1
         return self._enqueue(slot, waits, run)
 
     def _runnable(self):
@@ -154,12 +162,12 @@ class Clock:
 
 
 def run_mix(seed, n_clients=4, n_eyes=2, n_slots=3, max_batch=4, steps=600, push_p=0.03, submit_p=0.5, out_ring=None,
-            max_advance=3):
+            max_advance=3, multi_eye=True):
     rng = random.Random(seed)
     be = FakeBackend(rng, max_advance)
     results = {}
     server = Server(be, hbm_budget=10**12, n_slots=n_slots, max_batch=max_batch, out_ring=out_ring, slot_pixels=64 * 36,
-                    clock=Clock(), on_complete=lambda r: results.__setitem__(r.rid, r.out.v))
+                    clock=Clock(), on_complete=lambda r: results.__setitem__(r.rid, r.out.v), multi_eye=multi_eye)
     pair_content = {}
     submitted = collections.defaultdict(list)     # (cid, eye) -> [(rid, info value, pair content)]
     next_content = 1
@@ -185,9 +193,10 @@ def run_mix(seed, n_clients=4, n_eyes=2, n_slots=3, max_batch=4, steps=600, push
     return server, be, results, submitted
 
 
+@pytest.mark.parametrize("multi_eye", [True, False], ids=["stereo-batches", "eye-batches"])
 @pytest.mark.parametrize("seed", range(8))
-def test_results_equal_sequential_renders_in_any_device_order(seed):
-    server, be, results, submitted = run_mix(seed)
+def test_results_equal_sequential_renders_in_any_device_order(seed, multi_eye):
+    server, be, results, submitted = run_mix(seed, n_eyes=2 + seed % 2, multi_eye=multi_eye)
     n = 0
     for key, reqs in submitted.items():
         prev = 0
@@ -217,10 +226,11 @@ def test_keyframe_pairs_replaced_under_load(seed):
 def test_batches_respect_size_and_pair_limits():
     server, be, _, _ = run_mix(3, n_clients=2, max_batch=3, submit_p=0.9, push_p=0.05, steps=800)
     assert be.launch_log
-    for size, _, pairs in be.launch_log:
+    for size, _, pairs, _, _ in be.launch_log:
         assert 1 <= size <= 3
         assert len(set(pairs)) == 1, "a batch mixed keyframe pairs"
-    assert any(size > 1 for size, _, _ in be.launch_log), "no request was ever batched"
+    assert any(size > 1 and chain for size, _, _, chain, _ in be.launch_log), "no eye's frames were ever batched"
+    assert any(not chain for _, _, _, chain, _ in be.launch_log), "no stereo batch"
 
 
 def test_small_output_ring_applies_backpressure():
