@@ -188,7 +188,11 @@ class Server:
     def close_client(self, cid: int) -> None:
         """The client leaves once its waiting and running requests are done."""
         if cid in self.clients:
-            self.clients[cid].closing = True
+            c = self.clients[cid]
+            c.closing = True
+            if not any(e.waiting or e.busy for e in c.eyes):
+                self._release(c)
+                self._admit()
         else:
             self.admit_queue = collections.deque(q for q in self.admit_queue if q[0] != cid)
             self.waiting_pairs.pop(cid, None)

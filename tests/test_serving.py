@@ -300,3 +300,17 @@ def test_pair_slot_keeps_only_running_readers():
     c = server.clients[0]
     assert server.batches > 100
     assert all(len(s.last_use or []) <= len(server.slots) for s in c.slots)
+
+
+def test_closing_an_idle_client_frees_its_budget_at_once():
+    be = FakeBackend(random.Random(2))
+    slot = FakeBackend.slot_bytes(64 * 36, 2, 2)
+    need = 2 * 5000 + 2 * 5 * 64 * 36 * 4
+    server = Server(be, hbm_budget=slot + need, n_slots=1, max_batch=2, slot_pixels=64 * 36, clock=Clock())
+    assert server.open_client(0, 64, 36, 2, Pair(5000))
+    assert not server.open_client(1, 64, 36, 2, Pair(5000))
+    server.close_client(0)                 # nothing waiting or running
+    assert not server.admitted(0) and server.admitted(1)
+    assert server.reserved == slot + need
+    server.close_client(1)
+    assert server.reserved == slot and not server.clients
