@@ -246,6 +246,8 @@ class Server:
         c = self.clients.get(cid)
         if c is None:
             raise KeyError(f"client {cid} is not admitted")
+        if c.closing:
+            raise ValueError(f"client {cid} is closing")
         if c.newest < 0:
             raise ValueError(f"client {cid} has no keyframe pair yet")
         if not 0 <= eye < len(c.eyes):
