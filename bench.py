@@ -55,7 +55,7 @@ WORKLOAD = "1080p interpolation, 3 cameras (main + aux +-0.3 m), soft shadows, t
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=34)   # 102 timed frames (3 per step)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--pairs", type=int, default=5)
