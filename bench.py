@@ -19,9 +19,10 @@ value: device-resident throughput (CUDA events on the rendering stream).
 e2e:   the same metric through the C ABI with host buffers: each step
        uploads the newly arrived keyframe data from pinned host memory
        (colour, z, motion and shadow images of the new keyframe for the 3
-       cameras, plus the earlier keyframe's forward motion and shadows; the
-       shadow images as RGB, expanded to RGBA on the device, since their alpha
-       is never read) and reads the 3 output frames back.
+       cameras, plus the earlier keyframe's forward motion and shadows; colour
+       and shadow images as RGB, expanded to RGBA on the device: the shadow
+       images' alpha is never read and the colour comes from opaque RGB sources)
+       and reads the 3 output frames back.
 
 --impl reference times the reference's per-frame algorithm on the host
 cores (the C oracle, OpenMP over all threads: the reference has no CPU
@@ -602,25 +603,26 @@ def run_e2e(args, seq, res, clients, r, dev, world):
     P = args.pairs
     n_cams = 1 + len(AUX)
     # Slab layout of one keyframe: [arrival part | forward part], each grouped by image kind
-    # over the cameras.  arrival = colour, z, backward motion, backward shadow A/B/Info;
-    # forward = forward motion, forward shadows.  Shadow images travel as packed RGB (the
-    # renderer never reads their alpha) and are expanded to RGBA on the device after upload
-    # (isti_rgb8_to_rgba8), one launch per part.
-    rgba, zb, mot, rgb = H * W * 4, H * W * 4, H * W * 6, H * W * 3   # each a multiple of 256 bytes
+    # over the cameras.  arrival = colour, backward shadow A/B/Info, z, backward motion;
+    # forward = forward motion, forward shadows.  Colour and shadow images travel as packed
+    # RGB and are expanded to RGBA on the device after upload (isti_rgb8_to_rgba8, one launch
+    # per part): the renderer never reads the shadow images' alpha, and the colour images
+    # come from RGB sources (alpha 255, what an RGB PNG decodes to; asserted below).
+    zb, mot, rgb = H * W * 4, H * W * 6, H * W * 3   # each a multiple of 256 bytes
     layout, off = {}, 0
-    for kind, n in (("color", rgba), ("z", zb), ("mb", mot), ("sb", 3 * rgb), ("mf", mot), ("sf", 3 * rgb)):
+    for kind, n in (("color", rgb), ("sb", 3 * rgb), ("z", zb), ("mb", mot), ("mf", mot), ("sf", 3 * rgb)):
         for c in range(n_cams):
             layout[(kind, c)] = (off, n)
             off += n
     slab_bytes = off
     A = layout[("mf", 0)][0]            # arrival part = [0, A), forward part = [A, slab_bytes)
-    sb_lo, sf_lo = layout[("sb", 0)][0], layout[("sf", 0)][0]
-    n_shadow = n_cams * 3               # shadow images per part
+    sf_lo = layout[("sf", 0)][0]
+    n_arr_rgb, n_fwd_rgb = 4 * n_cams, 3 * n_cams   # RGB images per part, contiguous from 0 / sf_lo
 
     def fields(slab, c):
         """Tensor views of camera c's images inside one slab (host or device)."""
         sl = lambda kind: slab[layout[(kind, c)][0]:layout[(kind, c)][0] + layout[(kind, c)][1]]
-        return dict(color=sl("color").view(H, W, 4), z=sl("z").view(torch.float32).view(H, W),
+        return dict(color=sl("color").view(H, W, 3), z=sl("z").view(torch.float32).view(H, W),
                     mf=sl("mf").view(torch.float16).view(H, W, 3), mb=sl("mb").view(torch.float16).view(H, W, 3),
                     sf=sl("sf").view(3, H, W, 3), sb=sl("sb").view(3, H, W, 3))
 
@@ -629,7 +631,9 @@ def run_e2e(args, seq, res, clients, r, dev, world):
         slab = torch.empty(slab_bytes, dtype=torch.uint8).pin_memory()
         for c in range(n_cams):
             kf, f = seq.keyframe(k, c), fields(slab, c)
-            f["color"].copy_(torch.from_numpy(np.ascontiguousarray(kf.color)))
+            if not (kf.color[..., 3] == 255).all():
+                raise RuntimeError("e2e uploads colour as RGB: the source colour must be opaque")
+            f["color"].copy_(torch.from_numpy(np.ascontiguousarray(kf.color[..., :3])))
             f["z"].copy_(torch.from_numpy(np.ascontiguousarray(kf.z, np.float32)))
             f["mf"].copy_(torch.from_numpy(np.ascontiguousarray(kf.motion_fwd, np.float16)))
             f["mb"].copy_(torch.from_numpy(np.ascontiguousarray(kf.motion_bwd, np.float16)))
@@ -638,21 +642,25 @@ def run_e2e(args, seq, res, clients, r, dev, world):
                 f["sb"][i].copy_(torch.from_numpy(np.ascontiguousarray(kf.shadow_bwd[i][..., :3])))
         host.append(slab)
     ring = [torch.empty(slab_bytes, dtype=torch.uint8, device=dev) for _ in range(P + 1)]
-    # RGBA shadow images the renderer reads, per slot: [backward | forward][camera][A, B, Info]
-    shadow = [torch.empty((2, n_cams, 3, H, W, 4), dtype=torch.uint8, device=dev) for _ in range(P + 1)]
+    # RGBA images the renderer reads, per slot: arrival [colour per camera, then A, B, Info
+    # per camera] and forward [A, B, Info per camera], in the order of the RGB blocks
+    rgba_arr = [torch.empty((n_arr_rgb, H, W, 4), dtype=torch.uint8, device=dev) for _ in range(P + 1)]
+    rgba_fwd = [torch.empty((n_fwd_rgb, H, W, 4), dtype=torch.uint8, device=dev) for _ in range(P + 1)]
     ring_fields = []
-    for s_, sh in zip(ring, shadow):
+    for s_, ra, rf in zip(ring, rgba_arr, rgba_fwd):
         per_cam = []
         for c in range(n_cams):
             f = fields(s_, c)
-            f["sb"], f["sf"] = [sh[0, c, i] for i in range(3)], [sh[1, c, i] for i in range(3)]
+            f["color"] = ra[c]
+            f["sb"] = [ra[n_cams + 3 * c + i] for i in range(3)]
+            f["sf"] = [rf[3 * c + i] for i in range(3)]
             per_cam.append(f)
         ring_fields.append(per_cam)
     lib = native.load()
     outs_dev = [[torch.zeros((H, W, 4), dtype=torch.uint8, device=dev) for _ in TS] for _ in range(2)]
     outs_host = [[torch.empty((H, W, 4), dtype=torch.uint8).pin_memory() for _ in TS] for _ in range(2)]
     up, comp, down = torch.cuda.Stream(dev), torch.cuda.Stream(dev), torch.cuda.Stream(dev)
-    xp = torch.cuda.Stream(dev, priority=-1)   # RGB -> RGBA expansion of the uploaded shadow images
+    xp = torch.cuda.Stream(dev, priority=-1)   # RGB -> RGBA expansion of the uploaded colour and shadow images
     ups = [up, xp]
     ev = lambda: torch.cuda.Event()
     up_done, comp_done, down_done = {}, {}, {}
@@ -681,9 +689,10 @@ def run_e2e(args, seq, res, clients, r, dev, world):
             copied = ev()
             copied.record(up)
             xp.wait_event(copied)
-            src = ring[slot][sb_lo if part == "arr" else sf_lo:][:n_shadow * rgb]
-            dst = shadow[slot][0 if part == "arr" else 1]
-            native.check(lib.isti_rgb8_to_rgba8(dst.data_ptr(), src.data_ptr(), n_shadow * H * W, C.c_void_p(xp.cuda_stream)))
+            n_img = n_arr_rgb if part == "arr" else n_fwd_rgb
+            src = ring[slot][0 if part == "arr" else sf_lo:][:n_img * rgb]
+            dst = rgba_arr[slot] if part == "arr" else rgba_fwd[slot]
+            native.check(lib.isti_rgb8_to_rgba8(dst.data_ptr(), src.data_ptr(), n_img * H * W, C.c_void_p(xp.cuda_stream)))
             if count:
                 counters["h2d"] += hi - lo
                 counters["launches"] += 1
@@ -752,7 +761,7 @@ def run_e2e(args, seq, res, clients, r, dev, world):
     return {"value": round(value, 2), "unit": "Mpix/s", "h2d_bytes_per_step": counters["h2d"] // args.steps,
             "d2h_bytes_per_step": counters["d2h"] // args.steps, "ms_per_step": round(ms / args.steps, 4),
             "expand_launches_per_step": counters["launches"] / args.steps,
-            "pipeline": "one contiguous slab per keyframe, 2 uploads per step (shadow images as RGB, "
+            "pipeline": "one contiguous slab per keyframe, 2 uploads per step (colour and shadow images as RGB, "
                         "expanded to RGBA on the device) / render / read-back overlapped"}
 
 
