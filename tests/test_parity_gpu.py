@@ -377,3 +377,27 @@ def test_autotuned_renders_equal_the_rule_and_the_oracle(cuda, case):
     np.testing.assert_array_equal(a[0].cpu().numpy(), exp)
     tuned.close()
     rule.close()
+
+
+def test_autotuned_unchained_batch_of_eight(cuda):
+    """Autotuning on an unchained batch of the largest size (8 frames, 4 views, shadows):
+    the tuning call and the next one equal the fixed rule frame by frame."""
+    import torch
+    seq = Sequence(144, 80, 2, seed=8080, aux_offsets=(0.3,), shadows=True, max_speed=2.0)
+    dev = DeviceFrame.from_host(seq.frame(0))
+    clients = [seq.client(0, b % 4, alpha=(b + 1) / 9) for b in range(8)]
+    g = torch.Generator().manual_seed(88)
+    prevs = [torch.randint(0, 256, (80, 144, 4), dtype=torch.uint8, generator=g).cuda() for _ in clients]
+    tuned, rule = Renderer(), Renderer()
+    tuned.set_autotune(True)
+    for rep in range(2):
+        a = [p.clone() for p in prevs]
+        b = [p.clone() for p in prevs]
+        tuned.render_batch(a, clients, dev, chain=False)
+        rule.render_batch(b, clients, dev, chain=False)
+        torch.cuda.synchronize()
+        for k in range(8):
+            assert torch.equal(a[k], b[k]), f"call {rep}, frame {k} differs"
+    assert len(tuned.tuning()) == 1 and tuned.tuning()[0]["n_frames"] == 8
+    tuned.close()
+    rule.close()

@@ -93,3 +93,52 @@ def test_simulated_clients_report_latency(cuda):
     assert st["requests"] == st["offered_requests"]
     assert 0 < st["p50_ms"] <= st["p99_ms"] < 1000
     assert st["keyframe_pairs_pushed"] >= 3 * 30 - 3
+
+
+@pytest.mark.gpu
+def test_budget_admission_and_closing_on_the_device(cuda):
+    """A budget that holds the slots and two of the three clients: the third waits, is
+    admitted when the first closes, and every result still equals rendering alone."""
+    import torch
+    clients = make_clients()
+    results = {}
+    be = CudaBackend()
+    slot_px = 132 * 78
+    footprints = []
+    probe = Server(be, hbm_budget=1 << 40, n_slots=1, max_batch=2, slot_pixels=slot_px, slot_views=4)
+    for cid, seq, pairs in clients:
+        footprints.append(probe.footprint(seq.width, seq.height, len(EYES), pairs[0]))
+    del probe
+    # room for clients 0 and 1, or for 1 and 2 (client 0 is the smallest)
+    assert footprints[0] < footprints[2]
+    budget = be.slot_bytes(slot_px, 4, 2) + footprints[1] + footprints[2] + footprints[0] // 2
+    server = Server(be, hbm_budget=budget, n_slots=1, max_batch=2, slot_pixels=slot_px, slot_views=4,
+                    on_complete=lambda r: results.__setitem__(r.rid, r.out.cpu()))
+    admitted = [server.open_client(cid, seq.width, seq.height, len(EYES), pairs[0]) for cid, seq, pairs in clients]
+    assert admitted == [True, True, False]
+    for cid, _, pairs in clients:
+        server.push_pair(cid, pairs[1])          # the waiting client keeps its newest pair
+    log = []
+    for cid, seq, _ in clients[:2]:
+        for eye in range(len(EYES)):
+            r = server.submit(cid, eye, eye_info(seq, 1, 0.5, EYES[eye]))
+            log.append((r.rid, cid, eye, 0.5))
+    server.close_client(0)
+    server.drain()
+    assert server.admitted(2) and not server.admitted(0)
+    assert server.reserved <= server.budget
+    cid, seq, _ = clients[2]
+    for alpha in (0.25, 0.75):
+        for eye in range(len(EYES)):
+            r = server.submit(cid, eye, eye_info(seq, 1, alpha, EYES[eye]))
+            log.append((r.rid, cid, eye, alpha))
+    server.drain()
+    torch.cuda.synchronize()
+    single = Renderer()
+    bufs = {}
+    for rid, cid, eye, alpha in log:
+        seq = clients[cid][1]
+        buf = bufs.setdefault((cid, eye), torch.zeros((seq.height, seq.width, 4), dtype=torch.uint8, device="cuda"))
+        single.render(buf, eye_info(seq, 1, alpha, EYES[eye]), DeviceFrame.from_host(seq.frame(1)))
+        assert torch.equal(buf.cpu(), results[rid]), f"request {rid} differs from rendering it alone"
+    single.close()
