@@ -7,10 +7,11 @@
   _lib/libisti_scene.so  procedural keyframe generator (host C, OpenMP)
 
 Objects are compiled in parallel into _lib/obj/ and linked by nvcc (static
-CUDA runtime).  The interpolation arithmetic is compiled with -fmad=false (no
-multiply-add contraction) and IEEE division / square root, and host code with
--ffp-contract=off, so results do not depend on the compiler's contraction
-choices and match the oracle bit for bit.
+CUDA runtime).  The interpolation arithmetic is compiled twice: with
+-fmad=false (no multiply-add contraction) and IEEE division / square root
+(isti_render.cu, the default mode, bit-exact against the oracle), and with the
+reference's -use_fast_math (isti_render_fm.cu, the reference GPU build's
+arithmetic).  Host code uses -ffp-contract=off.
 """
 from __future__ import annotations
 
@@ -27,7 +28,13 @@ HOST_SRC = os.path.join(CSRC, "host")
 INCLUDE = os.path.join(REPO_DIR, "include")
 
 CUDA_ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CUDA_SOURCES = ["isti_render.cu", "isti_metrics.cu"]
+CUDA_SOURCES = ["isti_render.cu", "isti_render_fm.cu", "isti_metrics.cu", "isti_unet.cu", "isti_flownet.cu", "isti_scene_gpu.cu"]
+# Translation units compiled with the reference's GPU arithmetic (-use_fast_math,
+# the reference's CMakeLists.txt:36) instead of -fmad=false / IEEE division.
+FAST_MATH_SOURCES = {"isti_render_fm.cu"}
+# Translation units with the compiler's default contraction (the learned initialiser:
+# tensor-core GEMMs with f32 accumulation, no bit-exactness contract).
+DEFAULT_MATH_SOURCES = {"isti_unet.cu", "isti_flownet.cu", "isti_scene_gpu.cu"}
 HOST_LIB_SOURCES = ["isti_io.cpp", "isti_dataset.cpp"]
 
 
@@ -57,8 +64,10 @@ def _obj(src: str) -> str:
 
 
 def _cuda_obj_cmd(src: str) -> list[str]:
+    base = os.path.basename(src)
+    arith = ["-use_fast_math"] if base in FAST_MATH_SOURCES else ([] if base in DEFAULT_MATH_SOURCES else ["-fmad=false"])
     return [
-        _nvcc(), "-std=c++20", "-O3", CUDA_ARCH, "-lineinfo", "-fmad=false",
+        _nvcc(), "-std=c++20", "-O3", CUDA_ARCH, "-lineinfo", *arith,
         "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INCLUDE, "-I", CSRC,
         "-c", src, "-o", _obj(src),
     ]

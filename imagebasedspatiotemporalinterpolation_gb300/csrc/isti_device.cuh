@@ -1,14 +1,27 @@
 // Device-side arithmetic of the interpolation path.
 //
 // Every function restates one helper of the reference renderer in the same
-// floating-point operation order; the translation unit is compiled with
-// -fmad=false (no multiply-add contraction) and IEEE division/square root, so
-// each result is bit-identical to the host oracle's.
+// floating-point operation order.  Two arithmetic modes, one per translation unit:
+//
+//  * IEEE (ISTI_FASTMATH = 0, isti_render.cu): compiled with -fmad=false, and the
+//    x-helpers below are the correctly rounded intrinsics, so each result is
+//    bit-identical to the host oracle's (and to the reference's code run on the CPU);
+//  * reference GPU semantics (ISTI_FASTMATH = 1, isti_render_fm.cu): compiled with
+//    the reference's -use_fast_math (CMakeLists.txt:36), the x-helpers are the plain
+//    operators, and every expression keeps the reference's tree, so the compiler
+//    contracts, divides and takes roots the way it does for the reference's own GPU
+//    build.  The exactness shortcuts of the IEEE mode (w / w = 1, quotients decided
+//    by an approximation, squared errors, to_8bit without the division) do not hold
+//    under those semantics and are replaced by the reference's direct expressions.
 #pragma once
 
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#ifndef ISTI_FASTMATH
+#define ISTI_FASTMATH 0
+#endif
 
 namespace isti
 {
@@ -21,6 +34,44 @@ constexpr float EPS_3 = 0.01f;
 constexpr unsigned long long SPLAT_EMPTY = 0xfefefefefefefefeull; // cudaMemset(..., 0xfe) of every byte
 constexpr uint32_t SOFTSHADOW_BITS = 2u;
 constexpr uint32_t SOFTSHADOW_VAL_MASK = 3u;
+constexpr bool FAST_MATH = ISTI_FASTMATH != 0;
+
+// one rounding per operation (IEEE) or the plain operator (reference GPU semantics)
+__device__ __forceinline__ float xadd(float a, float b)
+{
+    if constexpr (FAST_MATH)
+        return a + b;
+    else
+        return __fadd_rn(a, b);
+}
+__device__ __forceinline__ float xsub(float a, float b)
+{
+    if constexpr (FAST_MATH)
+        return a - b;
+    else
+        return __fsub_rn(a, b);
+}
+__device__ __forceinline__ float xmul(float a, float b)
+{
+    if constexpr (FAST_MATH)
+        return a * b;
+    else
+        return __fmul_rn(a, b);
+}
+__device__ __forceinline__ float xdiv(float a, float b)
+{
+    if constexpr (FAST_MATH)
+        return a / b;
+    else
+        return __fdiv_rn(a, b);
+}
+__device__ __forceinline__ float xsqrt(float a)
+{
+    if constexpr (FAST_MATH)
+        return sqrtf(a);
+    else
+        return __fsqrt_rn(a);
+}
 
 struct KeyInfo
 {
@@ -49,8 +100,8 @@ __device__ __forceinline__ float2 pixel2cs(uint32_t px, uint32_t py, uint32_t w,
     float ax = (float)px + 0.5f, ay = (float)py + 0.5f;
     ax = 2.0f * ax;
     ay = 2.0f * ay;
-    ax = __fdiv_rn(ax, (float)w);
-    ay = __fdiv_rn(ay, (float)h);
+    ax = xdiv(ax, (float)w);
+    ay = xdiv(ay, (float)h);
     return make_float2(ax - 1.0f, ay - 1.0f);
 }
 
@@ -78,6 +129,11 @@ __device__ __forceinline__ bool in_range(int2 p, uint32_t w, uint32_t h)
 // approximate quotient lies within 1e-4 (relative) of the bounds.
 __device__ __forceinline__ bool quotient_inside(float n, float d, float lim)
 {
+    if constexpr (FAST_MATH)
+    {
+        const float q = n / d;
+        return q > -lim && q < lim;
+    }
     const float ad = fabsf(d);
     if (ad >= 0x1p-126f && ad <= 0x1p126f)
     {
@@ -87,7 +143,7 @@ __device__ __forceinline__ bool quotient_inside(float n, float d, float lim)
         if (q > lim * 1.0001f)
             return false;
     }
-    const float e = __fdiv_rn(n, d);
+    const float e = xdiv(n, d);
     return e > -lim && e < lim;
 }
 
@@ -95,10 +151,10 @@ __device__ __forceinline__ bool quotient_inside(float n, float d, float lim)
 __device__ __forceinline__ float4 matvec(const float *m, float4 v)
 {
     float4 r;
-    r.x = __fadd_rn(__fadd_rn(__fmul_rn(m[0], v.x), __fmul_rn(m[4], v.y)), __fadd_rn(__fmul_rn(m[8], v.z), __fmul_rn(m[12], v.w)));
-    r.y = __fadd_rn(__fadd_rn(__fmul_rn(m[1], v.x), __fmul_rn(m[5], v.y)), __fadd_rn(__fmul_rn(m[9], v.z), __fmul_rn(m[13], v.w)));
-    r.z = __fadd_rn(__fadd_rn(__fmul_rn(m[2], v.x), __fmul_rn(m[6], v.y)), __fadd_rn(__fmul_rn(m[10], v.z), __fmul_rn(m[14], v.w)));
-    r.w = __fadd_rn(__fadd_rn(__fmul_rn(m[3], v.x), __fmul_rn(m[7], v.y)), __fadd_rn(__fmul_rn(m[11], v.z), __fmul_rn(m[15], v.w)));
+    r.x = xadd(xadd(xmul(m[0], v.x), xmul(m[4], v.y)), xadd(xmul(m[8], v.z), xmul(m[12], v.w)));
+    r.y = xadd(xadd(xmul(m[1], v.x), xmul(m[5], v.y)), xadd(xmul(m[9], v.z), xmul(m[13], v.w)));
+    r.z = xadd(xadd(xmul(m[2], v.x), xmul(m[6], v.y)), xadd(xmul(m[10], v.z), xmul(m[14], v.w)));
+    r.w = xadd(xadd(xmul(m[3], v.x), xmul(m[7], v.y)), xadd(xmul(m[11], v.z), xmul(m[15], v.w)));
     return r;
 }
 
@@ -112,23 +168,23 @@ __device__ __forceinline__ float self_ratio(float w)
 __device__ __forceinline__ float4 project(const float *m, float4 v)
 {
     const float4 p = matvec(m, v);
-    return make_float4(__fdiv_rn(p.x, p.w), __fdiv_rn(p.y, p.w), __fdiv_rn(p.z, p.w), self_ratio(p.w));
+    return make_float4(xdiv(p.x, p.w), xdiv(p.y, p.w), xdiv(p.z, p.w), FAST_MATH ? xdiv(p.w, p.w) : self_ratio(p.w));
 }
 
-__device__ __forceinline__ float z_to_depth(float z) { return __fmul_rn(__fadd_rn(z, 1.0f), 0.5f); } // :89-91
-__device__ __forceinline__ float depth_to_z(float d) { return __fsub_rn(__fmul_rn(d, 2.0f), 1.0f); } // :93-95
+__device__ __forceinline__ float z_to_depth(float z) { return xmul(xadd(z, 1.0f), 0.5f); } // :89-91
+__device__ __forceinline__ float depth_to_z(float d) { return xsub(xmul(d, 2.0f), 1.0f); } // :93-95
 
 // lerp_color, include/util/helper_common.h:22-25: (a + t * (b - a)) / 255
 __device__ __forceinline__ float lerp_ch(uint32_t a, uint32_t b, float t)
 {
     const float fa = (float)a, fb = (float)b;
-    return __fdiv_rn(__fadd_rn(fa, __fmul_rn(t, __fsub_rn(fb, fa))), 255.f);
+    return xdiv(xadd(fa, xmul(t, xsub(fb, fa))), 255.f);
 }
 
 // to_8bit, include/util/helper_common.h:27-30: min(255, max(0, int(f * 255)))
 __device__ __forceinline__ uint32_t to_8bit(float f)
 {
-    const int v = __float2int_rz(__fmul_rn(f, 255.f));
+    const int v = __float2int_rz(xmul(f, 255.f));
     return (uint32_t)min(255, max(0, v));
 }
 
@@ -139,11 +195,13 @@ __device__ __forceinline__ uint32_t to_8bit(float f)
 // the division.
 __device__ __forceinline__ uint32_t to_8bit_255ths(float v)
 {
+    if constexpr (FAST_MATH)
+        return to_8bit(v / 255.f);
     const float fl = floorf(v);
-    const float fr = __fsub_rn(v, fl);
+    const float fr = xsub(v, fl);
     if (v >= 0.0f && v < 256.0f && (fr == 0.0f || (fr > 0x1p-12f && fr < 1.0f - 0x1p-12f)))
         return (uint32_t)fl;
-    return to_8bit(__fdiv_rn(v, 255.f));
+    return to_8bit(xdiv(v, 255.f));
 }
 
 // color_to_uchar4(lerp_color(a, b, t)), packed RGBA8 in a uint32 (R in bits 0-7)
@@ -154,20 +212,22 @@ __device__ __forceinline__ uint32_t lerp_color_u8(uint32_t a, uint32_t b, float 
     for (int c = 0; c < 4; c++)
     {
         const float fa = (float)((a >> (8 * c)) & 255u), fb = (float)((b >> (8 * c)) & 255u);
-        r |= to_8bit_255ths(__fadd_rn(fa, __fmul_rn(t, __fsub_rn(fb, fa)))) << (8 * c);
+        r |= to_8bit_255ths(xadd(fa, xmul(t, xsub(fb, fa)))) << (8 * c);
     }
     return r;
 }
 
-// sqrtf(s) < e, IEEE-exact: the square root is only taken within 0.01 % of e^2
+// sqrtf(s) < e; IEEE-exact mode: the square root is only taken within 0.01 % of e^2
 __device__ __forceinline__ bool sqrt_less(float s, float e)
 {
+    if constexpr (FAST_MATH)
+        return sqrtf(s) < e;
     const float e2 = e * e;
     if (s < e2 * 0.9999f)
         return true;
     if (s > e2 * 1.0001f)
         return false;
-    return __fsqrt_rn(s) < e;
+    return xsqrt(s) < e;
 }
 
 // float -> unsigned char of make_uchar4(float, ...): truncation, saturation, NaN -> 0

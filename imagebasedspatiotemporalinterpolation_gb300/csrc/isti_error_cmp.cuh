@@ -61,7 +61,9 @@ ISTI_EC float err_float(uint32_t u)
 
 ISTI_EC float err_sqrt(float x)
 {
-#ifdef __CUDA_ARCH__
+#if defined(__CUDA_ARCH__) && defined(ISTI_FASTMATH) && ISTI_FASTMATH
+    return sqrtf(x); // the reference's length() under -use_fast_math
+#elif defined(__CUDA_ARCH__)
     return __fsqrt_rn(x);
 #else
     return sqrtf(x);

@@ -100,6 +100,13 @@ struct FrameParams
     int32_t n_views, n_aux, n_frames, linear, chain;
     int32_t use_tma;          // key tiles fetched by TMA (every view's row pitch a multiple of 16 bytes)
     int32_t row_pairs;        // pairs of output rows per reprojection block
+    // Failure-detection test hook: the reprojection block with this linear index
+    // (blockIdx.y * gridDim.x + blockIdx.x) announces its tile bytes but issues no copy,
+    // so its bounded wait runs out after `wait_limit` polls; -1 = none.  0 = default limit.
+    // The host derives the index from an output pixel (withhold_x, withhold_y; -1 = none).
+    int32_t withhold_block;
+    uint32_t wait_limit;
+    int32_t withhold_x, withhold_y;
 };
 
 // One 3-D tensor map per source view over its splat keys: (x, y, frame), u64 elements.
@@ -133,19 +140,21 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, uint32_t 
     return ok != 0;
 }
 
-// Waits for phase `parity` of the barrier with an iteration limit; on timeout the device
-// status word is set and the wait is retried once more with the same limit (the copies
-// may still be landing), then the block carries on.
-__device__ __forceinline__ void mbar_wait_bounded(unsigned long long *bar, uint32_t parity, int32_t *status)
+// Waits for phase `parity` of the barrier with an iteration limit (0: the default of 2^22
+// polls, seconds at most).  On timeout the device status word is set and the wait is
+// retried once more with the same limit (the copies may still be landing).  Returns false
+// when both waits gave up: the tiles are then not to be read.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, uint32_t parity, int32_t *status, uint32_t limit)
 {
-    constexpr uint32_t LIMIT = 1u << 22;
-    for (uint32_t i = 0; i < LIMIT; i++)
+    const uint32_t lim = limit ? limit : (1u << 22);
+    for (uint32_t i = 0; i < lim; i++)
         if (mbar_try_wait(bar, parity))
-            return;
+            return true;
     atomicExch(status, (int32_t)ISTI_ERR_TIMEOUT);
-    for (uint32_t i = 0; i < LIMIT; i++)
+    for (uint32_t i = 0; i < lim; i++)
         if (mbar_try_wait(bar, parity))
-            return;
+            return true;
+    return false;
 }
 
 // 3-D tiled bulk copy global -> shared, completion counted on `bar`.  x * 8 bytes must be a
@@ -235,7 +244,7 @@ __global__ void __launch_bounds__(256, 8) splat_kernel(const __grid_constant__ F
     const float pcx = __ldg(v.lut + x), pcy = __ldg(v.lut + v.w + y); // pixel2CS(idx2D, resolution)
     const float4 cs_from = make_float4(pcx, pcy, z_from, 1.0f);
     const float4 ws_from = project(v.inv_vp, cs_from);
-    const float4 moved = make_float4(__fadd_rn(pcx, om.x), __fadd_rn(pcy, om.y), __fadd_rn(z_from, om.z), 1.0f);
+    const float4 moved = make_float4(xadd(pcx, om.x), xadd(pcy, om.y), xadd(z_from, om.z), 1.0f);
     const float4 ws_to = project(v.inv_vp, moved);
 
     // visible_in_main: WS2CS(posWS_from, viewproj_mat_from_main) inside +-(1 - 1e-3), src/renderer.cu:104-107
@@ -245,10 +254,10 @@ __global__ void __launch_bounds__(256, 8) splat_kernel(const __grid_constant__ F
     const float vis = visible ? 1.0f : 0.0f;
 
     const float4 cs_to = project(v.vp_to, ws_to);
-    const float fmx = __fsub_rn(cs_to.x, cs_from.x), fmy = __fsub_rn(cs_to.y, cs_from.y), fmz = __fsub_rn(cs_to.z, cs_from.z);
+    const float fmx = xsub(cs_to.x, cs_from.x), fmy = xsub(cs_to.y, cs_from.y), fmz = xsub(cs_to.z, cs_from.z);
     v.full_ff[idx] = make_float4(fmx, fmy, fmz, vis);
-    const float4 d_ws = make_float4(__fsub_rn(ws_to.x, ws_from.x), __fsub_rn(ws_to.y, ws_from.y), __fsub_rn(ws_to.z, ws_from.z),
-                                    __fsub_rn(ws_to.w, ws_from.w));
+    const float4 d_ws = make_float4(xsub(ws_to.x, ws_from.x), xsub(ws_to.y, ws_from.y), xsub(ws_to.z, ws_from.z),
+                                    xsub(ws_to.w, ws_from.w));
 
     // client-camera part, per frame.  Unrolled over the batch limit, so the client matrix
     // p.cam_vp[k] is read as constant operands rather than by indexed loads (1080p, 3
@@ -259,15 +268,15 @@ __global__ void __launch_bounds__(256, 8) splat_kernel(const __grid_constant__ F
     {
         if (k >= p.n_frames)
             break;
-        const float wg = v.forward ? p.f[k].alpha : __fsub_rn(1.0f, p.f[k].alpha);
+        const float wg = v.forward ? p.f[k].alpha : xsub(1.0f, p.f[k].alpha);
         unsigned long long *keys = v.splat + k * p.key_stride;
         float4 *cam = v.cam_ff + k * p.cam_stride;
         if (!p.linear)
         {
-            const float4 scaled = make_float4(__fadd_rn(ws_from.x, __fmul_rn(wg, d_ws.x)), __fadd_rn(ws_from.y, __fmul_rn(wg, d_ws.y)),
-                                              __fadd_rn(ws_from.z, __fmul_rn(wg, d_ws.z)), __fadd_rn(ws_from.w, __fmul_rn(wg, d_ws.w)));
+            const float4 scaled = make_float4(xadd(ws_from.x, xmul(wg, d_ws.x)), xadd(ws_from.y, xmul(wg, d_ws.y)),
+                                              xadd(ws_from.z, xmul(wg, d_ws.z)), xadd(ws_from.w, xmul(wg, d_ws.w)));
             const float4 pc = project(p.cam_vp[k], scaled);
-            cam[idx] = make_float4(__fsub_rn(pc.x, cs_from.x), __fsub_rn(pc.y, cs_from.y), __fsub_rn(pc.z, cs_from.z), vis);
+            cam[idx] = make_float4(xsub(pc.x, cs_from.x), xsub(pc.y, cs_from.y), xsub(pc.z, cs_from.z), vis);
             const float depth_cam = z_to_depth(pc.z);
             const int2 pix = cs2pixel(pc.x, pc.y, v.w, v.h);
             if (in_range(pix, v.w, v.h) && !(depth_cam < 0.0f))
@@ -275,7 +284,7 @@ __global__ void __launch_bounds__(256, 8) splat_kernel(const __grid_constant__ F
         }
         else
         {
-            cam[idx] = make_float4(__fmul_rn(fmx, wg), __fmul_rn(fmy, wg), __fmul_rn(fmz, wg), vis);
+            cam[idx] = make_float4(xmul(fmx, wg), xmul(fmy, wg), xmul(fmz, wg), vis);
             atomicMin(keys + idx, encode_key(z_to_depth(z_from), x, y));
         }
     }
@@ -334,18 +343,18 @@ __device__ __forceinline__ uint32_t color_from_shadow_idx(uint32_t sidx, int32_t
     if (sidx < (uint32_t)sfpa && sidx > 0 && s.levels)
     {
         const int32_t my_val = (int32_t)((s.bf >> (SOFTSHADOW_BITS * sidx)) & SOFTSHADOW_VAL_MASK);
-        const float t = __fdiv_rn((float)(my_val - s.mn), (float)(s.mx - s.mn));
+        const float t = xdiv((float)(my_val - s.mn), (float)(s.mx - s.mn));
         const uint32_t cmin = s.mn == s.init ? s.color : s.sha;
         const uint32_t cmax = s.mx == s.init ? s.color : s.shb;
         // (float)(1.0 - (double)t): t is k / d with d in {1, 2, 3} (or NaN), for which the
         // double difference is exact, so one float subtraction rounds identically.
-        const float omt = __fsub_rn(1.0f, t);
+        const float omt = xsub(1.0f, t);
         uint32_t r = 255u << 24;
 #pragma unroll
         for (int c = 0; c < 3; c++)
         {
             const float a = (float)((cmin >> (8 * c)) & 255u), b = (float)((cmax >> (8 * c)) & 255u);
-            r |= cvt_u8(__fadd_rn(__fmul_rn(a, omt), __fmul_rn(b, t))) << (8 * c);
+            r |= cvt_u8(xadd(xmul(a, omt), xmul(b, t))) << (8 * c);
         }
         return r;
     }
@@ -362,12 +371,12 @@ struct ShadowFrames
 __device__ __forceinline__ ShadowFrames shadow_frames(const FrameCfg &c)
 {
     ShadowFrames sf;
-    const float fa = __fmul_rn((float)c.fpa, c.alpha);
-    const float sa = __fmul_rn((float)c.sfpa, c.alpha);
+    const float fa = xmul((float)c.fpa, c.alpha);
+    const float sa = xmul((float)c.sfpa, c.alpha);
     sf.frame_idx = __float2uint_rn(fa);
-    sf.sfx = __float2uint_rd(__fadd_rn(sa, 1e-9f));
-    sf.sfy = __float2uint_ru(__fsub_rn(sa, 1e-9f));
-    sf.sft = __fsub_rn(sa, (float)sf.sfx);
+    sf.sfx = __float2uint_rd(xadd(sa, 1e-9f));
+    sf.sfy = __float2uint_ru(xsub(sa, 1e-9f));
+    sf.sft = xsub(sa, (float)sf.sfx);
     return sf;
 }
 
@@ -412,7 +421,7 @@ __device__ uint32_t second_chance(float weight, const ShadowFrames &sf, const Fr
     const float sz = ld_f(from.z, sx, sy, from.w, from.h);
     const PixelShade s_from = load_shade(from, sx, sy, on_from, c.sfpa);
     const float2 spcs = view_pixel2cs(from, sx, sy);
-    const float pcx = __fadd_rn(spcs.x, m_ft.x), pcy = __fadd_rn(spcs.y, m_ft.y), pcz = __fadd_rn(sz, m_ft.z);
+    const float pcx = xadd(spcs.x, m_ft.x), pcy = xadd(spcs.y, m_ft.y), pcz = xadd(sz, m_ft.z);
     const int2 pp = cs2pixel(pcx, pcy, to.w, to.h);
 
     uint32_t out = color_from_shadow(sf, c, from, on_from, s_from);
@@ -425,9 +434,9 @@ __device__ uint32_t second_chance(float weight, const ShadowFrames &sf, const Fr
         const float az = __ldg(to.z + pi);
         const float4 m_tf = __ldg(to.full_ff + pi);
         const PixelShade s_to = load_shade(to, (uint32_t)pp.x, (uint32_t)pp.y, on_to, c.sfpa);
-        const float dx = __fsub_rn(m_ft.x, -m_tf.x), dy = __fsub_rn(m_ft.y, -m_tf.y), dz = __fsub_rn(m_ft.z, -m_tf.z);
-        if (sqrt_less(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)), EPS_3) &&
-            fabsf(__fsub_rn(az, pcz)) < eps2)
+        const float dx = xsub(m_ft.x, -m_tf.x), dy = xsub(m_ft.y, -m_tf.y), dz = xsub(m_ft.z, -m_tf.z);
+        if (sqrt_less(xadd(xadd(xmul(dx, dx), xmul(dy, dy)), xmul(dz, dz)), EPS_3) &&
+            fabsf(xsub(az, pcz)) < eps2)
             out = lerp_color_u8(color_from_shadow(sf, c, to, on_to, s_to), out, weight);
     }
     return out;
@@ -450,7 +459,7 @@ struct DirRes
 // the roots are faster (1080p, 3 frames, 6 views: 0.537 ms roots, 0.548 squared; 2 views at
 // 48 registers 0.238 -> 0.222 ms squared; 7x7 window at 56, 6 views 1.116 -> 1.092 ms).
 template <int REGS>
-constexpr bool SQUARED_ERRORS = REGS != REPROJ_REGS_MANY_VIEWS;
+constexpr bool SQUARED_ERRORS = !FAST_MATH && REGS != REPROJ_REGS_MANY_VIEWS;
 
 template <bool SQ>
 constexpr uint32_t ERR_EPS_1_FULL_RES = err_eps<SQ>(EPS_1_FULL_RES); // error < EPS_1 <=> pattern < this
@@ -523,7 +532,7 @@ __device__ __forceinline__ CamRes cam_result(const DirRes &f, const DirRes &b, c
     if (fok || bok)
     {
         const bool both = fok && bok;
-        const bool similar = fabsf(__fsub_rn(depth_to_z(f.depth), depth_to_z(b.depth))) < eps2;
+        const bool similar = fabsf(xsub(depth_to_z(f.depth), depth_to_z(b.depth))) < eps2;
         const bool choose_fwd = (both && !similar && f.depth < b.depth) || ((!both || similar) && err_less<SQ>(fe, be));
         r.valid = true;
         if (choose_fwd)
@@ -575,7 +584,7 @@ __device__ __forceinline__ bool resolve_pixel(const DirRes *res, int lane, const
         bool take = !best.valid;
         if (best.valid && r.valid)
         {
-            const bool similar = fabsf(__fsub_rn(depth_to_z(best.depth), depth_to_z(r.depth))) < EPS_2_LOW_RES;
+            const bool similar = fabsf(xsub(depth_to_z(best.depth), depth_to_z(r.depth))) < EPS_2_LOW_RES;
             take = (!similar && r.depth < best.depth) || (similar && r.priority >= best.priority && err_less<SQ>(r.error, best.error));
         }
         if (take)
@@ -593,7 +602,7 @@ __device__ __forceinline__ bool resolve_pixel(const DirRes *res, int lane, const
         bool choose_aux = !m.valid;
         if (m.valid && !best.vis)
         {
-            const bool similar = fabsf(__fsub_rn(depth_to_z(best.depth), depth_to_z(m.depth))) < EPS_2_LOW_RES;
+            const bool similar = fabsf(xsub(depth_to_z(best.depth), depth_to_z(m.depth))) < EPS_2_LOW_RES;
             choose_aux = !similar && best.depth < m.depth;
         }
         if (choose_aux)
@@ -607,7 +616,7 @@ __device__ __forceinline__ bool resolve_pixel(const DirRes *res, int lane, const
 
     const ShadowFrames sf = shadow_frames(c);
     const float eps2 = cam == 0 ? EPS_2_FULL_RES : EPS_2_LOW_RES;
-    const float oma = __fsub_rn(1.0f, c.alpha);
+    const float oma = xsub(1.0f, c.alpha);
     if (MAV && fin.blend)
     {
         const DevView &vf = p.v[2 * cam], &vb = p.v[2 * cam + 1];
@@ -728,14 +737,19 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
                 {
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     mbar_expect_tx(&bar, (uint32_t)(nv * T::BYTES));
-                    for (int w = 0; w < nv; w++)
-                    {
-                        const DevView &vv = p.v[w];
-                        const uint32_t wx0 = vv.sx == 1 ? x0 : x0 / vv.sx, wy0 = vv.sy == 1 ? y0 : y0 / vv.sy;
-                        tma_load_3d(tiles + (size_t)w * T::ELEMS, &km.m[w], tile_x0(wx0, SW), (int)wy0 - SW, k, &bar);
-                    }
+                    if (p.withhold_block != (int32_t)(blockIdx.y * gridDim.x + blockIdx.x))
+                        for (int w = 0; w < nv; w++)
+                        {
+                            const DevView &vv = p.v[w];
+                            const uint32_t wx0 = vv.sx == 1 ? x0 : x0 / vv.sx, wy0 = vv.sy == 1 ? y0 : y0 / vv.sy;
+                            tma_load_3d(tiles + (size_t)w * T::ELEMS, &km.m[w], tile_x0(wx0, SW), (int)wy0 - SW, k, &bar);
+                        }
                 }
-                mbar_wait_bounded(&bar, (uint32_t)(round & 1), p.status);
+                // A block whose copies did not arrive (status word set) reads none of its tiles
+                // and writes nothing; the decision is block-wide, so every thread leaves together.
+                const bool arrived = mbar_wait_bounded(&bar, (uint32_t)(round & 1), p.status, p.wait_limit);
+                if (__syncthreads_or(arrived ? 0 : 1))
+                    return;
             }
             else
             {
@@ -769,6 +783,13 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
                     ax[r] = ((uint32_t)lo) >> 16;
                     ay[r] = (uint32_t)lo & 0xFFFFu;
                     s[r] = rok[r] && search_ok && d_init[r] > 0.0f;
+                    // a selected key with positive depth is a splat of an in-range source pixel;
+                    // the clamp keeps every gather inside the view even if a tile were stale
+                    if (s[r])
+                    {
+                        ax[r] = min(ax[r], vwid - 1u);
+                        ay[r] = min(ay[r], vhei - 1u);
+                    }
                     // the depth read after the search is mostly at or next to the start (a
                     // splatted source pixel, in range): fetch its line into L1 during the search
                     // (3x3 window, 6 views: 0.537 -> 0.533 ms; no gain for the 7x7 window)
@@ -787,7 +808,7 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
 #pragma unroll
                     for (int r = 0; r < ROWS; r++)
                     {
-                        const int2 t = cs2pixel(__fsub_rn(qx, m[r].x), __fsub_rn(qy[r], m[r].y), vwid, vhei);
+                        const int2 t = cs2pixel(xsub(qx, m[r].x), xsub(qy[r], m[r].y), vwid, vhei);
                         if (s[r] && in_range(t, vwid, vhei))
                         {
                             ax[r] = (uint32_t)t.x;
@@ -820,10 +841,14 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
                     d.depth = d_init[r];
                     if (s[r])
                     {
-                        d.depth = z_to_depth(__fadd_rn(zz[r], m[r].z));
-                        const float ex = __fmul_rn(__fsub_rn(__fadd_rn(fx[r], m[r].x), pcx), v.err_sx);
-                        const float ey = __fmul_rn(__fsub_rn(__fadd_rn(fy[r], m[r].y), pcy[r]), v.err_sy);
-                        d.error_vis = pack_error_vis<SQUARED_ERRORS<REGS>>(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), m[r].w > 0.0f);
+                        d.depth = z_to_depth(xadd(zz[r], m[r].z));
+                        // the scale res / min(res) (src/renderer.cu:213): the host's IEEE quotient, or
+                        // under the reference's GPU semantics its device division
+                        const float esx = FAST_MATH ? xdiv((float)vwid, (float)min(vwid, vhei)) : v.err_sx;
+                        const float esy = FAST_MATH ? xdiv((float)vhei, (float)min(vwid, vhei)) : v.err_sy;
+                        const float ex = xmul(xsub(xadd(fx[r], m[r].x), pcx), esx);
+                        const float ey = xmul(xsub(xadd(fy[r], m[r].y), pcy[r]), esy);
+                        d.error_vis = pack_error_vis<SQUARED_ERRORS<REGS>>(xadd(xmul(ex, ex), xmul(ey, ey)), m[r].w > 0.0f);
                     }
                     d.src = (ax[r] << 16) | ay[r];
                     res[((u * ROWS + r) * nv + vw) * 32 + lane] = d;
@@ -909,13 +934,13 @@ __global__ void timewarp_mean_kernel(const __grid_constant__ FrameParams p)
     double acc = 0.0;
     for (uint32_t y = 0; y < v.h; y++)
         acc = __dadd_rn(acc, p.tw_rows[y]);
-    *p.tw_mean = __fdiv_rn(__double2float_rn(acc), (float)(v.w * v.h));
+    *p.tw_mean = xdiv(__double2float_rn(acc), (float)(v.w * v.h));
     *p.status = 0;
 }
 
 __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz)
 {
-    return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
+    return xadd(xadd(xmul(ax, bx), xmul(ay, by)), xmul(az, bz));
 }
 
 // timewarp_kernel body for one pixel and client camera; false: the ray is parallel to the plane (no write)
@@ -926,25 +951,25 @@ __device__ __forceinline__ bool timewarp_pixel(const float *cam_ivp, const DevVi
     const float4 nws = project(cam_ivp, make_float4(pcs.x, pcs.y, 0.0f, 1.0f));
     const float4 fws = project(cam_ivp, make_float4(pcs.x, pcs.y, 1.0f, 1.0f));
     // ray_dir = normalize(vec3(farWS - nearWS)), glm-subset normalize: v * (1 / sqrt(dot(v, v)))
-    float dx = __fsub_rn(fws.x, nws.x), dy = __fsub_rn(fws.y, nws.y), dz = __fsub_rn(fws.z, nws.z);
-    const float sd = __fdiv_rn(1.0f, __fsqrt_rn(dot3(dx, dy, dz, dx, dy, dz)));
-    dx = __fmul_rn(dx, sd);
-    dy = __fmul_rn(dy, sd);
-    dz = __fmul_rn(dz, sd);
+    float dx = xsub(fws.x, nws.x), dy = xsub(fws.y, nws.y), dz = xsub(fws.z, nws.z);
+    const float sd = xdiv(1.0f, xsqrt(dot3(dx, dy, dz, dx, dy, dz)));
+    dx = xmul(dx, sd);
+    dy = xmul(dy, sd);
+    dz = xmul(dz, sd);
     // plane through inv_viewproj_mat_to[3] facing the centre of the keyframe at depth_to
     const float4 cws = project(to.inv_vp, make_float4(0.0f, 0.0f, depth_to, 1.0f));
     const float cpx = to.inv_vp[12], cpy = to.inv_vp[13], cpz = to.inv_vp[14], cpw = to.inv_vp[15];
-    float nx = __fsub_rn(cws.x, cpx), ny = __fsub_rn(cws.y, cpy), nz = __fsub_rn(cws.z, cpz);
-    const float nw = __fsub_rn(cws.w, cpw);
-    const float sn = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(dot3(nx, ny, nz, nx, ny, nz), __fmul_rn(nw, nw)))); // 4-component normalize
-    nx = __fmul_rn(nx, sn);
-    ny = __fmul_rn(ny, sn);
-    nz = __fmul_rn(nz, sn);
+    float nx = xsub(cws.x, cpx), ny = xsub(cws.y, cpy), nz = xsub(cws.z, cpz);
+    const float nw = xsub(cws.w, cpw);
+    const float sn = xdiv(1.0f, xsqrt(xadd(dot3(nx, ny, nz, nx, ny, nz), xmul(nw, nw)))); // 4-component normalize
+    nx = xmul(nx, sn);
+    ny = xmul(ny, sn);
+    nz = xmul(nz, sn);
     const float denom = dot3(dx, dy, dz, nx, ny, nz);
     if (fabsf(denom) < 1e-6f)
         return false;
-    const float t = __fdiv_rn(dot3(__fsub_rn(cpx, nws.x), __fsub_rn(cpy, nws.y), __fsub_rn(cpz, nws.z), nx, ny, nz), denom);
-    const float4 hit = make_float4(__fadd_rn(nws.x, __fmul_rn(t, dx)), __fadd_rn(nws.y, __fmul_rn(t, dy)), __fadd_rn(nws.z, __fmul_rn(t, dz)), 1.0f);
+    const float t = xdiv(dot3(xsub(cpx, nws.x), xsub(cpy, nws.y), xsub(cpz, nws.z), nx, ny, nz), denom);
+    const float4 hit = make_float4(xadd(nws.x, xmul(t, dx)), xadd(nws.y, xmul(t, dy)), xadd(nws.z, xmul(t, dz)), 1.0f);
     const float4 pc = project(to.vp_self, hit); // WS2CS(intersection, viewproj_mat_to)
     int2 pix = cs2pixel(pc.x, pc.y, to.w, to.h);
     const DevView *src = &to;
@@ -998,7 +1023,7 @@ __global__ void __launch_bounds__(256) timewarp_kernel(const __grid_constant__ F
 // d <- 2 d - 1 (2 d is exact, so the two roundings are those of the
 // reference).  VEC: four pixels per thread with 16-byte accesses (z 16-byte
 // aligned), the last n % 4 pixels one per thread.
-__device__ __forceinline__ float unity_depth_to_z(float d) { return __fsub_rn(__fmul_rn(2.0f, __fsub_rn(1.0f, d)), 1.0f); }
+__device__ __forceinline__ float unity_depth_to_z(float d) { return xsub(xmul(2.0f, xsub(1.0f, d)), 1.0f); }
 
 template <bool VEC>
 __global__ void depth_to_z_kernel(float *__restrict__ z, size_t n)

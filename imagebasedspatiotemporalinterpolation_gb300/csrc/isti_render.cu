@@ -11,7 +11,12 @@
 // blocks the host.
 #include "isti.h"
 #include "isti_dataset.h"
+#include "isti_arith.h"
 #include "isti_kernels.cuh"
+#include "isti_launch.cuh"
+#include "isti_learned.cuh"
+#include "isti_unet.h"
+#include "isti_train.h"
 #include "host/isti_error.hpp"
 
 #include <algorithm>
@@ -42,6 +47,17 @@ struct isti_renderer
     // autotuning of the reprojection launch: one entry per tuned shape class
     bool autotune = false;
     std::vector<isti_tuning> tuned;
+    // arithmetic of the kernels (isti_renderer_set_arithmetic)
+    int32_t arith = ISTI_ARITH_IEEE;
+    // learned render path: its own arena (keys for the fallback tiles, keyframe parts,
+    // network input and output, tile flags) and the parameters of its last call
+    void *learned_arena = nullptr;
+    size_t learned_bytes = 0;
+    isti::LearnedParams learned{};
+    bool has_learned = false;
+    // failure-detection test hook (isti_renderer_test_withhold_tile)
+    int32_t withhold_x = -1, withhold_y = -1;
+    uint32_t wait_limit = 0;
 };
 
 namespace
@@ -175,27 +191,13 @@ Layout layout_for(int mode, const isti_view *const *views, int n_views, int n_fr
     return mode == ISTI_MODE_TIMEWARP ? timewarp_layout(views) : layout_of(views, n_views, n_frames);
 }
 
-// Enqueues the timewarp of one batch (src/renderer.cu:615-629): mean z of the forward
-// keyframe (two kernels), then one kernel over the output pixels.
-cudaError_t launch_timewarp(isti::FrameParams &p, char *base, cudaStream_t stream, cudaEvent_t after_mean, cudaEvent_t after_nothing)
-{
-    p.tw_rows = reinterpret_cast<double *>(base);
-    p.tw_mean = reinterpret_cast<float *>(base + align_up((size_t)p.v[0].h * sizeof(double), 256));
-    isti::timewarp_rowsum_kernel<<<(p.v[0].h + 127) / 128, 128, 0, stream>>>(p);
-    isti::timewarp_mean_kernel<<<1, 32, 0, stream>>>(p);
-    if (after_mean)
-        cudaEventRecord(after_mean, stream);
-    if (after_nothing)
-        cudaEventRecord(after_nothing, stream); // no splat stage in this mode
-    isti::timewarp_kernel<<<dim3((p.out_w + 31) / 32, (p.out_h + 7) / 8), dim3(32, 8), 0, stream>>>(p);
-    return cudaGetLastError();
-}
-
 // Fills the kernel parameters for one batch whose intermediates live at `base`.
 void fill_params(isti::FrameParams &p, int n_frames, void *const *outs, const isti_render_info *infos, const isti_frame_data *frame,
                  const isti_view *const *views, int n_views, const Layout &l, char *base, bool chain)
 {
     std::memset(&p, 0, sizeof p);
+    p.withhold_block = -1;
+    p.withhold_x = p.withhold_y = -1;
     const isti_render_info &info = infos[0];
     size_t off_key = 0, off_cam = l.key_bytes, off_full = l.key_bytes + l.cam_bytes, off_lut = l.key_bytes + l.cam_bytes + l.ff_bytes;
     for (int k = 0; k < n_views; k++)
@@ -260,174 +262,6 @@ void fill_params(isti::FrameParams &p, int n_frames, void *const *outs, const is
     p.chain = chain ? 1 : 0;
 }
 
-// ---- tensor maps for the TMA-staged key tiles ----
-
-using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *, const cuuint64_t *,
-                                   const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_tiled()
-{
-    static EncodeTiledFn fn = [] {
-        void *f = nullptr;
-        cudaDriverEntryPointQueryResult q{};
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-            q != cudaDriverEntryPointSuccess)
-            return (EncodeTiledFn) nullptr;
-        return reinterpret_cast<EncodeTiledFn>(f);
-    }();
-    return fn;
-}
-
-// One 3-D map (x, y, frame) per view over its keys; false when a view cannot be
-// described (row pitch not a multiple of 16 bytes, image smaller than a tile) or
-// the driver has no tensor-map support: the kernel then loads tiles with plain loads.
-template <int SW>
-bool make_key_maps(const isti::FrameParams &p, isti::KeyMaps &km)
-{
-    using T = isti::Tile<SW>;
-    EncodeTiledFn enc = encode_tiled();
-    if (!enc)
-        return false;
-    for (int k = 0; k < p.n_views; k++)
-    {
-        const isti::DevView &v = p.v[k];
-        if ((v.w * 8u) % 16u != 0 || v.w < (uint32_t)T::W || v.h < (uint32_t)T::H)
-            return false;
-        const cuuint64_t dims[3] = {v.w, v.h, (cuuint64_t)p.n_frames};
-        const cuuint64_t strides[2] = {(cuuint64_t)v.w * 8u, (cuuint64_t)p.key_stride * 8u};
-        const cuuint32_t box[3] = {(cuuint32_t)T::W, (cuuint32_t)T::H, 1};
-        const cuuint32_t estr[3] = {1, 1, 1};
-        if (enc(&km.m[k], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, v.splat, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-            return false;
-    }
-    return true;
-}
-
-// A reprojection launch shape: register cap and output row pairs per block (0: the fixed rule).
-struct ReprojChoice
-{
-    int regs = 0;
-    int row_pairs = 0;
-};
-
-// The fixed rule: register cap by window size and view count (isti_kernels.cuh), row pairs
-// so that every warp has a colour task in phase 2.
-int rule_regs(int sw, int n_views)
-{
-    if (sw != 1)
-        return isti::REPROJ_REGS_WIDE_WINDOW;
-    return n_views >= isti::REPROJ_MANY_VIEWS ? isti::REPROJ_REGS_MANY_VIEWS : isti::REPROJ_REGS;
-}
-
-int rule_row_pairs(int n_views, int n_frames) { return std::max(1, std::min(3, n_views / (isti::ROWS * n_frames))); }
-
-template <int SW, int SI, bool MAV, int REGS>
-cudaError_t launch_reproj_regs(isti::FrameParams &p, cudaStream_t stream, int row_pairs)
-{
-    // One unit's key tiles per TMA round: the least shared memory per block, so the most
-    // resident blocks and the largest L1 (1080p, 6 views, 3 frames, 8 blocks per SM: one
-    // frame per round 0.569 ms, two 0.581 ms; at 7 blocks two frames 0.590, three 0.594).
-    // Row pairs per block: enough (frame, row) tasks for every warp in phase 2 when there
-    // are fewer frames than views need (a single frame of 6 views: 3 row pairs).
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess)
-        return e;
-    p.row_pairs = row_pairs > 0 ? std::min(row_pairs, 3) : rule_row_pairs(p.n_views, p.n_frames);
-    static thread_local isti::KeyMaps km; // 2 KiB, passed by value as a kernel parameter
-    p.use_tma = make_key_maps<SW>(p, km) ? 1 : 0;
-    const size_t smem = isti::reproj_smem<SW>(p.n_views, p.n_frames * p.row_pairs);
-    // raise the kernel's dynamic shared-memory limit once to the largest size requested, so
-    // that calls inside a CUDA graph capture make no attribute calls after a first uncaptured
-    // call of the same shape
-    static std::mutex attr_mutex;
-    static int attr_set[64] = {}; // per device
-    if (smem > 48 * 1024)
-    {
-        std::lock_guard<std::mutex> lock(attr_mutex);
-        int &cur = attr_set[dev & 63];
-        if ((int)smem > cur)
-        {
-            e = cudaFuncSetAttribute(isti::reproj_kernel<SW, SI, MAV, REGS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess)
-                return e;
-            cur = (int)smem;
-        }
-    }
-    const uint32_t block_rows = (uint32_t)(isti::ROWS * p.row_pairs);
-    const dim3 gr((p.out_w + 31) / 32, (p.out_h + block_rows - 1) / block_rows);
-    isti::reproj_kernel<SW, SI, MAV, REGS><<<gr, dim3(32, p.n_views), smem, stream>>>(p, km);
-    return cudaGetLastError();
-}
-
-template <int SW, int SI, bool MAV>
-cudaError_t launch_reproj(isti::FrameParams &p, cudaStream_t stream, ReprojChoice c)
-{
-    const int regs = c.regs > 0 ? c.regs : rule_regs(SW, p.n_views);
-    if constexpr (SW == 1)
-    {
-        if (regs == isti::REPROJ_REGS_MANY_VIEWS)
-            return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS_MANY_VIEWS>(p, stream, c.row_pairs);
-        return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS>(p, stream, c.row_pairs);
-    }
-    else
-        return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS_WIDE_WINDOW>(p, stream, c.row_pairs);
-}
-
-// window size of the reprojection of a render mode (src/renderer.cu:676-693)
-int mode_window(int mode) { return mode == ISTI_MODE_BACKWARD_BIDIRECTIONAL ? 3 : 1; }
-
-// register caps a mode's reprojection is built with (the autotuner's candidates)
-std::vector<int> mode_regs(int mode)
-{
-    if (mode_window(mode) == 1)
-        return {isti::REPROJ_REGS_MANY_VIEWS, isti::REPROJ_REGS};
-    return {isti::REPROJ_REGS_WIDE_WINDOW};
-}
-
-cudaError_t launch_reproj_mode(isti::FrameParams &p, int mode, cudaStream_t stream, ReprojChoice c)
-{
-    switch (mode)
-    {
-    case ISTI_MODE_OURS:
-    case ISTI_MODE_BACKWARD_UNIDIRECTIONAL:
-        return launch_reproj<1, 3, false>(p, stream, c);
-    case ISTI_MODE_SPLATTING:
-        return launch_reproj<1, 0, false>(p, stream, c);
-    case ISTI_MODE_BACKWARD_BIDIRECTIONAL:
-        return launch_reproj<3, 5, true>(p, stream, c);
-    }
-    return cudaGetLastError();
-}
-
-// Enqueues the three kernels of one batch; events (optional) are recorded after init and splat.
-cudaError_t launch_batch(isti::FrameParams &p, int mode, cudaStream_t stream, cudaEvent_t after_init, cudaEvent_t after_splat,
-                         ReprojChoice choice)
-{
-    uint32_t max_w = 0, max_h = 0;
-    for (int k = 0; k < p.n_views; k++)
-    {
-        max_w = p.v[k].w > max_w ? p.v[k].w : max_w;
-        max_h = p.v[k].h > max_h ? p.v[k].h : max_h;
-    }
-    // init: about 8 x 16-byte stores per thread, at least enough threads for the tables (<= 65535 entries)
-    size_t init_blocks = (p.key_units + 8 * 256 - 1) / (8 * 256);
-    if (init_blocks < 256)
-        init_blocks = 256;
-    if (init_blocks > 152 * 64)
-        init_blocks = 152 * 64;
-    isti::init_kernel<<<(unsigned)init_blocks, 256, 0, stream>>>(p);
-    if (after_init)
-        cudaEventRecord(after_init, stream);
-    const dim3 gs((max_w + 31) / 32, (max_h + 7) / 8, p.n_views);
-    isti::splat_kernel<<<gs, dim3(32, 8), 0, stream>>>(p);
-    if (after_splat)
-        cudaEventRecord(after_splat, stream);
-    return launch_reproj_mode(p, mode, stream, choice);
-}
-
 bool has_shadows(const isti::FrameParams &p)
 {
     for (int k = 0; k < p.n_views; k++)
@@ -449,15 +283,22 @@ isti_tuning *find_tuning(isti_renderer *r, int mode, const isti::FrameParams &p)
 // Times every candidate launch of the reprojection of the batch just enqueued (same inputs,
 // same outputs: each run rewrites them identically) and records the fastest for its shape
 // class.  One untimed launch per candidate first (module loading), then REPEAT timed ones.
+cudaError_t launch_reproj_arith(isti_renderer *r, isti::FrameParams &p, int mode, cudaStream_t stream, isti::ReprojChoice c)
+{
+    if (r->arith == ISTI_ARITH_REFERENCE_GPU)
+        return isti_fm_launch_reproj_mode(&p, mode, stream, c.regs, c.row_pairs);
+    return isti::launch_reproj_mode(p, mode, stream, c);
+}
+
 isti_status tune_reproj(isti_renderer *r, int mode, cudaStream_t stream)
 {
     constexpr int REPEAT = 3;
     isti::FrameParams &p = r->last;
-    std::vector<ReprojChoice> cands;
-    for (int regs : mode_regs(mode))
+    std::vector<isti::ReprojChoice> cands;
+    for (int regs : isti::mode_regs(mode))
         for (int np = 1; np <= 3; np++)
             cands.push_back({regs, np});
-    const ReprojChoice rule{rule_regs(mode_window(mode), p.n_views), rule_row_pairs(p.n_views, p.n_frames)};
+    const isti::ReprojChoice rule{isti::rule_regs(isti::mode_window(mode), p.n_views), isti::rule_row_pairs(p.n_views, p.n_frames)};
     std::vector<cudaEvent_t> ev(2 * cands.size(), nullptr);
     cudaError_t e = cudaSuccess;
     for (cudaEvent_t &x : ev)
@@ -465,11 +306,11 @@ isti_status tune_reproj(isti_renderer *r, int mode, cudaStream_t stream)
             e = cudaEventCreate(&x);
     for (size_t i = 0; i < cands.size() && e == cudaSuccess; i++)
     {
-        e = launch_reproj_mode(p, mode, stream, cands[i]);
+        e = launch_reproj_arith(r, p, mode, stream, cands[i]);
         if (e == cudaSuccess)
             e = cudaEventRecord(ev[2 * i], stream);
         for (int k = 0; k < REPEAT && e == cudaSuccess; k++)
-            e = launch_reproj_mode(p, mode, stream, cands[i]);
+            e = launch_reproj_arith(r, p, mode, stream, cands[i]);
         if (e == cudaSuccess)
             e = cudaEventRecord(ev[2 * i + 1], stream);
     }
@@ -548,6 +389,9 @@ isti_status render_batch(isti_renderer *r, int n_frames, void *const *outs, cons
     }
     char *base = static_cast<char *>(r->arena);
     fill_params(r->last, n_frames, outs, infos, frame, views, n_views, l, base, chain);
+    r->last.withhold_x = r->withhold_x;
+    r->last.withhold_y = r->withhold_y;
+    r->last.wait_limit = r->wait_limit;
 
     cudaEvent_t *ev = nullptr;
     if (r->timing)
@@ -568,12 +412,17 @@ isti_status render_batch(isti_renderer *r, int n_frames, void *const *outs, cons
         r->timed_launches += 3;
         cudaEventRecord(ev[0], stream);
     }
-    ReprojChoice choice{};
+    isti::ReprojChoice choice{};
     const isti_tuning *tuned = timewarp ? nullptr : find_tuning(r, infos[0].mode, r->last);
     if (tuned)
         choice = {tuned->regs, tuned->row_pairs};
-    e = timewarp ? launch_timewarp(r->last, base, stream, ev ? ev[1] : nullptr, ev ? ev[2] : nullptr)
-                 : launch_batch(r->last, infos[0].mode, stream, ev ? ev[1] : nullptr, ev ? ev[2] : nullptr, choice);
+    cudaEvent_t ev1 = ev ? ev[1] : nullptr, ev2 = ev ? ev[2] : nullptr;
+    if (r->arith == ISTI_ARITH_REFERENCE_GPU)
+        e = timewarp ? isti_fm_launch_timewarp(&r->last, base, stream, ev1, ev2)
+                     : isti_fm_launch_batch(&r->last, infos[0].mode, stream, ev1, ev2, choice.regs, choice.row_pairs);
+    else
+        e = timewarp ? isti::launch_timewarp(r->last, base, stream, ev1, ev2)
+                     : isti::launch_batch(r->last, infos[0].mode, stream, ev1, ev2, choice);
     if (ev)
         cudaEventRecord(ev[3], stream);
     if (e != cudaSuccess)
@@ -638,6 +487,8 @@ isti_status isti_renderer_destroy(isti_renderer *r)
     isti_status s = ISTI_OK;
     for (cudaEvent_t ev : r->events)
         cudaEventDestroy(ev);
+    if (r->learned_arena)
+        cudaFree(r->learned_arena);
     if (r->arena)
     {
         cudaError_t e = cudaFree(r->arena);
@@ -677,6 +528,30 @@ isti_status isti_renderer_device_status(isti_renderer *r, int32_t *device_status
     e = cudaMemcpy(device_status, r->last.status, sizeof(int32_t), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess)
         return cuda_fail(e, "cudaMemcpy");
+    return ISTI_OK;
+}
+
+isti_status isti_renderer_set_arithmetic(isti_renderer *r, int32_t arith)
+{
+    if (!r)
+        return fail(ISTI_ERR_INVALID_ARG, "renderer is NULL");
+    if (arith != ISTI_ARITH_IEEE && arith != ISTI_ARITH_REFERENCE_GPU)
+        return fail(ISTI_ERR_INVALID_ARG, "unknown arithmetic mode");
+    if (arith == ISTI_ARITH_REFERENCE_GPU && isti_fm_params_size() != sizeof(isti::FrameParams))
+        return fail(ISTI_ERR_UNSUPPORTED, "kernel parameter layouts of the two arithmetic modes differ");
+    if (arith != r->arith)
+        r->tuned.clear(); // launch timings belong to one set of kernels
+    r->arith = arith;
+    return ISTI_OK;
+}
+
+isti_status isti_renderer_test_withhold_tile(isti_renderer *r, int32_t x, int32_t y, uint32_t wait_limit)
+{
+    if (!r)
+        return fail(ISTI_ERR_INVALID_ARG, "renderer is NULL");
+    r->withhold_x = x;
+    r->withhold_y = y;
+    r->wait_limit = wait_limit;
     return ISTI_OK;
 }
 
@@ -765,6 +640,202 @@ isti_status isti_renderer_view_buffers(const isti_renderer *r, int32_t view, con
 
 } // extern "C"
 
+// ============================ learned initialisation ============================
+
+namespace
+{
+constexpr int LEARNED_MAX_FRAMES = ISTI_MAX_BATCH_FRAMES;
+
+int quarter_grid(uint32_t n) { return (int)(((n + 3) / 4 + 7) / 8 * 8); }
+} // namespace
+
+// Lays out the learned arena for a call and fills r->learned (everything but the stages).
+isti_status learned_setup(isti_renderer *r, isti_flownet *net, int32_t n_frames, void *const *out_rgba, const isti_render_info *infos,
+                          const isti_frame_data *frame, int32_t iterations, __half **guess_out);
+
+extern "C" isti_status isti_render_learned(isti_renderer *r, isti_flownet *net, int32_t n_frames, void *const *out_rgba,
+                                           const isti_render_info *infos, const isti_frame_data *frame, int32_t iterations, void *stream_ptr)
+{
+    __half *guess = nullptr;
+    isti_status st = learned_setup(r, net, n_frames, out_rgba, infos, frame, iterations, &guess);
+    if (st != ISTI_OK)
+        return st;
+    const cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
+    isti::LearnedParams &p = r->learned;
+    const uint32_t w = infos[0].width, h = infos[0].height;
+    cudaError_t e = cudaMemsetAsync(p.fallback_count, 0, 4, stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(p.fp.status, 0, 4, stream);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaMemsetAsync");
+    const dim3 b2(32, 8);
+    isti::keyframe_kernel<<<dim3((w + 31) / 32, (h + 7) / 8, 2), b2, 0, stream>>>(p);
+    if (net)
+    {
+        isti::input_kernel<<<dim3((p.wq + 31) / 32, (p.hq + 7) / 8, n_frames), b2, 0, stream>>>(p);
+        e = cudaGetLastError();
+        if (e != cudaSuccess)
+            return cuda_fail(e, "learned input launch");
+        st = isti_flownet_forward(net, p.net_in, n_frames, p.hq, p.wq, nullptr, guess, stream);
+        if (st != ISTI_OK)
+            return st;
+    }
+    const dim3 gt(p.tiles_x, p.tiles_y, n_frames);
+    isti::learned_kernel<<<gt, dim3(isti::LT_W, isti::LT_H), 0, stream>>>(p);
+    isti::fallback_init_kernel<<<gt, dim3(isti::LT_W, isti::LT_H), 0, stream>>>(p);
+    isti::fallback_splat_kernel<<<dim3((w + 31) / 32, (h + 7) / 8, 2 * n_frames), b2, 0, stream>>>(p);
+    isti::fallback_reproj_kernel<<<gt, dim3(isti::LT_W, isti::LT_H), 0, stream>>>(p);
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return cuda_fail(e, "learned render launch");
+    r->has_learned = true;
+    return ISTI_OK;
+}
+
+extern "C" isti_status isti_learned_input(isti_renderer *r, int32_t n_frames, const isti_render_info *infos, const isti_frame_data *frame,
+                                          void *net_input, void *stream_ptr)
+{
+    if (!net_input || ((uintptr_t)net_input & 15u))
+        return fail(ISTI_ERR_INVALID_ARG, "net_input must be a 16-byte aligned device buffer");
+    // the outputs are not touched by the input stages: the render info's frames only need a
+    // placeholder address each
+    void *dummy[isti::MAX_FRAMES];
+    for (int k = 0; k < isti::MAX_FRAMES; k++)
+        dummy[k] = net_input;
+    __half *guess = nullptr;
+    isti_status st = learned_setup(r, nullptr, n_frames, dummy, infos, frame, 1, &guess);
+    if (st != ISTI_OK)
+        return st;
+    const cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
+    isti::LearnedParams p = r->learned;
+    p.net_in = static_cast<__nv_bfloat16 *>(net_input);
+    const uint32_t w = infos[0].width, h = infos[0].height;
+    const dim3 b2(32, 8);
+    isti::keyframe_kernel<<<dim3((w + 31) / 32, (h + 7) / 8, 2), b2, 0, stream>>>(p);
+    isti::input_kernel<<<dim3((p.wq + 31) / 32, (p.hq + 7) / 8, n_frames), b2, 0, stream>>>(p);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? ISTI_OK : cuda_fail(e, "learned input launch");
+}
+
+extern "C" isti_status isti_learned_labels(isti_renderer *r, int32_t frame_index, float *labels, void *stream_ptr)
+{
+    if (!r || !labels || ((uintptr_t)labels & 15u))
+        return fail(ISTI_ERR_INVALID_ARG, "NULL or unaligned argument");
+    if (!r->has_frame || r->last.tw_mean != nullptr || r->last.n_aux != 0 || r->last.linear)
+        return fail(ISTI_ERR_INVALID_ARG, "labels need a preceding plain render (main camera only, modes 0/2/3)");
+    if (frame_index < 0 || frame_index >= r->last.n_frames)
+        return fail(ISTI_ERR_INVALID_ARG, "frame index out of range");
+    const int hq = quarter_grid(r->last.out_h), wq = quarter_grid(r->last.out_w);
+    isti::label_kernel<<<dim3((wq + 31) / 32, (hq + 7) / 8), dim3(32, 8), 0, static_cast<cudaStream_t>(stream_ptr)>>>(r->last, frame_index, hq,
+                                                                                                                         wq, labels);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? ISTI_OK : cuda_fail(e, "label launch");
+}
+
+extern "C" isti_status isti_learned_grid(uint32_t width, uint32_t height, int32_t *grid_w, int32_t *grid_h)
+{
+    if (!grid_w || !grid_h)
+        return fail(ISTI_ERR_INVALID_ARG, "NULL argument");
+    *grid_w = quarter_grid(width);
+    *grid_h = quarter_grid(height);
+    return ISTI_OK;
+}
+
+isti_status learned_setup(isti_renderer *r, isti_flownet *net, int32_t n_frames, void *const *out_rgba, const isti_render_info *infos,
+                          const isti_frame_data *frame, int32_t iterations, __half **guess_out)
+{
+    if (!r || !out_rgba || !infos || !frame)
+        return fail(ISTI_ERR_INVALID_ARG, "NULL argument");
+    const isti_view *views[isti::MAX_VIEWS];
+    int n_views = 0;
+    const isti_status st = validate(n_frames, out_rgba, infos, frame, views, n_views);
+    if (st != ISTI_OK)
+        return st;
+    if (frame->num_aux != 0)
+        return fail(ISTI_ERR_INVALID_ARG, "isti_render_learned renders the main camera only (num_aux must be 0)");
+    if (infos[0].mode != ISTI_MODE_OURS && infos[0].mode != ISTI_MODE_BACKWARD_UNIDIRECTIONAL)
+        return fail(ISTI_ERR_INVALID_ARG, "isti_render_learned implements modes 0 and 2 (3x3 window, 3 search iterations)");
+    if (iterations < 0 || iterations > 16)
+        return fail(ISTI_ERR_INVALID_ARG, "iterations must be 0..16");
+    int cur = 0;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaGetDevice");
+    if (cur != r->device)
+        return fail(ISTI_ERR_INVALID_ARG, "renderer was created on another device");
+    const uint32_t w = infos[0].width, h = infos[0].height;
+    const size_t px = (size_t)w * h;
+    const int hq = quarter_grid(h), wq = quarter_grid(w);
+    const int tiles_x = (int)((w + isti::LT_W - 1) / isti::LT_W), tiles_y = (int)((h + isti::LT_H - 1) / isti::LT_H);
+    // [keys: frames x 2 views][full flow: 2 views][lut: 2 views][status] (fill_params' layout, no cam flow)
+    // then [ws: 2 views][dws: 2 views][network input][network output][tile flags][fallback count]
+    Layout l{};
+    for (int k = 0; k < 2; k++)
+    {
+        l.key_frame_bytes += align_up(px * 8, 256);
+        l.lut_bytes += align_up((size_t)(w + h) * 4, 256);
+    }
+    l.ff_bytes = 2 * align_up(px * 16, 256);
+    l.key_bytes = l.key_frame_bytes * n_frames;
+    l.total = l.key_bytes + l.ff_bytes + l.lut_bytes + STATUS_BYTES;
+    const size_t ws_bytes = align_up(px * 16, 256);
+    const size_t in_bytes = align_up((size_t)n_frames * hq * wq * 16 * 2, 256);
+    const size_t guess_bytes = align_up((size_t)n_frames * hq * wq * 4 * 2, 256);
+    const size_t flag_bytes = align_up((size_t)n_frames * tiles_x * tiles_y * 4, 256);
+    const size_t total = l.total + 4 * ws_bytes + in_bytes + guess_bytes + flag_bytes + 256;
+    if (total > r->learned_bytes)
+    {
+        if (r->learned_arena)
+            cudaFree(r->learned_arena);
+        r->learned_arena = nullptr;
+        r->learned_bytes = 0;
+        e = cudaMalloc(&r->learned_arena, total);
+        if (e != cudaSuccess)
+            return e == cudaErrorMemoryAllocation ? fail(ISTI_ERR_OOM, "cudaMalloc of the learned-path arena failed") : cuda_fail(e, "cudaMalloc");
+        r->learned_bytes = total;
+    }
+    char *base = static_cast<char *>(r->learned_arena);
+    isti::LearnedParams &p = r->learned;
+    fill_params(p.fp, n_frames, out_rgba, infos, frame, views, n_views, l, base, false);
+    for (int v = 0; v < 2; v++)
+        p.fp.v[v].cam_ff = nullptr; // the client-camera flow is computed on the fly
+    char *extra = base + l.total;
+    for (int v = 0; v < 2; v++)
+    {
+        p.ws[v] = reinterpret_cast<float4 *>(extra + v * ws_bytes);
+        p.dws[v] = reinterpret_cast<float4 *>(extra + (2 + v) * ws_bytes);
+    }
+    p.net_in = reinterpret_cast<__nv_bfloat16 *>(extra + 4 * ws_bytes);
+    __half *guess = reinterpret_cast<__half *>(extra + 4 * ws_bytes + in_bytes);
+    p.guess = net ? guess : nullptr;
+    p.tile_flags = reinterpret_cast<uint32_t *>(extra + 4 * ws_bytes + in_bytes + guess_bytes);
+    p.fallback_count = reinterpret_cast<int32_t *>(extra + 4 * ws_bytes + in_bytes + guess_bytes + flag_bytes);
+    p.hq = hq;
+    p.wq = wq;
+    p.learned_iters = iterations;
+    p.tiles_x = tiles_x;
+    p.tiles_y = tiles_y;
+    *guess_out = guess;
+    return ISTI_OK;
+}
+
+extern "C" isti_status isti_renderer_learned_stats(isti_renderer *r, int32_t *fallback_tiles, int32_t *tiles)
+{
+    if (!r || !fallback_tiles || !tiles)
+        return fail(ISTI_ERR_INVALID_ARG, "NULL argument");
+    *fallback_tiles = 0;
+    *tiles = 0;
+    if (!r->has_learned)
+        return ISTI_OK;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess)
+        e = cudaMemcpy(fallback_tiles, r->learned.fallback_count, 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "reading the fallback count");
+    *tiles = r->learned.tiles_x * r->learned.tiles_y * r->learned.fp.n_frames;
+    return ISTI_OK;
+}
+
 // ============================ rendering without allocation ============================
 //
 // isti_render_noalloc serves callers that may not allocate device memory while
@@ -777,28 +848,40 @@ namespace
 {
 // Fixed scratch for isti_render_noalloc: ISTI_NOALLOC_SCRATCH_BYTES (64 MiB), loaded
 // with the module on every GPU that uses the library and kept until the process exits.
+// Its last 256 bytes hold the device status word of the no-allocation calls, at a fixed
+// place whatever the frame's layout, so isti_noalloc_device_status can read it.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[ISTI_NOALLOC_SCRATCH_BYTES];
+constexpr size_t NOALLOC_STATUS_OFFSET = (size_t)ISTI_NOALLOC_SCRATCH_BYTES - 256;
+static_assert(NOALLOC_STATUS_OFFSET % 256 == 0, "status word must stay aligned");
 
 constexpr int NOALLOC_MAX_DEVICES = 64;
 std::mutex g_noalloc_mutex;
 void *g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
 
 // Device address of g_noalloc_scratch on the current device.  In host code the
-// array's name only denotes a host-side shadow, so the address is looked up once
-// per device (with that device current) and cached.
-isti_status noalloc_scratch(int device, char **out)
+// array's name only denotes a host-side shadow, so the address is looked up with the
+// device current.  It is looked up again on every call made outside a stream capture
+// (a reset device or a recreated context may place the module elsewhere); a call
+// inside a capture uses the address of the last uncaptured call on that device.
+isti_status noalloc_scratch(int device, cudaStream_t stream, char **out)
 {
     if (device < 0 || device >= NOALLOC_MAX_DEVICES)
         return fail(ISTI_ERR_UNSUPPORTED, "device ordinal beyond the no-allocation scratch table");
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(stream, &cs);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaStreamIsCapturing");
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[device])
+    if (cs == cudaStreamCaptureStatusNone)
     {
         void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess)
             return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
         g_noalloc_ptr[device] = p;
     }
+    else if (!g_noalloc_ptr[device])
+        return fail(ISTI_ERR_INVALID_ARG, "the first isti_render_noalloc call on a device must not be captured");
     *out = static_cast<char *>(g_noalloc_ptr[device]);
     return ISTI_OK;
 }
@@ -815,26 +898,43 @@ extern "C" isti_status isti_render_noalloc(void *out_rgba, const isti_render_inf
     if (st != ISTI_OK)
         return st;
     const Layout l = layout_for(info->mode, views, n_views, 1);
-    if (l.total > ISTI_NOALLOC_SCRATCH_BYTES)
+    if (l.total > NOALLOC_STATUS_OFFSET)
         return fail(ISTI_ERR_INVALID_ARG, "frame needs " + std::to_string(l.total) + " bytes of scratch; isti_render_noalloc holds at most " +
+                                              std::to_string(NOALLOC_STATUS_OFFSET) + " of its " +
                                               std::to_string((size_t)ISTI_NOALLOC_SCRATCH_BYTES) + " (use isti_render for larger frames)");
     int device = 0;
     cudaError_t e = cudaGetDevice(&device);
     if (e != cudaSuccess)
         return cuda_fail(e, "cudaGetDevice");
+    const cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
     char *base = nullptr;
-    st = noalloc_scratch(device, &base);
+    st = noalloc_scratch(device, stream, &base);
     if (st != ISTI_OK)
         return st;
     isti::FrameParams p;
     fill_params(p, 1, outs, info, frame, views, n_views, l, base, false);
-    // The array keeps the previous call's contents: the init kernel resets every key to
-    // the reference's empty value (all bytes 0xfe), the tables and the status word; the
-    // flow fields are fully rewritten by the splat kernel before the reprojection reads them.
-    e = info->mode == ISTI_MODE_TIMEWARP ? launch_timewarp(p, base, static_cast<cudaStream_t>(stream_ptr), nullptr, nullptr)
-                                         : launch_batch(p, info->mode, static_cast<cudaStream_t>(stream_ptr), nullptr, nullptr, ReprojChoice{});
+    p.status = reinterpret_cast<int32_t *>(base + NOALLOC_STATUS_OFFSET);
+    // The array keeps the previous call's contents: the init kernel (the timewarp's mean
+    // kernel in mode 4) resets the status word, the init kernel every key to the
+    // reference's empty value (all bytes 0xfe) and the tables; the flow fields are fully
+    // rewritten by the splat kernel before the reprojection reads them.
+    e = info->mode == ISTI_MODE_TIMEWARP ? isti::launch_timewarp(p, base, stream, nullptr, nullptr)
+                                         : isti::launch_batch(p, info->mode, stream, nullptr, nullptr, isti::ReprojChoice{});
     if (e != cudaSuccess)
         return cuda_fail(e, "kernel launch");
+    return ISTI_OK;
+}
+
+extern "C" isti_status isti_noalloc_device_status(int32_t *device_status)
+{
+    if (!device_status)
+        return fail(ISTI_ERR_INVALID_ARG, "NULL argument");
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaDeviceSynchronize");
+    e = cudaMemcpyFromSymbol(device_status, g_noalloc_scratch, sizeof(int32_t), NOALLOC_STATUS_OFFSET, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "reading the no-allocation status word");
     return ISTI_OK;
 }
 

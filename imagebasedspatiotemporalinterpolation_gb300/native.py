@@ -17,6 +17,9 @@ ISTI_ERR_CUDA = 3
 ISTI_ERR_TIMEOUT = 4
 ISTI_ERR_UNSUPPORTED = 5
 
+ARITH_IEEE = 0           # ISTI_ARITH_IEEE
+ARITH_REFERENCE_GPU = 1  # ISTI_ARITH_REFERENCE_GPU
+
 MODE_OURS = 0
 MODE_BACKWARD_BIDIRECTIONAL = 1
 MODE_BACKWARD_UNIDIRECTIONAL = 2
@@ -87,6 +90,9 @@ SIGNATURES = {
     "isti_renderer_tuning_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "isti_renderer_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(IstiTuning)]),
     "isti_render_noalloc": (C.c_int, [C.c_void_p, C.POINTER(IstiRenderInfo), C.POINTER(IstiFrameData), C.c_void_p]),
+    "isti_noalloc_device_status": (C.c_int, [C.POINTER(C.c_int32)]),
+    "isti_renderer_set_arithmetic": (C.c_int, [C.c_void_p, C.c_int32]),
+    "isti_renderer_test_withhold_tile": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_uint32]),
     "isti_render_batch": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(IstiRenderInfo),
                                     C.POINTER(IstiFrameData), C.c_int32, C.c_void_p]),
 }
@@ -153,7 +159,46 @@ METRICS_SIGNATURES = {
 
 FLIP_DEFAULT_PPD = 0.7 * 3840 / 0.7 * 3.141592653589793 / 180  # eval.py: 0.7 m wide 4K screen at 0.7 m
 
-ALL_SIGNATURES = {**SIGNATURES, **IO_SIGNATURES, **DATASET_SIGNATURES, **METRICS_SIGNATURES}
+_VP = C.c_void_p
+# include/isti_unet.h
+UNET_SIGNATURES = {
+    "isti_unet_packed_bytes": (C.c_size_t, [C.c_int32, C.c_int32, C.c_int32]),
+    "isti_unet_pack": (C.c_int, [C.c_int32, _VP, C.c_int32, C.c_int32, C.c_int32, _VP, _VP]),
+    "isti_unet_conv": (C.c_int, [C.c_int32, _VP, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _VP, _VP, _VP, C.c_int32, _VP, C.c_int32,
+                                 _VP, _VP]),
+    "isti_unet_wgrad_scratch_bytes": (C.c_size_t, [C.c_int32] * 6),
+    "isti_unet_wgrad": (C.c_int, [C.c_int32, _VP, _VP, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _VP, C.c_int32, _VP,
+                                  C.c_size_t, _VP, _VP]),
+    "isti_flownet_input_channels": (C.c_int32, []),
+    "isti_flownet_output_channels": (C.c_int32, []),
+    "isti_flownet_num_layers": (C.c_int32, []),
+    "isti_flownet_layer": (C.c_int, [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_int32)]),
+    "isti_flownet_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint64]),
+    "isti_flownet_destroy": (C.c_int, [_VP]),
+    "isti_flownet_tensors": (C.c_int, [_VP, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)]),
+    "isti_flownet_param_offsets": (C.c_int, [_VP, C.c_int32, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    "isti_flownet_sync_params": (C.c_int, [_VP, _VP]),
+    "isti_flownet_forward": (C.c_int, [_VP, _VP, C.c_int32, C.c_int32, C.c_int32, _VP, _VP, _VP]),
+    "isti_flownet_backward": (C.c_int, [_VP, _VP, _VP, C.c_int32, C.c_int32, C.c_int32, _VP]),
+    "isti_flownet_adam": (C.c_int, [_VP, C.c_float, _VP]),
+    "isti_flownet_loss": (C.c_int, [_VP, C.POINTER(C.c_void_p)]),
+    "isti_flownet_device_status": (C.c_int, [_VP, C.POINTER(C.c_int32)]),
+    "isti_render_learned": (C.c_int, [_VP, _VP, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(IstiRenderInfo), C.POINTER(IstiFrameData),
+                                      C.c_int32, _VP]),
+    "isti_renderer_learned_stats": (C.c_int, [_VP, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+}
+
+# include/isti_train.h
+TRAIN_SIGNATURES = {
+    "isti_scene_raycast": (C.c_int, [_VP, C.c_int32, C.c_uint32, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double,
+                                     C.c_double, _VP, _VP, _VP]),
+    "isti_learned_grid": (C.c_int, [C.c_uint32, C.c_uint32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "isti_learned_input": (C.c_int, [_VP, C.c_int32, C.POINTER(IstiRenderInfo), C.POINTER(IstiFrameData), _VP, _VP]),
+    "isti_learned_labels": (C.c_int, [_VP, C.c_int32, _VP, _VP]),
+}
+
+ALL_SIGNATURES = {**SIGNATURES, **IO_SIGNATURES, **DATASET_SIGNATURES, **METRICS_SIGNATURES, **UNET_SIGNATURES, **TRAIN_SIGNATURES}
 
 MAX_BATCH_FRAMES = 8  # ISTI_MAX_BATCH_FRAMES
 

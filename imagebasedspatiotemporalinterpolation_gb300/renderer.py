@@ -191,11 +191,43 @@ class Renderer:
         s = (stream or torch.cuda.current_stream()).cuda_stream
         check(self._lib.isti_render_batch(self._h, n, outs, ris, C.byref(frame_data.to_c()), int(chain), C.c_void_p(s)))
 
+    def render_learned(self, render_buffers, infos, frame_data: DeviceFrame, net=None, iterations: int = 1, stream=None) -> None:
+        """isti_render_learned: the frames of one keyframe pair (main camera only) with the
+        search started from the learned initialiser `net` (a flownet.FlowNet; None = at the
+        output pixel) and `iterations` search steps; tiles left unresolved are rendered by
+        the plain method.  Each buffer is updated in place like isti_render."""
+        torch = _torch()
+        n = len(infos)
+        if n != len(render_buffers) or not 1 <= n <= native.MAX_BATCH_FRAMES:
+            raise ValueError(f"need 1..{native.MAX_BATCH_FRAMES} frames and one buffer per frame")
+        ris = (IstiRenderInfo * n)(*[i if isinstance(i, IstiRenderInfo) else render_info(i) for i in infos])
+        outs = (C.c_void_p * n)(*[_dptr(b) for b in render_buffers])
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        check(self._lib.isti_render_learned(self._h, net.handle if net is not None else None, n, outs, ris,
+                                            C.byref(frame_data.to_c()), int(iterations), C.c_void_p(s)))
+
+    def learned_stats(self) -> tuple[int, int]:
+        """(tiles rendered by the plain method, all tiles) of the last learned call (waits)."""
+        a, b = C.c_int32(), C.c_int32()
+        check(self._lib.isti_renderer_learned_stats(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def device_status(self) -> int:
         """Waits for the device; 0, or ISTI_ERR_TIMEOUT when a kernel's bounded wait gave up."""
         s = C.c_int32()
         check(self._lib.isti_renderer_device_status(self._h, C.byref(s)))
         return s.value
+
+    def set_arithmetic(self, arith: int) -> None:
+        """isti_renderer_set_arithmetic: native.ARITH_IEEE (default, bit-exact against the
+        oracle) or native.ARITH_REFERENCE_GPU (the reference GPU build's -use_fast_math)."""
+        check(self._lib.isti_renderer_set_arithmetic(self._h, int(arith)))
+
+    def test_withhold_tile(self, x: int, y: int, wait_limit: int = 0) -> None:
+        """Failure-detection hook (isti_renderer_test_withhold_tile): the reprojection block
+        covering output pixel (x, y) issues no tile copy, so its bounded wait runs out and
+        the device status turns ISTI_ERR_TIMEOUT.  x < 0 switches it off."""
+        check(self._lib.isti_renderer_test_withhold_tile(self._h, int(x), int(y), int(wait_limit)))
 
     def enable_timing(self, on: bool = True) -> None:
         check(self._lib.isti_renderer_enable_timing(self._h, int(on)))

@@ -31,8 +31,10 @@
  *    intermediates, so use one renderer per concurrently rendering stream.
  *  - Errors are returned, never thrown; isti_last_error() describes the last
  *    failure on the calling thread.
- *  - Arithmetic is IEEE binary32 with every multiply and add rounded
- *    separately (no contraction), so results are reproducible bit for bit.
+ *  - Arithmetic (isti_renderer_set_arithmetic): by default IEEE binary32 with
+ *    every multiply and add rounded separately (no contraction), reproducible
+ *    bit for bit on any host; or the reference GPU build's own arithmetic
+ *    (-use_fast_math), which reproduces that build's results.
  */
 #ifndef ISTI_H
 #define ISTI_H
@@ -178,6 +180,31 @@ typedef struct isti_timing
  * wait inside a kernel gave up (its frame is then not trustworthy). */
 isti_status isti_renderer_device_status(isti_renderer *r, int32_t *device_status);
 
+/* Arithmetic of a renderer's kernels (no counterpart in the reference, which has one
+ * build).  ISTI_ARITH_IEEE (the default): every float operation correctly rounded
+ * and none contracted, in the reference source's operation order -- the results
+ * equal the reference's code executed under IEEE rules (on a CPU) bit for bit.
+ * ISTI_ARITH_REFERENCE_GPU: the kernels compiled as the reference compiles its
+ * renderer (-use_fast_math, CMakeLists.txt:36: approximate division and square
+ * root, flushed denormals, contracted multiply-adds) with the reference's
+ * expression trees -- the results follow the reference's own GPU build.  Takes
+ * effect from the next render; autotuning results are dropped on a change. */
+typedef enum isti_arithmetic
+{
+    ISTI_ARITH_IEEE = 0,
+    ISTI_ARITH_REFERENCE_GPU = 1
+} isti_arithmetic;
+isti_status isti_renderer_set_arithmetic(isti_renderer *r, int32_t arith);
+
+/* Failure-detection test hook (no counterpart in the reference).  From the next
+ * render on, the reprojection block that covers output pixel (x, y) announces its
+ * splat-key tiles but issues no copy, so its bounded wait runs out after
+ * `wait_limit` polls (0: the default limit, seconds at most): the block sets
+ * ISTI_ERR_TIMEOUT in the device status word and leaves without reading a tile or
+ * writing a pixel; every other block renders normally.  Only renders that fetch
+ * their tiles by TMA have such a wait.  x < 0 switches the hook off. */
+isti_status isti_renderer_test_withhold_tile(isti_renderer *r, int32_t x, int32_t y, uint32_t wait_limit);
+
 isti_status isti_renderer_enable_timing(isti_renderer *r, int32_t on);
 /* Waits for the recorded events, returns the sums and resets them. */
 isti_status isti_renderer_timing(isti_renderer *r, isti_timing *out);
@@ -218,16 +245,25 @@ isti_status isti_renderer_tuning(const isti_renderer *r, int32_t index, isti_tun
  * that loads the library until the process exits).
  *
  *  - Limit: the sum over source views of width*height*40 bytes (each buffer
- *    rounded up to 256 bytes) must fit in ISTI_NOALLOC_SCRATCH_BYTES, e.g.
- *    640x360 with up to two aux cameras; larger frames are rejected with
- *    ISTI_ERR_INVALID_ARG.
- *  - The first call on a device looks up the array's device address; make
- *    that first call before any stream capture.
+ *    rounded up to 256 bytes) must fit in ISTI_NOALLOC_SCRATCH_BYTES minus the
+ *    256 bytes of its status word, e.g. 640x360 with up to two aux cameras;
+ *    larger frames are rejected with ISTI_ERR_INVALID_ARG.
+ *  - A call made outside a stream capture looks up the array's device address
+ *    (with the device current) and remembers it; a captured call uses the
+ *    remembered one.  So make the first call on a device, and the first call
+ *    after a device reset, before any stream capture.
  *  - Every call uses the same array and re-initialises the keys itself; calls
  *    whose work overlaps on the GPU (other streams, other threads) race on it,
  *    so serialise them. */
 #define ISTI_NOALLOC_SCRATCH_BYTES (64u << 20)
 isti_status isti_render_noalloc(void *out_rgba, const isti_render_info *info, const isti_frame_data *frame, void *stream);
+
+/* Device-side status of the last isti_render_noalloc call on the current device
+ * (the counterpart of isti_renderer_device_status for the call without a
+ * renderer): waits for the device, then stores ISTI_OK, or ISTI_ERR_TIMEOUT when
+ * a bounded wait inside a kernel gave up (that frame is then not trustworthy).
+ * The word sits at a fixed place in the scratch array; the next call resets it. */
+isti_status isti_noalloc_device_status(int32_t *device_status);
 
 #ifdef __cplusplus
 }

@@ -5,7 +5,10 @@ Two CPU implementations of the reference renderer's per-frame path:
 * ``run_oracle``: isti_oracle.c, a plain C restatement of src/renderer.cu
   (built into oracle/_build/ by ``build()``, here and on the GPU host);
 * ``run_reference``: the reference's own src/renderer.cu compiled for the CPU
-  by build_ref.py (oracle/_ref/, only where the reference tree exists).
+  by build_ref.py (oracle/_ref/, only where the reference tree exists);
+* ``run_reference_gpu`` / ``time_reference_gpu``: the same renderer.cu compiled
+  for the GPU with the reference's CUDA flags (-use_fast_math), from the copy
+  build_ref.py stages under oracle/_ref/gpu/ (oracle/_ref/libisti_ref_gpu.so).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline/reference
 legs use this package, as the checker or as the timed CPU baseline.
@@ -23,6 +26,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_LIB = os.path.join(BUILD_DIR, "libisti_oracle.so")
 REF_LIB = os.path.join(REF_DIR, "libisti_ref.so")
+REF_GPU_LIB = os.path.join(REF_DIR, "libisti_ref_gpu.so")
 
 Mat16 = C.c_float * 16
 
@@ -64,7 +68,10 @@ def build(verbose: bool = False) -> None:
             print(" ".join(cmd))
         subprocess.run(cmd, check=True)
     from . import build_ref
-    build_ref.build(os.environ.get("ISTI_REFERENCE_DIR", "/root/reference"), verbose=verbose)
+    ref = os.environ.get("ISTI_REFERENCE_DIR")
+    if ref:
+        build_ref.build(ref, verbose=verbose)
+    build_ref.build_gpu(verbose=verbose)
 
 
 def mat16(m) -> Mat16:
@@ -172,3 +179,39 @@ def run_reference(frame, client, prev_out=None):
     if rc != 0:
         raise RuntimeError("reference renderer failed")
     return out, splats, cam, full
+
+
+def reference_gpu_available() -> bool:
+    return os.path.exists(REF_GPU_LIB)
+
+
+def run_reference_gpu(frame, client, prev_out=None):
+    """The reference's own renderer.cu built for the GPU with -use_fast_math, on the
+    current CUDA device.  Returns (out, splats, cam_ffs, full_ffs) like run_reference."""
+    lib = _load(REF_GPU_LIB, "isti_refgpu_render")
+    m = _Marshal(frame, client)
+    out = np.zeros((client.height, client.width, 4), np.uint8) if prev_out is None else np.array(prev_out, np.uint8, copy=True)
+    outs, splats, cam, full = _outs(frame)
+    rc = lib.isti_refgpu_render(C.byref(m.frame), C.byref(m.info), C.c_void_p(out.ctypes.data), outs)
+    if rc != 0:
+        raise RuntimeError("reference GPU renderer failed")
+    return out, splats, cam, full
+
+
+def time_reference_gpu(frame, clients, warmup: int = 3, repeats: int = 10) -> np.ndarray:
+    """Per-call device milliseconds of the reference's Renderer::render on the GPU:
+    one Renderer and FrameData kept alive, `warmup` untimed rounds, then `repeats`
+    rounds over the client frames, each call bracketed by CUDA events on the legacy
+    default stream.  Returns an array of repeats * len(clients) times."""
+    lib = _load(REF_GPU_LIB, "isti_refgpu_time")
+    lib.isti_refgpu_time.restype = C.c_int
+    m = _Marshal(frame, clients[0])
+    infos = (OracleRenderInfo * len(clients))(*[
+        OracleRenderInfo(c.width, c.height, c.alpha, mat16(c.viewproj), mat16(c.inv_viewproj), c.frames_per_anchor,
+                         c.shadow_frames_per_anchor, int(c.no_shadows), c.mode) for c in clients])
+    ms = np.zeros(repeats * len(clients), np.float32)
+    rc = lib.isti_refgpu_time(C.byref(m.frame), infos, C.c_int(len(clients)), C.c_int(warmup), C.c_int(repeats),
+                              C.c_void_p(ms.ctypes.data))
+    if rc != 0:
+        raise RuntimeError("reference GPU timing failed")
+    return ms

@@ -1,4 +1,4 @@
-"""Recipe: compile the reference's own src/renderer.cu for the CPU.
+"""Recipe: compile the reference's own src/renderer.cu for the CPU and the GPU.
 
 Test infrastructure.  The reference renderer is CUDA; there is no GPU in the
 build container and the reference sources are not available where the GPU
@@ -12,13 +12,22 @@ oracle/_ref/ (never committed): each kernel launch ``K<<<grid, block>>>(args)``
 becomes ``isti_refhost::launch(grid, block, K)(args)``, which g++ can parse.
 All other lines are compiled as they are.
 
-Usage: python oracle/build_ref.py [--reference /root/reference]
-Writes oracle/_ref/libisti_ref.so.  Exits 0 without building when the
-reference tree is absent.
+GPU build (``stage_gpu`` + ``build_gpu``): unmodified copies of
+src/renderer.cu and the headers it includes are staged under oracle/_ref/gpu/
+(never committed; they travel with the working tree to the GPU host, where the
+reference tree itself is absent), and ``build_gpu`` compiles them with
+ref_gpu/ref_gpu_driver.cu by nvcc for sm_103a with the reference's own CUDA
+flags (CMakeLists.txt:36 minus -keep) into oracle/_ref/libisti_ref_gpu.so.
+
+Usage: python oracle/build_ref.py --reference <reference tree>
+       (or ISTI_REFERENCE_DIR=<reference tree> python oracle/build_ref.py)
+Writes oracle/_ref/libisti_ref.so, stages oracle/_ref/gpu/ and, where nvcc is
+available, builds oracle/_ref/libisti_ref_gpu.so.
 """
 import argparse
 import os
 import re
+import shutil
 import subprocess
 import sys
 
@@ -29,6 +38,52 @@ LAUNCH_RE = re.compile(r"([A-Za-z_]\w*(?:\s*<[^<>;()]*>)?)\s*<<<(.*?)>>>")
 
 def rewrite_launches(src: str) -> tuple[str, int]:
     return LAUNCH_RE.subn(lambda m: f"isti_refhost::launch({m.group(2)}, {m.group(1)})", src)
+
+
+GPU_DIR = os.path.join(OUT_DIR, "gpu")
+GPU_LIB = os.path.join(OUT_DIR, "libisti_ref_gpu.so")
+# src/renderer.cu and everything it includes from the reference's include/ tree
+GPU_SOURCES = ["src/renderer.cu", "include/renderer.h", "include/data.h", "include/util/image_buffer.h",
+               "include/util/helper_common.h", "include/util/helper_math.h", "include/util/helper_math_ext.h",
+               "include/util/cuda_helper_device.h", "include/util/cuda_helper_host.h"]
+
+
+def stage_gpu(reference: str, verbose: bool = False) -> bool:
+    """Copies the reference sources of the GPU build under oracle/_ref/gpu/, unmodified."""
+    if not all(os.path.isfile(os.path.join(reference, f)) for f in GPU_SOURCES):
+        return False
+    for f in GPU_SOURCES:
+        dst = os.path.join(GPU_DIR, "renderer.cu" if f == "src/renderer.cu" else f)
+        os.makedirs(os.path.dirname(dst), exist_ok=True)
+        src = os.path.join(reference, f)
+        if not os.path.exists(dst) or open(src, "rb").read() != open(dst, "rb").read():
+            shutil.copyfile(src, dst)
+    if verbose:
+        print(f"staged {len(GPU_SOURCES)} reference files under {GPU_DIR}")
+    return True
+
+
+def build_gpu(verbose: bool = False) -> str | None:
+    """Compiles the staged reference renderer for sm_103a (no GPU needed to build)."""
+    renderer = os.path.join(GPU_DIR, "renderer.cu")
+    driver = os.path.join(HERE, "ref_gpu", "ref_gpu_driver.cu")
+    nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    if not os.path.isfile(renderer) or not os.path.isfile(nvcc):
+        return None
+    deps = [renderer, driver, os.path.join(HERE, "isti_oracle.h"), os.path.join(HERE, "ref_host", "glm", "glm.hpp")]
+    if os.path.exists(GPU_LIB) and os.path.getmtime(GPU_LIB) > max(os.path.getmtime(d) for d in deps):
+        return GPU_LIB
+    cmd = [nvcc, "-std=c++20", "-O3", "-gencode=arch=compute_103a,code=sm_103a",
+           # the reference's CUDA flags, CMakeLists.txt:36 (without -keep and --ptxas-options=-v)
+           "-Xcompiler", "-D_FORCE_INLINES", "-DVERBOSE", "--expt-extended-lambda", "-use_fast_math",
+           "--expt-relaxed-constexpr",
+           "-Xcompiler", "-fPIC", "-shared", "-w",
+           "-I", GPU_DIR, "-I", os.path.join(GPU_DIR, "include"), "-I", os.path.join(HERE, "ref_host"),
+           driver, "-o", GPU_LIB]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.run(cmd, check=True)
+    return GPU_LIB
 
 
 def build(reference: str, verbose: bool = False) -> str | None:
@@ -67,6 +122,7 @@ def build(reference: str, verbose: bool = False) -> str | None:
         print(" ".join(cmd))
     subprocess.run(cmd, check=True)
     build_io(reference, verbose)
+    stage_gpu(reference, verbose)
     return lib
 
 
@@ -93,11 +149,16 @@ def build_io(reference: str, verbose: bool = False) -> str | None:
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("ISTI_REFERENCE_DIR"))
     args = ap.parse_args()
+    if not args.reference:
+        ap.error("give --reference or set ISTI_REFERENCE_DIR")
     lib = build(args.reference, verbose=True)
     if lib:
         print(f"built {lib}")
+    gpu = build_gpu(verbose=True)
+    if gpu:
+        print(f"built {gpu}")
     return 0
 
 

@@ -19,6 +19,14 @@
 
 #include <cmath>
 
+// Device-callable where nvcc compiles the reference for the GPU (as genuine glm
+// does under CUDA); plain host functions for the host build.
+#ifdef __CUDACC__
+#define ISTI_GLM_HD __host__ __device__
+#else
+#define ISTI_GLM_HD
+#endif
+
 namespace glm
 {
 struct vec4;
@@ -26,69 +34,69 @@ struct vec4;
 struct vec3
 {
     float x, y, z;
-    vec3() : x(0.f), y(0.f), z(0.f) {}
-    explicit vec3(float s) : x(s), y(s), z(s) {}
-    vec3(float a, float b, float c) : x(a), y(b), z(c) {}
-    vec3(const vec4 &v);  // implicit narrowing copy of xyz, as glm allows
-    float &operator[](int i) { return (&x)[i]; }
-    const float &operator[](int i) const { return (&x)[i]; }
+    ISTI_GLM_HD vec3() : x(0.f), y(0.f), z(0.f) {}
+    ISTI_GLM_HD explicit vec3(float s) : x(s), y(s), z(s) {}
+    ISTI_GLM_HD vec3(float a, float b, float c) : x(a), y(b), z(c) {}
+    ISTI_GLM_HD vec3(const vec4 &v);  // implicit narrowing copy of xyz, as glm allows
+    ISTI_GLM_HD float &operator[](int i) { return (&x)[i]; }
+    ISTI_GLM_HD const float &operator[](int i) const { return (&x)[i]; }
 };
 
 struct vec4
 {
     float x, y, z, w;
-    vec4() : x(0.f), y(0.f), z(0.f), w(0.f) {}
-    explicit vec4(float s) : x(s), y(s), z(s), w(s) {}
-    vec4(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
-    vec4(const vec3 &v, float d) : x(v.x), y(v.y), z(v.z), w(d) {}
-    float &operator[](int i) { return (&x)[i]; }
-    const float &operator[](int i) const { return (&x)[i]; }
+    ISTI_GLM_HD vec4() : x(0.f), y(0.f), z(0.f), w(0.f) {}
+    ISTI_GLM_HD explicit vec4(float s) : x(s), y(s), z(s), w(s) {}
+    ISTI_GLM_HD vec4(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
+    ISTI_GLM_HD vec4(const vec3 &v, float d) : x(v.x), y(v.y), z(v.z), w(d) {}
+    ISTI_GLM_HD float &operator[](int i) { return (&x)[i]; }
+    ISTI_GLM_HD const float &operator[](int i) const { return (&x)[i]; }
 };
 
-inline vec3::vec3(const vec4 &v) : x(v.x), y(v.y), z(v.z) {}
+ISTI_GLM_HD inline vec3::vec3(const vec4 &v) : x(v.x), y(v.y), z(v.z) {}
 
-inline vec4 operator+(const vec4 &a, const vec4 &b) { return vec4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
-inline vec4 operator-(const vec4 &a, const vec4 &b) { return vec4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
-inline vec4 operator-(const vec4 &a) { return vec4(-a.x, -a.y, -a.z, -a.w); }
-inline vec4 operator*(const vec4 &a, float s) { return vec4(a.x * s, a.y * s, a.z * s, a.w * s); }
-inline vec4 operator*(float s, const vec4 &a) { return vec4(s * a.x, s * a.y, s * a.z, s * a.w); }
-inline vec4 operator*(const vec4 &a, const vec4 &b) { return vec4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
-inline vec4 operator/(const vec4 &a, float s) { return vec4(a.x / s, a.y / s, a.z / s, a.w / s); }
+ISTI_GLM_HD inline vec4 operator+(const vec4 &a, const vec4 &b) { return vec4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+ISTI_GLM_HD inline vec4 operator-(const vec4 &a, const vec4 &b) { return vec4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
+ISTI_GLM_HD inline vec4 operator-(const vec4 &a) { return vec4(-a.x, -a.y, -a.z, -a.w); }
+ISTI_GLM_HD inline vec4 operator*(const vec4 &a, float s) { return vec4(a.x * s, a.y * s, a.z * s, a.w * s); }
+ISTI_GLM_HD inline vec4 operator*(float s, const vec4 &a) { return vec4(s * a.x, s * a.y, s * a.z, s * a.w); }
+ISTI_GLM_HD inline vec4 operator*(const vec4 &a, const vec4 &b) { return vec4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
+ISTI_GLM_HD inline vec4 operator/(const vec4 &a, float s) { return vec4(a.x / s, a.y / s, a.z / s, a.w / s); }
 
-inline vec3 operator+(const vec3 &a, const vec3 &b) { return vec3(a.x + b.x, a.y + b.y, a.z + b.z); }
-inline vec3 operator-(const vec3 &a, const vec3 &b) { return vec3(a.x - b.x, a.y - b.y, a.z - b.z); }
-inline vec3 operator-(const vec3 &a) { return vec3(-a.x, -a.y, -a.z); }
-inline vec3 operator*(const vec3 &a, float s) { return vec3(a.x * s, a.y * s, a.z * s); }
-inline vec3 operator*(float s, const vec3 &a) { return vec3(s * a.x, s * a.y, s * a.z); }
-inline vec3 operator/(const vec3 &a, float s) { return vec3(a.x / s, a.y / s, a.z / s); }
+ISTI_GLM_HD inline vec3 operator+(const vec3 &a, const vec3 &b) { return vec3(a.x + b.x, a.y + b.y, a.z + b.z); }
+ISTI_GLM_HD inline vec3 operator-(const vec3 &a, const vec3 &b) { return vec3(a.x - b.x, a.y - b.y, a.z - b.z); }
+ISTI_GLM_HD inline vec3 operator-(const vec3 &a) { return vec3(-a.x, -a.y, -a.z); }
+ISTI_GLM_HD inline vec3 operator*(const vec3 &a, float s) { return vec3(a.x * s, a.y * s, a.z * s); }
+ISTI_GLM_HD inline vec3 operator*(float s, const vec3 &a) { return vec3(s * a.x, s * a.y, s * a.z); }
+ISTI_GLM_HD inline vec3 operator/(const vec3 &a, float s) { return vec3(a.x / s, a.y / s, a.z / s); }
 
-inline float dot(const vec3 &a, const vec3 &b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
-inline float dot(const vec4 &a, const vec4 &b) { return ((a.x * b.x + a.y * b.y) + a.z * b.z) + a.w * b.w; }
-inline vec3 normalize(const vec3 &v) { return v * (1.0f / std::sqrt(dot(v, v))); }
-inline vec4 normalize(const vec4 &v) { return v * (1.0f / std::sqrt(dot(v, v))); }
+ISTI_GLM_HD inline float dot(const vec3 &a, const vec3 &b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+ISTI_GLM_HD inline float dot(const vec4 &a, const vec4 &b) { return ((a.x * b.x + a.y * b.y) + a.z * b.z) + a.w * b.w; }
+ISTI_GLM_HD inline vec3 normalize(const vec3 &v) { return v * (1.0f / sqrtf(dot(v, v))); }
+ISTI_GLM_HD inline vec4 normalize(const vec4 &v) { return v * (1.0f / sqrtf(dot(v, v))); }
 
 struct mat4
 {
     vec4 value[4];
-    mat4() : value{vec4(1.f, 0.f, 0.f, 0.f), vec4(0.f, 1.f, 0.f, 0.f), vec4(0.f, 0.f, 1.f, 0.f), vec4(0.f, 0.f, 0.f, 1.f)} {}
-    explicit mat4(float s) : value{vec4(s, 0.f, 0.f, 0.f), vec4(0.f, s, 0.f, 0.f), vec4(0.f, 0.f, s, 0.f), vec4(0.f, 0.f, 0.f, s)} {}
-    mat4(const vec4 &c0, const vec4 &c1, const vec4 &c2, const vec4 &c3) : value{c0, c1, c2, c3} {}
+    ISTI_GLM_HD mat4() : value{vec4(1.f, 0.f, 0.f, 0.f), vec4(0.f, 1.f, 0.f, 0.f), vec4(0.f, 0.f, 1.f, 0.f), vec4(0.f, 0.f, 0.f, 1.f)} {}
+    ISTI_GLM_HD explicit mat4(float s) : value{vec4(s, 0.f, 0.f, 0.f), vec4(0.f, s, 0.f, 0.f), vec4(0.f, 0.f, s, 0.f), vec4(0.f, 0.f, 0.f, s)} {}
+    ISTI_GLM_HD mat4(const vec4 &c0, const vec4 &c1, const vec4 &c2, const vec4 &c3) : value{c0, c1, c2, c3} {}
     // 16 scalars, column by column
-    mat4(float x0, float y0, float z0, float w0, float x1, float y1, float z1, float w1,
+    ISTI_GLM_HD mat4(float x0, float y0, float z0, float w0, float x1, float y1, float z1, float w1,
          float x2, float y2, float z2, float w2, float x3, float y3, float z3, float w3)
         : value{vec4(x0, y0, z0, w0), vec4(x1, y1, z1, w1), vec4(x2, y2, z2, w2), vec4(x3, y3, z3, w3)} {}
-    vec4 &operator[](int c) { return value[c]; }
-    const vec4 &operator[](int c) const { return value[c]; }
+    ISTI_GLM_HD vec4 &operator[](int c) { return value[c]; }
+    ISTI_GLM_HD const vec4 &operator[](int c) const { return value[c]; }
 };
 
-inline vec4 operator*(const mat4 &m, const vec4 &v)
+ISTI_GLM_HD inline vec4 operator*(const mat4 &m, const vec4 &v)
 {
     const vec4 a = m[0] * v.x + m[1] * v.y;
     const vec4 b = m[2] * v.z + m[3] * v.w;
     return a + b;
 }
 
-inline mat4 operator*(const mat4 &a, const mat4 &b)
+ISTI_GLM_HD inline mat4 operator*(const mat4 &a, const mat4 &b)
 {
     return mat4(a * b[0], a * b[1], a * b[2], a * b[3]);
 }

@@ -23,6 +23,14 @@ from imagebasedspatiotemporalinterpolation_gb300.scene import Sequence  # noqa: 
 from tests.golden import fixtures  # noqa: E402
 
 
+def reference_dir() -> str:
+    """The reference tree, named by the ISTI_REFERENCE_DIR environment variable."""
+    ref = os.environ.get("ISTI_REFERENCE_DIR")
+    if not ref or not os.path.isdir(ref):
+        raise SystemExit("set ISTI_REFERENCE_DIR to the reference tree")
+    return ref
+
+
 def pattern(h, w):
     y, x = np.mgrid[0:h, 0:w]
     return np.stack([(x * 7) % 256, (y * 13) % 256, (x + y) % 256, np.full_like(x, 255)], -1).astype(np.uint8)
@@ -138,14 +146,14 @@ def io_cases():
     print(f"io: {len(expected)} files")
 
 
-def metrics_cases(reference="/root/reference"):
+def metrics_cases(reference=None):
     """PSNR / SSIM of seeded image pairs by the reference's own evaluation code:
     scripts/loss_utils.ssim and eval.py's psnr_fn (torch, CPU), on (1, 3, H, W)
     float tensors of the RGB bytes / 255 as eval.py's loader makes them."""
     import torch
     import torch.nn.functional as F
 
-    sys.path.insert(0, os.path.join(reference, "scripts"))
+    sys.path.insert(0, os.path.join(reference or reference_dir(), "scripts"))
     from loss_utils import ssim  # the reference's implementation
 
     rng = np.random.default_rng(77)
@@ -171,7 +179,7 @@ def metrics_cases(reference="/root/reference"):
     print(f"metrics: {len(pairs)} pairs")
 
 
-def flip_cases(reference="/root/reference"):
+def flip_cases(reference=None):
     """LDR-FLIP (eval.py's flip_fn(render, ground_truth)) of the metric pairs plus an
     interpolated frame against its analytic ground truth, computed by the
     reference's scripts/flip_loss.py.  That file places every tensor on 'cuda';
@@ -179,7 +187,7 @@ def flip_cases(reference="/root/reference"):
     torch.zeros redirected for the duration of the call."""
     import torch
 
-    sys.path.insert(0, os.path.join(reference, "scripts"))
+    sys.path.insert(0, os.path.join(reference or reference_dir(), "scripts"))
     pairs = dict(np.load(os.path.join(fixtures.GOLDEN_DIR, "metrics", "pairs.npz")))
     names = [k[:-2] for k in pairs if k.endswith("_a")]
     seq = Sequence(96, 54, 2, seed=21, aux_offsets=(-0.3, 0.3), shadows=True, max_speed=2.0)

@@ -13,7 +13,8 @@ import pytest
 from imagebasedspatiotemporalinterpolation_gb300 import _build, native
 
 HEADER = os.path.join(_build.INCLUDE, "isti.h")
-HEADERS = [os.path.join(_build.INCLUDE, h) for h in ("isti.h", "isti_io.h", "isti_dataset.h", "isti_metrics.h")]
+HEADERS = [os.path.join(_build.INCLUDE, h) for h in ("isti.h", "isti_io.h", "isti_dataset.h", "isti_metrics.h", "isti_unet.h",
+                                                    "isti_train.h")]
 
 
 def declared_functions(path):
