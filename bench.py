@@ -68,8 +68,13 @@ def parse():
     ap.add_argument("--no-quality", action="store_true", help="skip PSNR / SSIM against the analytic ground truth")
     ap.add_argument("--no-graph-batch", action="store_true", help="skip the mixed-resolution batch under a CUDA graph")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving loop with simulated clients")
-    ap.add_argument("--serve-seconds", type=float, default=10.0, help="real time of the serving loop (the config runs 60 s)")
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="real time of the serving loop (the configuration's 60 s)")
+    ap.add_argument("--serve-learned", type=int, default=1, help="serve with the learned initialiser when its weights exist")
     ap.add_argument("--serve-slots", type=int, default=4, help="concurrent batches (streams) of the serving loop")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-initialiser comparison")
+    ap.add_argument("--no-config1", action="store_true", help="skip the 640x360 configuration")
+    ap.add_argument("--no-reference-gpu", action="store_true", help="skip timing the reference's own GPU build")
+    ap.add_argument("--clock-log", default=None, help="write the raw nvidia-smi clock samples of the timed region to this CSV")
     return ap.parse_args()
 
 
@@ -101,10 +106,10 @@ def profile_traffic(kernel: str):
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
 
-    def __init__(self, index: int):
+    def __init__(self, index: int, path: str | None = None):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else None
+        self.path = path  # raw samples are written here when given (--clock-log)
 
     def start(self):
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
@@ -285,7 +290,7 @@ def main_ours(args):
     # ---- timed region (device-resident inputs): one batched call per keyframe interval
     sev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    clocks = ClockSampler(local)
+    clocks = ClockSampler(local, args.clock_log)
     r.timing()          # discard warm-up
     r.enable_timing(True)
     if world > 1:
@@ -344,6 +349,13 @@ def main_ours(args):
     serving = None
     if not args.no_serving:
         serving = run_serving(args, dev, rank)
+
+    # ---- learned initialiser vs plain at 1080p, configuration 1, the reference's own GPU build
+    learned = None if args.no_learned else run_learned(args, dev, rank)
+    config1 = None if args.no_config1 else run_config1(args, dev, rank)
+    reference_gpu = None
+    if rank == 0 and not args.no_reference_gpu:
+        reference_gpu = run_reference_gpu(args, dev, seq, per_frame["p50_frame_ms"] if per_frame else None)
 
     # ---- roofline of the dominant kernel.  Algorithmic bytes per interpolated output pixel
     # (the per-unit figure of the path): every source view's inputs once and the output once,
@@ -425,6 +437,9 @@ def main_ours(args):
                                     "splat_kernel": round(per_launch_ms["splat_kernel"], 4),
                                     "reproj_kernel": round(per_launch_ms["reproj_kernel"], 4)},
             "per_frame_api": per_frame,
+            "learned_vs_plain": learned,
+            "config1": config1,
+            "reference_gpu": reference_gpu,
             "graph_batch_mixed": graph_batch,
             "serving": serving,
             "gpu_launches": tim["kernel_launches"],
@@ -439,6 +454,167 @@ def main_ours(args):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def run_reference_gpu(args, dev, seq, ours_frame_ms):
+    """The reference's own renderer.cu built for sm_103a with its -use_fast_math flags
+    (oracle/_ref/libisti_ref_gpu.so, staged from the reference sources), timed on this GPU
+    as its frame loop runs it: one Renderer::render per client frame on the legacy default
+    stream (its memsets, splat launches, host synchronisation, aux-info copy and
+    reprojection launch), CUDA events around each call.  Same keyframes and client frames
+    as the main workload.  A baseline reported beside the line, not the measured product."""
+    import numpy as np
+
+    import oracle
+    if not oracle.reference_gpu_available():
+        return {"unavailable": "reference sources not staged (oracle/build_ref.py needs the reference tree)"}
+    out = {}
+    for name, (sq, ts) in {"config2_1080p_6views_shadows": (seq, TS)}.items():
+        frame = sq.frame(0)
+        ms = oracle.time_reference_gpu(frame, [sq.client(0, b) for b in ts], warmup=max(3, args.warmup), repeats=10)
+        p50 = float(np.median(ms))
+        out[name] = {"ms_per_frame_p50": round(p50, 4), "ms_per_frame_p99": round(float(np.percentile(ms, 99)), 4),
+                     "mpix_s": round(sq.width * sq.height / 1e6 / (p50 / 1e3), 2), "frames_timed": int(ms.size)}
+    out["config2_1080p_6views_shadows"]["ours_per_frame_call_ms_p50"] = ours_frame_ms
+    out["build"] = "src/renderer.cu unmodified, nvcc -arch sm_103a -use_fast_math --expt-relaxed-constexpr (CMakeLists.txt:36)"
+    return out
+
+
+def run_config1(args, dev, rank):
+    """Benchmark configuration 1: one interpolated frame at t = 0.5 between two 640x360
+    keyframes, main camera only, mode 0, no shadows.  Device-resident keyframes, one
+    isti_render call per step on 5 resident pairs in turn; the reference GPU build and the
+    CPU port (the C oracle, all threads) timed on the same frames."""
+    import numpy as np
+    import torch
+
+    from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame, Renderer
+    from imagebasedspatiotemporalinterpolation_gb300.scene import Sequence
+    import oracle
+
+    w, h, pairs = 640, 360, 5
+    seq = Sequence(w, h, pairs + 1, seed=args.seed + 11 + rank)
+    frames = [DeviceFrame.from_host(seq.frame(p), dev) for p in range(pairs)]
+    clients = [seq.client(p, 2) for p in range(pairs)]
+    out = torch.zeros((h, w, 4), dtype=torch.uint8, device=dev)
+    r = Renderer()
+    for s in range(max(3, args.warmup)):
+        r.render(out, clients[s % pairs], frames[s % pairs])
+    n = max(60, args.steps * 3)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+    torch.cuda.synchronize()
+    for s, (a, b) in enumerate(ev):
+        a.record()
+        r.render(out, clients[s % pairs], frames[s % pairs])
+        b.record()
+    torch.cuda.synchronize()
+    ms = sorted(a.elapsed_time(b) for a, b in ev)
+    r.close()
+    res = {"workload": "640x360, main camera only, t = 0.5, mode 0, no shadows (one isti_render call per frame)",
+           "mpix_s": round(n * w * h / 1e6 / (sum(ms) / 1e3), 2), "p50_frame_ms": round(ms[len(ms) // 2], 4),
+           "p99_frame_ms": round(ms[min(len(ms) - 1, int(0.99 * len(ms)))], 4)}
+    if rank == 0 and oracle.reference_gpu_available():
+        rg = oracle.time_reference_gpu(seq.frame(0), [clients[0]], warmup=5, repeats=30)
+        res["reference_gpu_ms_per_frame_p50"] = round(float(np.median(rg)), 4)
+    if rank == 0 and not args.no_cpu_baseline:
+        oracle.build()
+        fr = seq.frame(0)
+        call = oracle.prepared_call(fr, clients[0], np.zeros((h, w, 4), np.uint8))
+        call()
+        t0, k = time.perf_counter(), 0
+        while time.perf_counter() - t0 < min(args.cpu_seconds, 5.0) or k == 0:
+            call()
+            k += 1
+        secs = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": round(k * w * h / 1e6 / secs, 3), "unit": "Mpix/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"{k} frames ({secs:.1f} s), C oracle (OpenMP, all threads)"}
+    return res
+
+
+def run_learned(args, dev, rank):
+    """Learned initialiser vs the plain method (benchmark configuration 4's evaluation):
+    1920x1080 held-out seeds of the training distribution (U[16, 256] spheres, |v| <= 1
+    m/s, camera rotation <= 5 degrees per keyframe interval), main camera only, t in
+    {0.25, 0.5, 0.75}.  Per step one call renders the 3 frames of a keyframe pair: the plain
+    path (isti_render_batch: splat + 3x3 window + 3 search iterations) or the learned path
+    (isti_render_learned: U-Net on tcgen05 + 1 search iteration + per-tile plain fallback),
+    on the same device-resident keyframes.  Quality: PSNR of each frame against the analytic
+    ray-cast of the client camera at its time, previous output = the previous ground truth
+    frame (temporal hole filling), for both paths."""
+    import numpy as np
+    import torch
+
+    from imagebasedspatiotemporalinterpolation_gb300 import train_flownet
+    from imagebasedspatiotemporalinterpolation_gb300.metrics import Quality
+    from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame, Renderer
+    from imagebasedspatiotemporalinterpolation_gb300.scene import Sequence
+
+    if not os.path.exists(train_flownet.DEFAULT_WEIGHTS):
+        return {"unavailable": "no trained weights (run train_flownet)"}
+    net = train_flownet.load()
+    w, h, n_seeds = 1920, 1080, 2
+    seqs, frames, clients, truths, prevs = [], [], [], [], []
+    for i in range(n_seeds):
+        seed = train_flownet.EVAL_SEED_BASE + 7 + i
+        rng = np.random.default_rng(seed)
+        sq = Sequence(w, h, 2, seed=seed, n_spheres=int(rng.integers(16, 257)), max_speed=1.0, max_rot_deg=5.0, max_step_m=0.1)
+        seqs.append(sq)
+        frames.append(DeviceFrame.from_host(sq.frame(0), dev))
+        clients.append([sq.client(0, b) for b in TS])
+        gt = [torch.from_numpy(sq.ground_truth(0, b)).to(dev) for b in [0] + list(TS)]
+        gt[0] = torch.from_numpy(sq.frame(0).fwd.color).to(dev)
+        truths.append(gt[1:])
+        prevs.append(gt[:-1])
+    r = Renderer()
+    outs = [torch.zeros((h, w, 4), dtype=torch.uint8, device=dev) for _ in TS]
+    paths = {"plain": lambda i: r.render_batch(outs, clients[i], frames[i], chain=False),
+             "learned": lambda i: r.render_learned(outs, clients[i], frames[i], net, 1)}
+    res = {}
+    for name, fn in paths.items():
+        for s in range(max(3, args.warmup)):
+            fn(s % n_seeds)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for s, (a, b) in enumerate(ev):
+            a.record()
+            fn(s % n_seeds)
+            b.record()
+        t1.record()
+        torch.cuda.synchronize()
+        ms = sorted(a.elapsed_time(b) for a, b in ev)
+        total = t0.elapsed_time(t1)
+        res[name] = {"mpix_s": round(args.steps * len(TS) * w * h / 1e6 / (total / 1e3), 2), "p50_call_ms": round(ms[len(ms) // 2], 4),
+                     "p99_call_ms": round(ms[min(len(ms) - 1, int(0.99 * len(ms)))], 4)}
+    # quality (outside the timed regions)
+    q = Quality(w, h, dev)
+    psnr = {k: [] for k in paths}
+    vs_plain, fallback = [], []
+    for i in range(n_seeds):
+        got = {}
+        for name in paths:
+            o = [p.clone() for p in prevs[i]]
+            if name == "plain":
+                r.render_batch(o, clients[i], frames[i], chain=False)
+            else:
+                r.render_learned(o, clients[i], frames[i], net, 1)
+                fb, tiles = r.learned_stats()
+                fallback.append(fb / max(1, tiles))
+            got[name] = o
+            psnr[name] += [q(a, t)["psnr"] for a, t in zip(o, truths[i])]
+        vs_plain += [q(a, b)["psnr"] for a, b in zip(got["learned"], got["plain"])]
+    r.close()
+    net.close()
+    mean = lambda v: float(sum(v) / len(v))
+    res["ratio_learned_over_plain"] = round(res["learned"]["mpix_s"] / res["plain"]["mpix_s"], 3)
+    res["psnr_vs_truth_db"] = {k: round(mean(v), 3) for k, v in psnr.items()}
+    res["dpsnr_db"] = round(mean(psnr["plain"]) - mean(psnr["learned"]), 3)
+    res["psnr_learned_vs_plain_db"] = round(mean([v for v in vs_plain if v != float("inf")] or [float("inf")]), 2)
+    res["fallback_tile_frac"] = round(mean(fallback), 4)
+    res["workload"] = ("1920x1080 held-out seeds, main camera only, 3 frames (t = 0.25/0.5/0.75) per call, "
+                       "learned: 1 search iteration (plain: 3) + per-tile plain fallback")
+    return res
 
 
 GB_RES = ((1280, 720), (1920, 1080), (2064, 2208))
@@ -469,15 +645,21 @@ def run_serving(args, dev, rank):
         seq = scene.Sequence(w, h, 3, seed=args.seed + 301 * (j + 1) + rank)
         seqs[(w, h)] = (seq, [PinnedPair(seq.frame(p)) for p in range(2)])
     max_w, max_h = max(GB_RES, key=lambda r: r[0] * r[1])
-    server = Server(CudaBackend(dev), hbm_budget=120 << 30, n_slots=args.serve_slots, max_batch=8,
+    from imagebasedspatiotemporalinterpolation_gb300 import train_flownet
+    weights = train_flownet.DEFAULT_WEIGHTS if (args.serve_learned and os.path.exists(train_flownet.DEFAULT_WEIGHTS)) else None
+    backend = CudaBackend(dev, learned_weights=weights)
+    server = Server(backend, hbm_budget=120 << 30, n_slots=args.serve_slots, max_batch=8,
                     slot_pixels=max_w * max_h, slot_views=2)
-    # every slot's renderer sized once for the largest batch (no allocation while serving)
+    # every slot's renderer (and network) sized once for the largest batch (no allocation while serving)
     big_seq = seqs[(max_w, max_h)][0]
     big = DeviceFrame.from_host(big_seq.frame(0), dev)
     outs = [torch.zeros((max_h, max_w, 4), dtype=torch.uint8, device=dev) for _ in range(8)]
     infos = [eye_info(big_seq, 0, b / 8, GB_EYES[0]) for b in range(8)]
-    for stream, renderer in server.slots:
+    for slot in server.slots:
+        stream, renderer = slot[0], slot[1]
         renderer.render_batch(outs, infos, big, chain=True, stream=stream)
+        if len(slot) > 2:
+            renderer.render_learned(outs, infos, big, slot[2], 1, chain=True, stream=stream)
     torch.cuda.synchronize()
     del outs, big
     sims = []
@@ -493,8 +675,10 @@ def run_serving(args, dev, rank):
             "batches": st["batches"], "frames_per_batch": round(st["frames_per_batch"], 2), "keyframe_uploads": st["uploads"],
             "clients": st["clients"], "admitted": st["admitted"], "seconds": args.serve_seconds,
             "reserved_gb": round(st["peak_reserved_bytes"] / 2**30, 2), "budget_gb": 120, "slots": args.serve_slots,
+            "method": "learned initialiser (1 iteration) + per-tile plain fallback" if weights else "plain",
+            "learned_batches": backend.learned_batches, "plain_batches": backend.plain_batches,
             "workload": "16 clients, stereo requests Poisson U[90,120] Hz, keyframe pairs 30 Hz, 1280x720 / 1920x1080 / "
-                        "2064x2208 per eye, main camera only, plain method, continuous batching"}
+                        "2064x2208 per eye, main camera only, continuous batching"}
 
 
 def run_graph_batch(args, dev, rank):

@@ -13,7 +13,7 @@
 //   s2 = up2(conv1x1 96->64 (d3)) + e2     d2 = relu(conv3x3 64->64)(s2)
 //   s1 = up2(conv1x1 64->32 (d2)) + e1     d1 = relu(conv3x3 32->32)(s1)
 //   flow = conv1x1 32->4 (d1)              [H,W,4] f32
-// 10 tensor-core layers + the head: 338,660 parameters.
+// 10 tensor-core layers + the head: 339,268 parameters.
 #include "isti_unet.h"
 #include "isti_unet_ops.h"
 #include "host/isti_error.hpp"

@@ -50,6 +50,8 @@ struct LearnedParams
     int32_t tiles_x, tiles_y;
     uint32_t *tile_flags;       // [frame][tiles_y][tiles_x]: 1 = the plain method renders this tile
     int32_t *fallback_count;    // marked tiles (all frames)
+    uint32_t *tile_list;        // the marked tiles' flag indices, fallback_count of them (any order)
+    uint8_t *valid;             // [frame][h][w]: 1 where the frame wrote a pixel (chained outputs only)
 };
 
 // client-camera position of source pixel (sx, sy) of view v for frame k: the splat kernel's
@@ -195,68 +197,113 @@ __device__ __forceinline__ bool learned_resolve(const LearnedParams &p, int k, c
 
 constexpr bool LEARNED_SQ = true; // squared errors (as the plain path's 2-view launch)
 
+// Next search position from an approximate client-camera flow (contracted multiply-adds, fast
+// division): the intermediate steps of the learned search only choose the next pixel; the
+// final step, whose error, depth and colour are kept, is exact.
+__device__ __forceinline__ void learned_step_approx(const LearnedParams &p, int v, int k, float qx, float qy, uint32_t &sx, uint32_t &sy)
+{
+    const DevView &dv = p.fp.v[v];
+    const uint32_t i = sy * dv.w + sx;
+    const float4 a = __ldg(p.ws[v] + i), d = __ldg(p.dws[v] + i);
+    const float wg = dv.forward ? p.fp.f[k].alpha : 1.0f - p.fp.f[k].alpha;
+    const float *m = p.fp.cam_vp[k];
+    const float x = fmaf(wg, d.x, a.x), y = fmaf(wg, d.y, a.y), z = fmaf(wg, d.z, a.z), w = fmaf(wg, d.w, a.w);
+    const float cx = fmaf(m[0], x, fmaf(m[4], y, fmaf(m[8], z, m[12] * w)));
+    const float cy = fmaf(m[1], x, fmaf(m[5], y, fmaf(m[9], z, m[13] * w)));
+    const float cw = fmaf(m[3], x, fmaf(m[7], y, fmaf(m[11], z, m[15] * w)));
+    const float mx = __fdividef(cx, cw) - __ldg(dv.lut + sx), my = __fdividef(cy, cw) - __ldg(dv.lut + dv.w + sy);
+    const int2 t = cs2pixel(qx - mx, qy - my, dv.w, dv.h);
+    if (in_range(t, dv.w, dv.h))
+    {
+        sx = (uint32_t)t.x;
+        sy = (uint32_t)t.y;
+    }
+}
+
+// One thread per output pixel handles every frame of the call (a pixel's sources for the
+// frames lie close together: the keyframe data stay in L1), both keyframes interleaved.
 __global__ void __launch_bounds__(LT_W *LT_H) learned_kernel(const __grid_constant__ LearnedParams p)
 {
-    const int k = blockIdx.z;
     const uint32_t x = blockIdx.x * LT_W + threadIdx.x, y = blockIdx.y * LT_H + threadIdx.y;
     const bool inb = x < p.fp.out_w && y < p.fp.out_h;
     const DevView &a = p.fp.v[0], &b = p.fp.v[1];
-    bool fail = false, ok = false;
-    uint32_t color = 0;
-    if (inb)
+    const float qx = inb ? __ldg(a.lut + x) : 0.0f, qy = inb ? __ldg(a.lut + a.w + y) : 0.0f; // pixel2CS of the output pixel
+    const uint32_t qxi = min(x / 4, (uint32_t)p.wq - 1), qyi = min(y / 4, (uint32_t)p.hq - 1);
+    for (int k = 0; k < p.fp.n_frames; k++)
     {
-        const float qx = __ldg(a.lut + x), qy = __ldg(a.lut + a.w + y); // pixel2CS of the output pixel (main view)
-        const float esx = a.err_sx, esy = a.err_sy;
-        float gx[2] = {0.f, 0.f}, gy[2] = {0.f, 0.f};
-        if (p.guess)
+        bool fail = false, ok = false;
+        uint32_t color = 0;
+        if (inb)
         {
-            const uint32_t qxi = min(x / 4, (uint32_t)p.wq - 1), qyi = min(y / 4, (uint32_t)p.hq - 1);
-            const uint2 g = *reinterpret_cast<const uint2 *>(p.guess + (((size_t)k * p.hq + qyi) * p.wq + qxi) * 4);
-            const float2 g0 = __half22float2(*reinterpret_cast<const __half2 *>(&g.x)), g1 = __half22float2(*reinterpret_cast<const __half2 *>(&g.y));
-            gx[0] = g0.x, gy[0] = g0.y, gx[1] = g1.x, gy[1] = g1.y;
-        }
-        DirRes d[2];
+            float g[4] = {0.f, 0.f, 0.f, 0.f};
+            if (p.guess)
+            {
+                const uint2 gg = *reinterpret_cast<const uint2 *>(p.guess + (((size_t)k * p.hq + qyi) * p.wq + qxi) * 4);
+                const float2 g0 = __half22float2(*reinterpret_cast<const __half2 *>(&gg.x));
+                const float2 g1 = __half22float2(*reinterpret_cast<const __half2 *>(&gg.y));
+                g[0] = g0.x, g[1] = g0.y, g[2] = g1.x, g[3] = g1.y;
+            }
+            const bool search[2] = {p.fp.f[k].alpha < 1.0f, true}; // src/renderer.cu:336
+            uint32_t sx[2], sy[2];
 #pragma unroll
-        for (int v = 0; v < 2; v++)
-        {
-            const DevView &dv = p.fp.v[v];
-            d[v].error_vis = ERR_UNSEARCHED_OF<LEARNED_SQ>;
-            d[v].depth = 0.0f;
-            d[v].src = 0;
-            if (v == 0 && !(p.fp.f[k].alpha < 1.0f))
-                continue; // the forward keyframe is not searched at t >= 1 (src/renderer.cu:336)
-            float fx = (float)x + 4.0f * gx[v], fy = (float)y + 4.0f * gy[v];
-            fx = isfinite(fx) ? fminf(fmaxf(fx, 0.0f), (float)(dv.w - 1)) : (float)x;
-            fy = isfinite(fy) ? fminf(fmaxf(fy, 0.0f), (float)(dv.h - 1)) : (float)y;
-            d[v] = learned_dir<LEARNED_SQ>(p, v, k, (uint32_t)__float2int_rn(fx), (uint32_t)__float2int_rn(fy), p.learned_iters, qx, qy,
-                                           qx, qy, esx, esy);
+            for (int v = 0; v < 2; v++)
+            {
+                const DevView &dv = p.fp.v[v];
+                float fx = (float)x + 4.0f * g[2 * v], fy = (float)y + 4.0f * g[2 * v + 1];
+                fx = isfinite(fx) ? fminf(fmaxf(fx, 0.0f), (float)(dv.w - 1)) : (float)x;
+                fy = isfinite(fy) ? fminf(fmaxf(fy, 0.0f), (float)(dv.h - 1)) : (float)y;
+                sx[v] = (uint32_t)__float2int_rn(fx);
+                sy[v] = (uint32_t)__float2int_rn(fy);
+            }
+            for (int it = 0; it < p.learned_iters; it++)
+            {
+#pragma unroll
+                for (int v = 0; v < 2; v++)
+                    if (search[v])
+                        learned_step_approx(p, v, k, qx, qy, sx[v], sy[v]);
+            }
+            DirRes d[2];
+#pragma unroll
+            for (int v = 0; v < 2; v++)
+            {
+                d[v].error_vis = ERR_UNSEARCHED_OF<LEARNED_SQ>;
+                d[v].depth = 0.0f;
+                d[v].src = (sx[v] << 16) | sy[v];
+                if (search[v])
+                    d[v] = learned_dir<LEARNED_SQ>(p, v, k, sx[v], sy[v], 0, qx, qy, qx, qy, a.err_sx, a.err_sy);
+            }
+            const bool conv0 = err_below<LEARNED_SQ>(dir_error(d[0]), ERR_EPS_1_FULL_RES<LEARNED_SQ>);
+            const bool conv1 = err_below<LEARNED_SQ>(dir_error(d[1]), ERR_EPS_1_FULL_RES<LEARNED_SQ>);
+            if (!conv0 && !conv1)
+            {
+                // sources on the far plane (z = 1: sky) in both keyframes are left to the temporal
+                // hole filling, as the plain method mostly leaves them
+                const float z0 = __ldg(a.z + (sy[0] * a.w + sx[0]));
+                const float z1 = __ldg(b.z + (sy[1] * b.w + sx[1]));
+                fail = !(z0 >= 1.0f && z1 >= 1.0f);
+            }
+            else
+                ok = learned_resolve<LEARNED_SQ>(p, k, d[0], d[1], color);
         }
-        const bool conv0 = err_below<LEARNED_SQ>(dir_error(d[0]), ERR_EPS_1_FULL_RES<LEARNED_SQ>);
-        const bool conv1 = err_below<LEARNED_SQ>(dir_error(d[1]), ERR_EPS_1_FULL_RES<LEARNED_SQ>);
-        if (!conv0 && !conv1)
+        if (p.learned_iters < 0)
+            fail = true; // every tile to the plain method (checks the fallback against the plain path)
+        const uint32_t flag_idx = ((uint32_t)k * p.tiles_y + blockIdx.y) * p.tiles_x + blockIdx.x;
+        if (__syncthreads_or(fail ? 1 : 0))
         {
-            // sources on the far plane (z = 1: sky) in both keyframes are left to the temporal
-            // hole filling, as the plain method mostly leaves them
-            const float z0 = __ldg(a.z + ((d[0].src & 0xFFFFu) * a.w + (d[0].src >> 16)));
-            const float z1 = __ldg(b.z + ((d[1].src & 0xFFFFu) * b.w + (d[1].src >> 16)));
-            fail = !(z0 >= 1.0f && z1 >= 1.0f);
+            if (threadIdx.x == 0 && threadIdx.y == 0)
+            {
+                p.tile_flags[flag_idx] = 1u;
+                p.tile_list[atomicAdd(p.fallback_count, 1)] = flag_idx;
+            }
+            continue;
         }
-        else
-            ok = learned_resolve<LEARNED_SQ>(p, k, d[0], d[1], color);
-    }
-    if (__syncthreads_or(fail ? 1 : 0))
-    {
         if (threadIdx.x == 0 && threadIdx.y == 0)
-        {
-            p.tile_flags[((size_t)k * p.tiles_y + blockIdx.y) * p.tiles_x + blockIdx.x] = 1u;
-            atomicAdd(p.fallback_count, 1);
-        }
-        return;
+            p.tile_flags[flag_idx] = 0u;
+        if (ok)
+            p.fp.out[k][y * p.fp.out_w + x] = color;
+        if (p.fp.chain && inb)
+            p.valid[((size_t)k * p.fp.out_h + y) * p.fp.out_w + x] = ok ? 1 : 0;
     }
-    if (threadIdx.x == 0 && threadIdx.y == 0)
-        p.tile_flags[((size_t)k * p.tiles_y + blockIdx.y) * p.tiles_x + blockIdx.x] = 0u;
-    if (ok)
-        p.fp.out[k][y * p.fp.out_w + x] = color;
 }
 
 // ---- fallback: the plain method for the marked tiles ----
@@ -266,38 +313,87 @@ __device__ __forceinline__ bool tile_marked(const LearnedParams &p, int k, uint3
     return __ldg(p.tile_flags + ((size_t)k * p.tiles_y + y / LT_H) * p.tiles_x + x / LT_W) != 0u;
 }
 
-// keys of every marked tile <- the empty value (both views)
-__global__ void __launch_bounds__(LT_W *LT_H) fallback_init_kernel(const __grid_constant__ LearnedParams p)
+// keys of every marked tile <- the empty value (both views).  A small grid walks the list of
+// marked tiles (blocks of LT_W x LT_H threads, one tile per iteration).
+__device__ __forceinline__ void tile_of(const LearnedParams &p, uint32_t flag_idx, int &k, uint32_t &x, uint32_t &y)
 {
-    if (*p.fallback_count == 0)
-        return;
-    const int k = blockIdx.z;
-    if (__ldg(p.tile_flags + ((size_t)k * p.tiles_y + blockIdx.y) * p.tiles_x + blockIdx.x) == 0u)
-        return;
-    const uint32_t x = blockIdx.x * LT_W + threadIdx.x, y = blockIdx.y * LT_H + threadIdx.y;
-    if (x >= p.fp.out_w || y >= p.fp.out_h)
-        return;
-    for (int v = 0; v < 2; v++)
-        p.fp.v[v].splat[k * p.fp.key_stride + y * p.fp.v[v].w + x] = SPLAT_EMPTY;
+    const uint32_t per_frame = (uint32_t)(p.tiles_x * p.tiles_y);
+    k = (int)(flag_idx / per_frame);
+    const uint32_t t = flag_idx % per_frame;
+    x = (t % (uint32_t)p.tiles_x) * LT_W + threadIdx.x;
+    y = (t / (uint32_t)p.tiles_x) * LT_H + threadIdx.y;
 }
 
-// every source pixel whose client-camera target lies in a marked tile: atomicMin of its key
-// (computeFlowFields_sortedSplatting_kernel, src/renderer.cu:110-145)
+__global__ void __launch_bounds__(LT_W *LT_H) fallback_init_kernel(const __grid_constant__ LearnedParams p)
+{
+    const int n = *p.fallback_count;
+    for (int i = blockIdx.x; i < n; i += gridDim.x)
+    {
+        int k;
+        uint32_t x, y;
+        tile_of(p, __ldg(p.tile_list + i), k, x, y);
+        if (x >= p.fp.out_w || y >= p.fp.out_h)
+            continue;
+        for (int v = 0; v < 2; v++)
+            p.fp.v[v].splat[k * p.fp.key_stride + y * p.fp.v[v].w + x] = SPLAT_EMPTY;
+    }
+}
+
+// Every source pixel whose client-camera target lies in a marked tile: atomicMin of its key
+// (computeFlowFields_sortedSplatting_kernel, src/renderer.cu:110-145).  One thread per source
+// pixel and view handles every frame (the keyframe part is read once).  An approximate
+// projection (contracted multiply-adds, fast division) first rejects targets farther than 2
+// pixels from every marked tile -- its error is orders of magnitude below that margin; a w
+// near zero or a non-finite value is never rejected -- and only candidates take the exact
+// projection of the plain path.
+__device__ __forceinline__ bool near_marked_tile(const LearnedParams &p, int k, float fx, float fy)
+{
+    const int x0 = max(0, (int)floorf(fx) - 2), x1 = min((int)p.fp.out_w - 1, (int)floorf(fx) + 2);
+    const int y0 = max(0, (int)floorf(fy) - 2), y1 = min((int)p.fp.out_h - 1, (int)floorf(fy) + 2);
+    if (x0 > x1 || y0 > y1)
+        return false;
+    for (int ty = y0 / LT_H; ty <= y1 / LT_H; ty++)
+        for (int tx = x0 / LT_W; tx <= x1 / LT_W; tx++)
+            if (__ldg(p.tile_flags + ((size_t)k * p.tiles_y + ty) * p.tiles_x + tx) != 0u)
+                return true;
+    return false;
+}
+
 __global__ void __launch_bounds__(256) fallback_splat_kernel(const __grid_constant__ LearnedParams p)
 {
     if (*p.fallback_count == 0)
         return;
-    const int v = blockIdx.z % 2, k = blockIdx.z / 2;
+    const int v = blockIdx.z;
     const DevView &dv = p.fp.v[v];
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= dv.w || y >= dv.h)
         return;
-    const float4 pc = learned_project(p, v, k, x, y);
-    const float depth_cam = z_to_depth(pc.z);
-    const int2 pix = cs2pixel(pc.x, pc.y, dv.w, dv.h);
-    if (!in_range(pix, dv.w, dv.h) || depth_cam < 0.0f || !tile_marked(p, k, (uint32_t)pix.x, (uint32_t)pix.y))
-        return;
-    atomicMin(dv.splat + k * p.fp.key_stride + ((uint32_t)pix.y * dv.w + (uint32_t)pix.x), encode_key(depth_cam, x, y));
+    const uint32_t i = y * dv.w + x;
+    const float4 a = __ldg(p.ws[v] + i), d = __ldg(p.dws[v] + i);
+    for (int k = 0; k < p.fp.n_frames; k++)
+    {
+        const float *m = p.fp.cam_vp[k];
+        const float wg = dv.forward ? p.fp.f[k].alpha : xsub(1.0f, p.fp.f[k].alpha);
+        // approximate target pixel
+        const float sx = fmaf(wg, d.x, a.x), sy = fmaf(wg, d.y, a.y), sz = fmaf(wg, d.z, a.z), sw = fmaf(wg, d.w, a.w);
+        const float qx = fmaf(m[0], sx, fmaf(m[4], sy, fmaf(m[8], sz, m[12] * sw)));
+        const float qy = fmaf(m[1], sx, fmaf(m[5], sy, fmaf(m[9], sz, m[13] * sw)));
+        const float qw = fmaf(m[3], sx, fmaf(m[7], sy, fmaf(m[11], sz, m[15] * sw)));
+        bool candidate = true;
+        if (isfinite(qx) && isfinite(qy) && fabsf(qw) > 1e-6f)
+        {
+            const float fx = (__fdividef(qx, qw) + 1.0f) * (float)dv.w * 0.5f, fy = (__fdividef(qy, qw) + 1.0f) * (float)dv.h * 0.5f;
+            candidate = isfinite(fx) && isfinite(fy) ? near_marked_tile(p, k, fx, fy) : true;
+        }
+        if (!candidate)
+            continue;
+        const float4 pc = learned_project(p, v, k, x, y);
+        const float depth_cam = z_to_depth(pc.z);
+        const int2 pix = cs2pixel(pc.x, pc.y, dv.w, dv.h);
+        if (!in_range(pix, dv.w, dv.h) || depth_cam < 0.0f || !tile_marked(p, k, (uint32_t)pix.x, (uint32_t)pix.y))
+            continue;
+        atomicMin(dv.splat + k * p.fp.key_stride + ((uint32_t)pix.y * dv.w + (uint32_t)pix.x), encode_key(depth_cam, x, y));
+    }
 }
 
 // window initialisation on global keys (initializeSearchFromSplatting<1>, src/renderer.cu:148-175)
@@ -324,34 +420,58 @@ __device__ __forceinline__ unsigned long long window_key_global(const unsigned l
 
 __global__ void __launch_bounds__(LT_W *LT_H) fallback_reproj_kernel(const __grid_constant__ LearnedParams p)
 {
-    if (*p.fallback_count == 0)
-        return;
-    const int k = blockIdx.z;
-    if (__ldg(p.tile_flags + ((size_t)k * p.tiles_y + blockIdx.y) * p.tiles_x + blockIdx.x) == 0u)
-        return;
-    const uint32_t x = blockIdx.x * LT_W + threadIdx.x, y = blockIdx.y * LT_H + threadIdx.y;
-    if (x >= p.fp.out_w || y >= p.fp.out_h)
-        return;
+    const int n = *p.fallback_count;
     const DevView &a = p.fp.v[0];
-    const float qx = __ldg(a.lut + x), qy = __ldg(a.lut + a.w + y);
-    DirRes d[2];
-#pragma unroll
-    for (int v = 0; v < 2; v++)
+    for (int i = blockIdx.x; i < n; i += gridDim.x)
     {
-        const DevView &dv = p.fp.v[v];
-        const unsigned long long lo = window_key_global(dv.splat + k * p.fp.key_stride, dv.w, dv.h, x, y);
-        d[v].depth = __uint_as_float((uint32_t)(lo >> 32));
-        d[v].src = (uint32_t)lo;
-        d[v].error_vis = ERR_UNSEARCHED_OF<LEARNED_SQ>;
-        const bool search_ok = v == 1 || p.fp.f[k].alpha < 1.0f;
-        if (search_ok && d[v].depth > 0.0f)
-            d[v] = learned_dir<LEARNED_SQ>(p, v, k, min(((uint32_t)lo) >> 16, dv.w - 1u), min((uint32_t)lo & 0xFFFFu, dv.h - 1u), 3, qx, qy, qx,
-                                           qy, dv.err_sx, dv.err_sy);
+        int k;
+        uint32_t x, y;
+        tile_of(p, __ldg(p.tile_list + i), k, x, y);
+        if (x >= p.fp.out_w || y >= p.fp.out_h)
+            continue;
+        const float qx = __ldg(a.lut + x), qy = __ldg(a.lut + a.w + y);
+        DirRes d[2];
+#pragma unroll
+        for (int v = 0; v < 2; v++)
+        {
+            const DevView &dv = p.fp.v[v];
+            const unsigned long long lo = window_key_global(dv.splat + k * p.fp.key_stride, dv.w, dv.h, x, y);
+            d[v].depth = __uint_as_float((uint32_t)(lo >> 32));
+            d[v].src = (uint32_t)lo;
+            d[v].error_vis = ERR_UNSEARCHED_OF<LEARNED_SQ>;
+            const bool search_ok = v == 1 || p.fp.f[k].alpha < 1.0f;
+            if (search_ok && d[v].depth > 0.0f)
+                d[v] = learned_dir<LEARNED_SQ>(p, v, k, min(((uint32_t)lo) >> 16, dv.w - 1u), min((uint32_t)lo & 0xFFFFu, dv.h - 1u), 3, qx, qy,
+                                               qx, qy, dv.err_sx, dv.err_sy);
+        }
+        uint32_t color = 0;
+        const bool ok = learned_resolve<LEARNED_SQ>(p, k, d[0], d[1], color);
+        if (ok)
+            p.fp.out[k][y * p.fp.out_w + x] = color;
+        if (p.fp.chain)
+            p.valid[((size_t)k * p.fp.out_h + y) * p.fp.out_w + x] = ok ? 1 : 0;
     }
-    uint32_t color = 0;
-    if (learned_resolve<LEARNED_SQ>(p, k, d[0], d[1], color))
-        p.fp.out[k][y * p.fp.out_w + x] = color;
 }
+
+// Chained outputs (isti_render_batch's chain_outputs semantics): one persistent buffer per
+// pixel that starts as out[0]'s content, takes each frame's written value and is copied to
+// out[k] after frame k.
+__global__ void __launch_bounds__(256) learned_chain_kernel(const __grid_constant__ LearnedParams p)
+{
+    const size_t n = (size_t)p.fp.out_w * p.fp.out_h;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    {
+        uint32_t run = p.fp.out[0][i];
+        for (int k = 1; k < p.fp.n_frames; k++)
+        {
+            if (p.valid[(size_t)k * n + i])
+                run = p.fp.out[k][i];
+            else
+                p.fp.out[k][i] = run;
+        }
+    }
+}
+
 // ---- training labels from a plain render ----
 
 // Per quarter-resolution pixel q of frame k of the last plain render (keys and client flow

@@ -651,13 +651,14 @@ int quarter_grid(uint32_t n) { return (int)(((n + 3) / 4 + 7) / 8 * 8); }
 
 // Lays out the learned arena for a call and fills r->learned (everything but the stages).
 isti_status learned_setup(isti_renderer *r, isti_flownet *net, int32_t n_frames, void *const *out_rgba, const isti_render_info *infos,
-                          const isti_frame_data *frame, int32_t iterations, __half **guess_out);
+                          const isti_frame_data *frame, int32_t iterations, bool chain, __half **guess_out);
 
 extern "C" isti_status isti_render_learned(isti_renderer *r, isti_flownet *net, int32_t n_frames, void *const *out_rgba,
-                                           const isti_render_info *infos, const isti_frame_data *frame, int32_t iterations, void *stream_ptr)
+                                           const isti_render_info *infos, const isti_frame_data *frame, int32_t iterations,
+                                           int32_t chain_outputs, void *stream_ptr)
 {
     __half *guess = nullptr;
-    isti_status st = learned_setup(r, net, n_frames, out_rgba, infos, frame, iterations, &guess);
+    isti_status st = learned_setup(r, net, n_frames, out_rgba, infos, frame, iterations, chain_outputs != 0, &guess);
     if (st != ISTI_OK)
         return st;
     const cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
@@ -680,11 +681,14 @@ extern "C" isti_status isti_render_learned(isti_renderer *r, isti_flownet *net, 
         if (st != ISTI_OK)
             return st;
     }
-    const dim3 gt(p.tiles_x, p.tiles_y, n_frames);
-    isti::learned_kernel<<<gt, dim3(isti::LT_W, isti::LT_H), 0, stream>>>(p);
-    isti::fallback_init_kernel<<<gt, dim3(isti::LT_W, isti::LT_H), 0, stream>>>(p);
-    isti::fallback_splat_kernel<<<dim3((w + 31) / 32, (h + 7) / 8, 2 * n_frames), b2, 0, stream>>>(p);
-    isti::fallback_reproj_kernel<<<gt, dim3(isti::LT_W, isti::LT_H), 0, stream>>>(p);
+    isti::learned_kernel<<<dim3(p.tiles_x, p.tiles_y), dim3(isti::LT_W, isti::LT_H), 0, stream>>>(p);
+    // the fallback kernels walk the list of marked tiles (none: they return at once)
+    const unsigned list_blocks = (unsigned)std::min(p.tiles_x * p.tiles_y * n_frames, 152 * 4);
+    isti::fallback_init_kernel<<<list_blocks, dim3(isti::LT_W, isti::LT_H), 0, stream>>>(p);
+    isti::fallback_splat_kernel<<<dim3((w + 31) / 32, (h + 7) / 8, 2), b2, 0, stream>>>(p);
+    isti::fallback_reproj_kernel<<<list_blocks, dim3(isti::LT_W, isti::LT_H), 0, stream>>>(p);
+    if (chain_outputs && n_frames > 1)
+        isti::learned_chain_kernel<<<(unsigned)std::min<size_t>(((size_t)w * h + 255) / 256, 152 * 8), 256, 0, stream>>>(p);
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return cuda_fail(e, "learned render launch");
@@ -703,7 +707,7 @@ extern "C" isti_status isti_learned_input(isti_renderer *r, int32_t n_frames, co
     for (int k = 0; k < isti::MAX_FRAMES; k++)
         dummy[k] = net_input;
     __half *guess = nullptr;
-    isti_status st = learned_setup(r, nullptr, n_frames, dummy, infos, frame, 1, &guess);
+    isti_status st = learned_setup(r, nullptr, n_frames, dummy, infos, frame, 1, false, &guess);
     if (st != ISTI_OK)
         return st;
     const cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
@@ -742,7 +746,7 @@ extern "C" isti_status isti_learned_grid(uint32_t width, uint32_t height, int32_
 }
 
 isti_status learned_setup(isti_renderer *r, isti_flownet *net, int32_t n_frames, void *const *out_rgba, const isti_render_info *infos,
-                          const isti_frame_data *frame, int32_t iterations, __half **guess_out)
+                          const isti_frame_data *frame, int32_t iterations, bool chain, __half **guess_out)
 {
     if (!r || !out_rgba || !infos || !frame)
         return fail(ISTI_ERR_INVALID_ARG, "NULL argument");
@@ -755,8 +759,8 @@ isti_status learned_setup(isti_renderer *r, isti_flownet *net, int32_t n_frames,
         return fail(ISTI_ERR_INVALID_ARG, "isti_render_learned renders the main camera only (num_aux must be 0)");
     if (infos[0].mode != ISTI_MODE_OURS && infos[0].mode != ISTI_MODE_BACKWARD_UNIDIRECTIONAL)
         return fail(ISTI_ERR_INVALID_ARG, "isti_render_learned implements modes 0 and 2 (3x3 window, 3 search iterations)");
-    if (iterations < 0 || iterations > 16)
-        return fail(ISTI_ERR_INVALID_ARG, "iterations must be 0..16");
+    if (iterations < -1 || iterations > 16)
+        return fail(ISTI_ERR_INVALID_ARG, "iterations must be -1..16");
     int cur = 0;
     cudaError_t e = cudaGetDevice(&cur);
     if (e != cudaSuccess)
@@ -781,8 +785,9 @@ isti_status learned_setup(isti_renderer *r, isti_flownet *net, int32_t n_frames,
     const size_t ws_bytes = align_up(px * 16, 256);
     const size_t in_bytes = align_up((size_t)n_frames * hq * wq * 16 * 2, 256);
     const size_t guess_bytes = align_up((size_t)n_frames * hq * wq * 4 * 2, 256);
-    const size_t flag_bytes = align_up((size_t)n_frames * tiles_x * tiles_y * 4, 256);
-    const size_t total = l.total + 4 * ws_bytes + in_bytes + guess_bytes + flag_bytes + 256;
+    const size_t flag_bytes = 2 * align_up((size_t)n_frames * tiles_x * tiles_y * 4, 256); // flags, then the marked-tile list
+    const size_t valid_bytes = align_up((size_t)n_frames * px, 256);
+    const size_t total = l.total + 4 * ws_bytes + in_bytes + guess_bytes + flag_bytes + 256 + valid_bytes;
     if (total > r->learned_bytes)
     {
         if (r->learned_arena)
@@ -796,7 +801,7 @@ isti_status learned_setup(isti_renderer *r, isti_flownet *net, int32_t n_frames,
     }
     char *base = static_cast<char *>(r->learned_arena);
     isti::LearnedParams &p = r->learned;
-    fill_params(p.fp, n_frames, out_rgba, infos, frame, views, n_views, l, base, false);
+    fill_params(p.fp, n_frames, out_rgba, infos, frame, views, n_views, l, base, chain);
     for (int v = 0; v < 2; v++)
         p.fp.v[v].cam_ff = nullptr; // the client-camera flow is computed on the fly
     char *extra = base + l.total;
@@ -809,7 +814,9 @@ isti_status learned_setup(isti_renderer *r, isti_flownet *net, int32_t n_frames,
     __half *guess = reinterpret_cast<__half *>(extra + 4 * ws_bytes + in_bytes);
     p.guess = net ? guess : nullptr;
     p.tile_flags = reinterpret_cast<uint32_t *>(extra + 4 * ws_bytes + in_bytes + guess_bytes);
+    p.tile_list = reinterpret_cast<uint32_t *>(extra + 4 * ws_bytes + in_bytes + guess_bytes + flag_bytes / 2);
     p.fallback_count = reinterpret_cast<int32_t *>(extra + 4 * ws_bytes + in_bytes + guess_bytes + flag_bytes);
+    p.valid = reinterpret_cast<uint8_t *>(extra + 4 * ws_bytes + in_bytes + guess_bytes + flag_bytes + 256);
     p.hq = hq;
     p.wq = wq;
     p.learned_iters = iterations;

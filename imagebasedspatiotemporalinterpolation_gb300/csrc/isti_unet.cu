@@ -54,6 +54,53 @@ isti_status nhwc_map(CUtensorMap &m, const void *base, int n, int h, int w, int 
     return ISTI_OK;
 }
 
+// 5-D map over an NHWC bf16 tensor with the channels split as (8, c / 8) and the chunk index
+// outermost: dims (c_lo, w, h, c_hi, n), box {8, 16 x, 8 y, ck / 8 chunks, 1}, so one copy lands
+// a stage's channel chunks one after another (the layout of ck / 8 separate 4-D boxes).
+// Returns false when the driver does not accept the strides.
+bool nhwc_chunked_map(CUtensorMap &m, const void *base, int n, int h, int w, int c, int ck)
+{
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc || ((uintptr_t)base & 15u) || c % 8 || ck % 8)
+        return false;
+    const cuuint64_t dims[5] = {8, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)(c / 8), (cuuint64_t)n};
+    const cuuint64_t strides[4] = {(cuuint64_t)c * 2u, (cuuint64_t)w * c * 2u, 16u, (cuuint64_t)h * w * c * 2u};
+    const cuuint32_t box[5] = {8, (cuuint32_t)TILE_W, (cuuint32_t)TILE_H, (cuuint32_t)(ck / 8), 1};
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    return enc(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// 5-D map for row_conv_kernel: box {8, 130 x, 3 y, ck / 8 chunks, 1} (a 128-pixel row segment
+// with its halo).
+bool nhwc_row_map(CUtensorMap &m, const void *base, int n, int h, int w, int c, int ck)
+{
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc || ((uintptr_t)base & 15u) || c % 8 || ck % 8)
+        return false;
+    const cuuint64_t dims[5] = {8, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)(c / 8), (cuuint64_t)n};
+    const cuuint64_t strides[4] = {(cuuint64_t)c * 2u, (cuuint64_t)w * c * 2u, 16u, (cuuint64_t)h * w * c * 2u};
+    const cuuint32_t box[5] = {8, (cuuint32_t)ROW_HALO, 3, (cuuint32_t)(ck / 8), 1};
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    return enc(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+int sm_count()
+{
+    static int n[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+        return 152;
+    if (!n[dev & 63])
+    {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        n[dev & 63] = v > 0 ? v : 152;
+    }
+    return n[dev & 63];
+}
+
 // A kernel's dynamic shared-memory limit, raised once per kernel and device to the largest
 // size asked (keyed by the kernel's address: instances of one template share a type).
 template <class K>
@@ -124,10 +171,6 @@ isti_status conv_launch(int taps, const void *x, int n, int h, int w, int cin, c
     isti_status st = status_word(status);
     if (st != ISTI_OK)
         return st;
-    CUtensorMap xmap;
-    st = nhwc_map(xmap, x, n, h, w, cin);
-    if (st != ISTI_OK)
-        return st;
     ConvParams p{};
     p.wpack = static_cast<const __nv_bfloat16 *>(wpack);
     p.bias = bias;
@@ -142,26 +185,59 @@ isti_status conv_launch(int taps, const void *x, int n, int h, int w, int cin, c
     p.ck = cin % 32 == 0 ? 32 : 16;
     p.tiles_x = (w + TILE_W - 1) / TILE_W;
     p.tiles_y = (h + TILE_H - 1) / TILE_H;
+    p.n_tiles = n * p.tiles_x * p.tiles_y;
     p.relu = relu;
+    CUtensorMap xmap;
+    // wide, thin 3x3 layers: row-tile kernel with a loaded-once halo and resident weights
+    const uint32_t w_bytes = 9u * (uint32_t)cin * cout * 2u;
+    if (taps == 9 && w >= ROW_M && w_bytes <= 96u * 1024u && nhwc_row_map(xmap, x, n, h, w, cin, p.ck))
+    {
+        const size_t w_region = (w_bytes + 1023) / 1024 * 1024, sb = row_stage_bytes(p.ck), tail = 16 * 8 + 16;
+        int per_sm = 2;
+        size_t stages = w_region + 2 * sb + 2 * 16 + tail <= 100 * 1024 ? (100 * 1024 - w_region - tail) / (sb + 16) : 0;
+        if (stages < 2)
+        {
+            per_sm = 1;
+            stages = (SMEM_BUDGET - w_region - tail) / (sb + 16);
+        }
+        p.stages = (int)std::min<size_t>(8, stages);
+        if (p.stages >= 2)
+        {
+            const size_t smem = w_region + (size_t)p.stages * sb + (2 * p.stages + 6) * 8 + 16;
+            const int units = n * h * ((w + ROW_M - 1) / ROW_M);
+            const int grid = std::min(units, sm_count() * per_sm);
+            cudaError_t e = smem_limit(row_conv_kernel<0>, smem);
+            if (e == cudaSuccess)
+                row_conv_kernel<0><<<(unsigned)grid, PCONV_THREADS, smem, stream>>>(p, xmap);
+            if (e == cudaSuccess)
+                e = cudaGetLastError();
+            return e == cudaSuccess ? ISTI_OK : cuda_fail(e, "isti_unet_conv launch");
+        }
+    }
+    p.chunked_map = nhwc_chunked_map(xmap, x, n, h, w, cin, p.ck) ? 1 : 0;
+    if (!p.chunked_map && (st = nhwc_map(xmap, x, n, h, w, cin)) != ISTI_OK)
+        return st;
+    // ring: about 100 KB, so that two CTAs share an SM; the ring runs across tiles
     const uint32_t sb = conv_stage_bytes(p.ck, cout);
-    const int iters = taps * (cin / p.ck);
-    p.stages = (int)std::min<size_t>(std::min<size_t>(8, (size_t)iters), std::max<size_t>(2, (96 * 1024) / sb));
-    const size_t smem = (size_t)p.stages * sb + (2 * p.stages + 1) * 8 + 16;
+    p.stages = (int)std::min<size_t>(16, std::max<size_t>(2, (100 * 1024) / sb));
+    const size_t smem = (size_t)p.stages * sb + (2 * p.stages + 5) * 8 + 16;
     if (smem > SMEM_BUDGET)
         return isti::set_error(ISTI_ERR_INVALID_ARG, "isti_unet_conv: stage does not fit in shared memory");
-    const size_t grid = (size_t)n * p.tiles_x * p.tiles_y;
+    const uint32_t ncols = 2 * tmem_cols(cout);
+    const int per_sm = std::max(1, std::min(2, (int)(512 / ncols)));
+    const int grid = std::min(p.n_tiles, sm_count() * per_sm);
     cudaError_t e;
     if (taps == 9)
     {
         e = smem_limit(conv_kernel<9>, smem);
         if (e == cudaSuccess)
-            conv_kernel<9><<<(unsigned)grid, CONV_THREADS, smem, stream>>>(p, xmap);
+            conv_kernel<9><<<(unsigned)grid, PCONV_THREADS, smem, stream>>>(p, xmap);
     }
     else
     {
         e = smem_limit(conv_kernel<1>, smem);
         if (e == cudaSuccess)
-            conv_kernel<1><<<(unsigned)grid, CONV_THREADS, smem, stream>>>(p, xmap);
+            conv_kernel<1><<<(unsigned)grid, PCONV_THREADS, smem, stream>>>(p, xmap);
     }
     if (e == cudaSuccess)
         e = cudaGetLastError();

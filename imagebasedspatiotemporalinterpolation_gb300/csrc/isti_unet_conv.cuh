@@ -38,7 +38,7 @@ namespace isti_unet
 {
 using namespace isti_tc;
 
-constexpr int CONV_THREADS = 128;
+constexpr int CONV_THREADS = 128; // weight-gradient kernel: warp 0 producer, warp 1 MMA, all four epilogue
 constexpr int TILE_W = 16, TILE_H = 8, TILE_M = TILE_W * TILE_H;
 constexpr uint32_t BOX_BYTES = TILE_M * 16; // one TMA box: 8 channels x 128 pixels
 
@@ -59,9 +59,10 @@ struct ConvParams
     int32_t *status;
     int w, h, b;
     int cin, cout, ck;          // ck: input channels per stage (16 or 32)
-    int tiles_x, tiles_y;
+    int tiles_x, tiles_y, n_tiles;
     int relu;
     int stages;                 // depth of the shared-memory ring
+    int chunked_map;            // 1: one 5-D box per stage (channel chunks outermost); 0: ck / 8 4-D boxes
 };
 
 __host__ __device__ constexpr uint32_t conv_stage_bytes(int ck, int cout) { return (uint32_t)ck * 256u + (uint32_t)ck * cout * 2u; }
@@ -69,25 +70,35 @@ __host__ __device__ constexpr uint32_t conv_stage_bytes(int ck, int cout) { retu
 // bf16 > 0 (positive, non-zero, not NaN)
 __device__ __forceinline__ bool bf16_positive(uint16_t b) { return (b & 0x8000u) == 0 && (b & 0x7fffu) != 0 && (b & 0x7fffu) <= 0x7f80u; }
 
+// 5-D tiled TMA load (c_lo, x, y, c_hi, n): the channel chunks of a box land one after another
+__device__ __forceinline__ void tma_load_5d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, int c3, int c4, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+constexpr int PCONV_THREADS = 192; // warp 0: TMA producer, warp 1: MMA issuer, warps 2-5: epilogue
+
+// Persistent convolution: each CTA works through tiles blockIdx.x, blockIdx.x + gridDim.x, ...
+// The producer runs ahead through the ring across tiles; the MMA issuer accumulates tile i into
+// TMEM buffer i % 2 while the epilogue warps drain buffer (i - 1) % 2 (acc_full / acc_empty
+// barriers), so stores overlap the next tile's loads and MMAs.
 template <int TAPS>
-__global__ void __launch_bounds__(CONV_THREADS) conv_kernel(const __grid_constant__ ConvParams p, const __grid_constant__ CUtensorMap xmap)
+__global__ void __launch_bounds__(PCONV_THREADS, 1) conv_kernel(const __grid_constant__ ConvParams p, const __grid_constant__ CUtensorMap xmap)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int S = p.stages;
     const uint32_t a_bytes = (uint32_t)p.ck * 256u, b_bytes = (uint32_t)p.ck * p.cout * 2u, stage_bytes = a_bytes + b_bytes;
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + (size_t)S * stage_bytes);
     uint64_t *empty = full + S;
-    uint64_t *done = empty + S;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    uint64_t *acc_full = empty + S;
+    uint64_t *acc_empty = acc_full + 2;
+    uint64_t *mma_done = acc_empty + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-
-    int t = blockIdx.x;
-    const int tx = t % p.tiles_x;
-    t /= p.tiles_x;
-    const int ty = t % p.tiles_y;
-    const int bi = t / p.tiles_y;
-    const int x0 = tx * TILE_W, y0 = ty * TILE_H;
-    const uint32_t ncols = tmem_cols(p.cout);
+    const uint32_t acc_cols = tmem_cols(p.cout), ncols = 2 * acc_cols;
 
     if (threadIdx.x == 0)
     {
@@ -96,7 +107,221 @@ __global__ void __launch_bounds__(CONV_THREADS) conv_kernel(const __grid_constan
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(done, 1);
+        for (int b = 0; b < 2; b++)
+        {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 4); // one arrival per epilogue warp
+        }
+        mbar_init(mma_done, 1);
+        fence_barrier_init();
+    }
+    if (warp == 0)
+        tmem_alloc(tmem_slot, ncols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const int chunks = p.cin / p.ck, iters = TAPS * chunks;
+
+    if (warp == 0 && lane == 0)
+    {
+        uint32_t g = 0;
+        bool stop = false;
+        for (int t = blockIdx.x; t < p.n_tiles && !stop; t += gridDim.x)
+        {
+            int tt = t;
+            const int tx = tt % p.tiles_x;
+            tt /= p.tiles_x;
+            const int ty = tt % p.tiles_y;
+            const int bi = tt / p.tiles_y;
+            const int x0 = tx * TILE_W, y0 = ty * TILE_H;
+            for (int it = 0; it < iters; it++, g++)
+            {
+                const uint32_t s = g % (uint32_t)S, r = g / (uint32_t)S;
+                if (r > 0 && !mbar_wait(&empty[s], (r - 1) & 1u, p.status))
+                {
+                    stop = true;
+                    break;
+                }
+                uint8_t *st = smem + (size_t)s * stage_bytes;
+                mbar_expect_tx(&full[s], stage_bytes);
+                const int tap = it / chunks, c = it % chunks;
+                const int dy = TAPS == 9 ? tap / 3 - 1 : 0, dx = TAPS == 9 ? tap % 3 - 1 : 0;
+                if (p.chunked_map)
+                    tma_load_5d(st, &xmap, 0, x0 + dx, y0 + dy, c * (p.ck / 8), bi, &full[s]);
+                else
+                    for (int j = 0; j < p.ck / 8; j++)
+                        tma_load_4d(st + j * BOX_BYTES, &xmap, c * p.ck + 8 * j, x0 + dx, y0 + dy, bi, &full[s]);
+                bulk_load(st + a_bytes, p.wpack + (size_t)it * p.ck * p.cout, b_bytes, &full[s]);
+            }
+        }
+        for (uint32_t q = g > (uint32_t)S ? g - (uint32_t)S : 0u; q < g; q++) // copies still landing
+            if (!mbar_wait(&full[q % (uint32_t)S], (q / (uint32_t)S) & 1u, p.status))
+                break;
+    }
+    else if (warp == 1 && lane == 0)
+    {
+        const uint32_t idesc = idesc_bf16(TILE_M, (uint32_t)p.cout, 0, 0);
+        const uint32_t lbo_b = (uint32_t)(p.cout / 8) * 128u;
+        uint32_t g = 0;
+        int i = 0;
+        bool stop = false;
+        for (int t = blockIdx.x; t < p.n_tiles && !stop; t += gridDim.x, i++)
+        {
+            const int buf = i & 1;
+            if (i >= 2 && !mbar_wait(&acc_empty[buf], (uint32_t)(((i >> 1) - 1) & 1), p.status))
+                break;
+            tc_fence_after();
+            const uint32_t d = tmem + (uint32_t)buf * acc_cols;
+            for (int it = 0; it < iters; it++, g++)
+            {
+                const uint32_t s = g % (uint32_t)S, r = g / (uint32_t)S;
+                if (!mbar_wait(&full[s], r & 1u, p.status))
+                {
+                    stop = true;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t a0 = smem_u32(smem + (size_t)s * stage_bytes), b0 = a0 + a_bytes;
+                for (int k = 0; k < p.ck / 16; k++)
+                    mma_bf16(d, smem_desc(a0 + k * 2 * BOX_BYTES, BOX_BYTES, 128), smem_desc(b0 + k * 2 * lbo_b, lbo_b, 128), idesc,
+                             it > 0 || k > 0);
+                mma_commit(&empty[s]);
+            }
+            if (!stop)
+                mma_commit(&acc_full[buf]);
+        }
+        mma_commit(mma_done);
+    }
+    else if (warp >= 2)
+    {
+        const int q = warp % 4; // the TMEM lane quadrant this warp may read
+        const int m = q * 32 + lane;
+        int i = 0;
+        for (int t = blockIdx.x; t < p.n_tiles; t += gridDim.x, i++)
+        {
+            const int buf = i & 1;
+            if (!mbar_wait(&acc_full[buf], (uint32_t)((i >> 1) & 1), p.status))
+                break;
+            tc_fence_after();
+            int tt = t;
+            const int tx = tt % p.tiles_x;
+            tt /= p.tiles_x;
+            const int ty = tt % p.tiles_y;
+            const int bi = tt / p.tiles_y;
+            const int px = tx * TILE_W + (m % TILE_W), py = ty * TILE_H + (m / TILE_W);
+            const bool inb = px < p.w && py < p.h;
+            const size_t pix = ((size_t)bi * p.h + (inb ? py : 0)) * p.w + (inb ? px : 0);
+            for (int c0 = 0; c0 < p.cout; c0 += 16)
+            {
+                uint32_t r[16];
+                tmem_ld16(tmem + (uint32_t)buf * acc_cols + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, r);
+                tmem_ld_wait();
+                if (!inb)
+                    continue;
+                float v[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++)
+                {
+                    v[j] = __uint_as_float(r[j]);
+                    if (p.bias)
+                        v[j] += __ldg(p.bias + c0 + j);
+                    if (p.relu)
+                        v[j] = fmaxf(v[j], 0.0f);
+                }
+                if (p.mask)
+                {
+                    const uint4 *mk = reinterpret_cast<const uint4 *>(p.mask + pix * p.cout + c0);
+                    const uint4 m0 = __ldg(mk), m1 = __ldg(mk + 1);
+                    const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+#pragma unroll
+                    for (int j = 0; j < 16; j++)
+                        if (!bf16_positive((uint16_t)(mw[j / 2] >> (16 * (j % 2)))))
+                            v[j] = 0.0f;
+                }
+                uint32_t o[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                {
+                    const __nv_bfloat162 h2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+                    o[j] = *reinterpret_cast<const uint32_t *>(&h2);
+                }
+                uint4 *dst = reinterpret_cast<uint4 *>(p.out + pix * p.cout + c0);
+                dst[0] = make_uint4(o[0], o[1], o[2], o[3]);
+                dst[1] = make_uint4(o[4], o[5], o[6], o[7]);
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0)
+                mbar_arrive(&acc_empty[buf]);
+        }
+    }
+    __syncwarp();
+    if (warp == 0)
+    {
+        if (lane == 0)
+            mbar_wait(mma_done, 0, p.status); // no MMA may still write TMEM when it is freed
+        __syncwarp();
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0)
+    {
+        tc_fence_after();
+        tmem_dealloc(tmem, ncols);
+    }
+}
+
+// ---- row-tile 3x3 convolution for the wide, thin layers ----
+//
+// A unit is 128 consecutive output pixels of one row (M = 128).  Per chunk of ck input
+// channels one TMA copy (5-D map, box {8, 130 x, 3 y, ck / 8 chunks, 1}) lands the unit's
+// halo -- 3 input rows of 130 pixels, chunk-major -- and the 9 taps are 9 descriptor start
+// offsets into it ((dy + 1) rows and (dx + 1) pixels on, 16 bytes per pixel and chunk), so
+// every input pixel is fetched for 3 units instead of 9 taps.  The weights of all taps and
+// chunks stay in shared memory for the CTA's lifetime (one bulk copy).  Roles and the
+// double-buffered TMEM accumulators are those of conv_kernel.
+constexpr int ROW_M = 128, ROW_HALO = ROW_M + 2;
+__host__ __device__ constexpr uint32_t row_chunk_bytes() { return 3u * ROW_HALO * 16u; }          // one 8-channel chunk
+__host__ __device__ constexpr uint32_t row_stage_bytes(int ck) { return ((uint32_t)(ck / 8) * row_chunk_bytes() + 1023u) / 1024u * 1024u; }
+
+template <int UNUSED = 0>
+__global__ void __launch_bounds__(PCONV_THREADS, 1) row_conv_kernel(const __grid_constant__ ConvParams p, const __grid_constant__ CUtensorMap xmap)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int S = p.stages;
+    const int chunks = p.cin / p.ck;
+    const uint32_t w_bytes = 9u * (uint32_t)p.cin * p.cout * 2u; // every tap and chunk, packed
+    const uint32_t w_region = (w_bytes + 1023u) / 1024u * 1024u;
+    const uint32_t a_bytes = (uint32_t)(p.ck / 8) * row_chunk_bytes(), stage_bytes = row_stage_bytes(p.ck);
+    uint8_t *wsm = smem;
+    uint8_t *ring = smem + w_region;
+    uint64_t *full = reinterpret_cast<uint64_t *>(ring + (size_t)S * stage_bytes);
+    uint64_t *empty = full + S;
+    uint64_t *acc_full = empty + S;
+    uint64_t *acc_empty = acc_full + 2;
+    uint64_t *mma_done = acc_empty + 2;
+    uint64_t *wbar = mma_done + 1;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(wbar + 1);
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const uint32_t acc_cols = tmem_cols(p.cout), ncols = 2 * acc_cols;
+    const int segs = (p.w + ROW_M - 1) / ROW_M;
+    const int n_units = p.b * p.h * segs;
+
+    if (threadIdx.x == 0)
+    {
+        for (int s = 0; s < S; s++)
+        {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; b++)
+        {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 4);
+        }
+        mbar_init(mma_done, 1);
+        mbar_init(wbar, 1);
         fence_barrier_init();
     }
     if (warp == 0)
@@ -106,99 +331,146 @@ __global__ void __launch_bounds__(CONV_THREADS) conv_kernel(const __grid_constan
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    const int chunks = p.cin / p.ck, iters = TAPS * chunks;
     if (warp == 0 && lane == 0)
     {
-        int issued = 0;
-        for (int it = 0; it < iters; it++)
+        mbar_expect_tx(wbar, w_bytes);
+        for (uint32_t o = 0; o < w_bytes; o += 32768u) // pieces of at most 32 KiB
+            bulk_load(wsm + o, reinterpret_cast<const uint8_t *>(p.wpack) + o, min(32768u, w_bytes - o), wbar);
+        uint32_t g = 0;
+        bool stop = false;
+        for (int u = blockIdx.x; u < n_units && !stop; u += gridDim.x)
         {
-            const int s = it % S, r = it / S;
-            if (r > 0 && !mbar_wait(&empty[s], (uint32_t)((r - 1) & 1), p.status))
-                break;
-            uint8_t *st = smem + (size_t)s * stage_bytes;
-            mbar_expect_tx(&full[s], stage_bytes);
-            const int tap = it / chunks, c = it % chunks;
-            const int dy = TAPS == 9 ? tap / 3 - 1 : 0, dx = TAPS == 9 ? tap % 3 - 1 : 0;
-            for (int j = 0; j < p.ck / 8; j++)
-                tma_load_4d(st + j * BOX_BYTES, &xmap, c * p.ck + 8 * j, x0 + dx, y0 + dy, bi, &full[s]);
-            bulk_load(st + a_bytes, p.wpack + (size_t)it * p.ck * p.cout, b_bytes, &full[s]);
-            issued = it + 1;
+            const int seg = u % segs, row = (u / segs) % p.h, bi = u / (segs * p.h);
+            for (int c = 0; c < chunks; c++, g++)
+            {
+                const uint32_t s = g % (uint32_t)S, r = g / (uint32_t)S;
+                if (r > 0 && !mbar_wait(&empty[s], (r - 1) & 1u, p.status))
+                {
+                    stop = true;
+                    break;
+                }
+                mbar_expect_tx(&full[s], a_bytes);
+                tma_load_5d(ring + (size_t)s * stage_bytes, &xmap, 0, seg * ROW_M - 1, row - 1, c * (p.ck / 8), bi, &full[s]);
+            }
         }
-        for (int it = issued > S ? issued - S : 0; it < issued; it++) // copies still landing
-            if (!mbar_wait(&full[it % S], (uint32_t)((it / S) & 1), p.status))
+        for (uint32_t q = g > (uint32_t)S ? g - (uint32_t)S : 0u; q < g; q++)
+            if (!mbar_wait(&full[q % (uint32_t)S], (q / (uint32_t)S) & 1u, p.status))
                 break;
+        mbar_wait(wbar, 0, p.status);
     }
     else if (warp == 1 && lane == 0)
     {
-        const uint32_t idesc = idesc_bf16(TILE_M, (uint32_t)p.cout, 0, 0);
+        const uint32_t idesc = idesc_bf16(ROW_M, (uint32_t)p.cout, 0, 0);
         const uint32_t lbo_b = (uint32_t)(p.cout / 8) * 128u;
-        for (int it = 0; it < iters; it++)
+        const uint32_t wbase = smem_u32(wsm);
+        uint32_t g = 0;
+        int i = 0;
+        bool stop = !mbar_wait(wbar, 0, p.status);
+        for (int u = blockIdx.x; u < n_units && !stop; u += gridDim.x, i++)
         {
-            const int s = it % S, r = it / S;
-            if (!mbar_wait(&full[s], (uint32_t)(r & 1), p.status))
+            const int buf = i & 1;
+            if (i >= 2 && !mbar_wait(&acc_empty[buf], (uint32_t)(((i >> 1) - 1) & 1), p.status))
                 break;
             tc_fence_after();
-            const uint32_t a0 = smem_u32(smem + (size_t)s * stage_bytes), b0 = a0 + a_bytes;
-            for (int k = 0; k < p.ck / 16; k++)
-                mma_bf16(tmem, smem_desc(a0 + k * 2 * BOX_BYTES, BOX_BYTES, 128), smem_desc(b0 + k * 2 * lbo_b, lbo_b, 128), idesc,
-                         it > 0 || k > 0);
-            mma_commit(&empty[s]);
+            const uint32_t d = tmem + (uint32_t)buf * acc_cols;
+            for (int c = 0; c < chunks; c++, g++)
+            {
+                const uint32_t s = g % (uint32_t)S, r = g / (uint32_t)S;
+                if (!mbar_wait(&full[s], r & 1u, p.status))
+                {
+                    stop = true;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t a0 = smem_u32(ring + (size_t)s * stage_bytes);
+                for (int tap = 0; tap < 9; tap++)
+                {
+                    const uint32_t shift = (uint32_t)((tap / 3) * ROW_HALO + (tap % 3)) * 16u;
+                    const uint32_t b0 = wbase + (uint32_t)(tap * chunks + c) * (uint32_t)p.ck * p.cout * 2u;
+                    for (int k = 0; k < p.ck / 16; k++)
+                        mma_bf16(d, smem_desc(a0 + (uint32_t)(2 * k) * row_chunk_bytes() + shift, row_chunk_bytes(), 128),
+                                 smem_desc(b0 + k * 2 * lbo_b, lbo_b, 128), idesc, c > 0 || tap > 0 || k > 0);
+                }
+                mma_commit(&empty[s]);
+            }
+            if (!stop)
+                mma_commit(&acc_full[buf]);
         }
-        mma_commit(done);
+        mma_commit(mma_done);
+    }
+    else if (warp >= 2)
+    {
+        const int q = warp % 4;
+        const int m = q * 32 + lane;
+        int i = 0;
+        for (int u = blockIdx.x; u < n_units; u += gridDim.x, i++)
+        {
+            const int buf = i & 1;
+            if (!mbar_wait(&acc_full[buf], (uint32_t)((i >> 1) & 1), p.status))
+                break;
+            tc_fence_after();
+            const int seg = u % segs, row = (u / segs) % p.h, bi = u / (segs * p.h);
+            const int px = seg * ROW_M + m;
+            const bool inb = px < p.w;
+            const size_t pix = ((size_t)bi * p.h + row) * p.w + (inb ? px : 0);
+            for (int c0 = 0; c0 < p.cout; c0 += 16)
+            {
+                uint32_t r[16];
+                tmem_ld16(tmem + (uint32_t)buf * acc_cols + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, r);
+                tmem_ld_wait();
+                if (!inb)
+                    continue;
+                float v[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++)
+                {
+                    v[j] = __uint_as_float(r[j]);
+                    if (p.bias)
+                        v[j] += __ldg(p.bias + c0 + j);
+                    if (p.relu)
+                        v[j] = fmaxf(v[j], 0.0f);
+                }
+                if (p.mask)
+                {
+                    const uint4 *mk = reinterpret_cast<const uint4 *>(p.mask + pix * p.cout + c0);
+                    const uint4 m0 = __ldg(mk), m1 = __ldg(mk + 1);
+                    const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+#pragma unroll
+                    for (int j = 0; j < 16; j++)
+                        if (!bf16_positive((uint16_t)(mw[j / 2] >> (16 * (j % 2)))))
+                            v[j] = 0.0f;
+                }
+                uint32_t o[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                {
+                    const __nv_bfloat162 h2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+                    o[j] = *reinterpret_cast<const uint32_t *>(&h2);
+                }
+                uint4 *dst = reinterpret_cast<uint4 *>(p.out + pix * p.cout + c0);
+                dst[0] = make_uint4(o[0], o[1], o[2], o[3]);
+                dst[1] = make_uint4(o[4], o[5], o[6], o[7]);
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0)
+                mbar_arrive(&acc_empty[buf]);
+        }
     }
     __syncwarp();
-
-    const bool ok = mbar_wait(done, 0, p.status);
-    tc_fence_after();
-    if (ok)
+    if (warp == 0)
     {
-        const int m = warp * 32 + lane; // TMEM lane = tile row
-        const int px = x0 + (m % TILE_W), py = y0 + (m / TILE_W);
-        const bool inb = px < p.w && py < p.h;
-        const size_t pix = ((size_t)bi * p.h + (inb ? py : 0)) * p.w + (inb ? px : 0);
-        for (int c0 = 0; c0 < p.cout; c0 += 16)
-        {
-            uint32_t r[16];
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
-            tmem_ld_wait();
-            if (!inb)
-                continue;
-            float v[16];
-#pragma unroll
-            for (int i = 0; i < 16; i++)
-            {
-                v[i] = __uint_as_float(r[i]);
-                if (p.bias)
-                    v[i] += __ldg(p.bias + c0 + i);
-                if (p.relu)
-                    v[i] = fmaxf(v[i], 0.0f);
-            }
-            if (p.mask)
-            {
-                const uint4 *mk = reinterpret_cast<const uint4 *>(p.mask + pix * p.cout + c0);
-                const uint4 m0 = __ldg(mk), m1 = __ldg(mk + 1);
-                const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
-#pragma unroll
-                for (int i = 0; i < 16; i++)
-                    if (!bf16_positive((uint16_t)(mw[i / 2] >> (16 * (i % 2)))))
-                        v[i] = 0.0f;
-            }
-            uint32_t o[8];
-#pragma unroll
-            for (int i = 0; i < 8; i++)
-            {
-                const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
-                o[i] = *reinterpret_cast<const uint32_t *>(&h);
-            }
-            uint4 *dst = reinterpret_cast<uint4 *>(p.out + pix * p.cout + c0);
-            dst[0] = make_uint4(o[0], o[1], o[2], o[3]);
-            dst[1] = make_uint4(o[4], o[5], o[6], o[7]);
-        }
+        if (lane == 0)
+            mbar_wait(mma_done, 0, p.status);
+        __syncwarp();
     }
     tc_fence_before();
     __syncthreads();
     if (warp == 0)
+    {
+        tc_fence_after();
         tmem_dealloc(tmem, ncols);
+    }
 }
 
 struct WgradParams

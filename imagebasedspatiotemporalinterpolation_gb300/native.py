@@ -185,7 +185,7 @@ UNET_SIGNATURES = {
     "isti_flownet_loss": (C.c_int, [_VP, C.POINTER(C.c_void_p)]),
     "isti_flownet_device_status": (C.c_int, [_VP, C.POINTER(C.c_int32)]),
     "isti_render_learned": (C.c_int, [_VP, _VP, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(IstiRenderInfo), C.POINTER(IstiFrameData),
-                                      C.c_int32, _VP]),
+                                      C.c_int32, C.c_int32, _VP]),
     "isti_renderer_learned_stats": (C.c_int, [_VP, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
 }
 

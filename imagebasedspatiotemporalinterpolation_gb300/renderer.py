@@ -191,11 +191,13 @@ class Renderer:
         s = (stream or torch.cuda.current_stream()).cuda_stream
         check(self._lib.isti_render_batch(self._h, n, outs, ris, C.byref(frame_data.to_c()), int(chain), C.c_void_p(s)))
 
-    def render_learned(self, render_buffers, infos, frame_data: DeviceFrame, net=None, iterations: int = 1, stream=None) -> None:
+    def render_learned(self, render_buffers, infos, frame_data: DeviceFrame, net=None, iterations: int = 1, chain: bool = False,
+                       stream=None) -> None:
         """isti_render_learned: the frames of one keyframe pair (main camera only) with the
         search started from the learned initialiser `net` (a flownet.FlowNet; None = at the
         output pixel) and `iterations` search steps; tiles left unresolved are rendered by
-        the plain method.  Each buffer is updated in place like isti_render."""
+        the plain method.  chain: as render_batch's (one persistent buffer across the frames);
+        otherwise each buffer is updated in place like isti_render."""
         torch = _torch()
         n = len(infos)
         if n != len(render_buffers) or not 1 <= n <= native.MAX_BATCH_FRAMES:
@@ -204,7 +206,7 @@ class Renderer:
         outs = (C.c_void_p * n)(*[_dptr(b) for b in render_buffers])
         s = (stream or torch.cuda.current_stream()).cuda_stream
         check(self._lib.isti_render_learned(self._h, net.handle if net is not None else None, n, outs, ris,
-                                            C.byref(frame_data.to_c()), int(iterations), C.c_void_p(s)))
+                                            C.byref(frame_data.to_c()), int(iterations), int(chain), C.c_void_p(s)))
 
     def learned_stats(self) -> tuple[int, int]:
         """(tiles rendered by the plain method, all tiles) of the last learned call (waits)."""

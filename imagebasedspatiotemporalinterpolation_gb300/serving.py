@@ -457,9 +457,12 @@ class PinnedPair:
 
 class CudaBackend:
     """Device side of the request loop: torch for buffers, streams and events, libisti for
-    every pixel (isti_render_batch)."""
+    every pixel.  With a learned-initialiser checkpoint (`learned_weights`), batches of
+    main-camera frames in modes 0/2 go through isti_render_learned (network guess, 1 search
+    iteration, per-tile plain fallback); every other batch through isti_render_batch.  Each
+    slot owns its network instance (activations are per instance)."""
 
-    def __init__(self, device="cuda"):
+    def __init__(self, device="cuda", learned_weights: str | None = None, learned_iterations: int = 1):
         import torch
 
         from .native import MAX_BATCH_FRAMES
@@ -467,6 +470,9 @@ class CudaBackend:
         self.device = torch.device(device)
         self.max_batch = MAX_BATCH_FRAMES
         self.upload_stream = torch.cuda.Stream(self.device)
+        self.learned_weights = learned_weights
+        self.learned_iterations = learned_iterations
+        self.learned_batches = self.plain_batches = 0
 
     @staticmethod
     def slot_bytes(pixels: int, views: int, frames: int) -> int:
@@ -484,7 +490,11 @@ class CudaBackend:
 
     def new_slot(self):
         from .renderer import Renderer
-        return (self.torch.cuda.Stream(self.device), Renderer())
+        slot = [self.torch.cuda.Stream(self.device), Renderer()]
+        if self.learned_weights:
+            from . import train_flownet
+            slot.append(train_flownet.load(self.learned_weights))
+        return tuple(slot)
 
     def alloc_pair(self, template):
         from .renderer import DeviceFrame, DeviceView
@@ -524,12 +534,18 @@ class CudaBackend:
         """Renders infos into outs (chained or not) after copying each (index, buffer) of
         `prefill` into outs[index]."""
         torch = self.torch
-        stream, renderer = slot
+        stream, renderer = slot[0], slot[1]
+        net = slot[2] if len(slot) > 2 else None
         self._wait(stream, waits)
         with torch.cuda.stream(stream):
             for i, src in prefill:
                 outs[i].copy_(src, non_blocking=True)
-            renderer.render_batch(outs, infos, dev_pair, chain=chain, stream=stream)
+            if net is not None and not dev_pair.aux_curr and all(int(i.mode) in (0, 2) for i in infos):
+                renderer.render_learned(outs, infos, dev_pair, net, self.learned_iterations, chain=chain, stream=stream)
+                self.learned_batches += 1
+            else:
+                renderer.render_batch(outs, infos, dev_pair, chain=chain, stream=stream)
+                self.plain_batches += 1
         ev = torch.cuda.Event()
         ev.record(stream)
         return ev

@@ -102,8 +102,8 @@ isti_status isti_flownet_device_status(isti_flownet *net, int32_t *status);
 /* ---- the learned render path ----
  *
  * Renders n_frames client frames of one keyframe pair (main camera only, modes 0 and
- * 2) like isti_render_batch with chain_outputs = 0, with the search started from the
- * network's guess instead of splatting:
+ * 2) like isti_render_batch (chain_outputs with the same meaning), with the search
+ * started from the network's guess instead of splatting:
  *  1. per keyframe pair: the client-independent part of the splat kernel (world
  *     positions and their motion, keyframe-to-keyframe flow);
  *  2. per frame: the network input at quarter resolution (inverse depth, object
@@ -118,10 +118,13 @@ isti_status isti_flownet_device_status(isti_flownet *net, int32_t *status);
  *     source pixel that splats into it, window initialisation and 3 iterations --
  *     with the plain path's results.
  * net == NULL starts every search at the output pixel itself (no initialiser).
+ * iterations == -1 sends every tile to the plain method (the result then equals
+ * isti_render_batch's bit for bit: a check of the fallback).
  * No host synchronisation; isti_renderer_learned_stats waits and reports how many
  * tiles of the last call went to the plain method. */
 isti_status isti_render_learned(isti_renderer *r, isti_flownet *net, int32_t n_frames, void *const *out_rgba,
-                                const isti_render_info *infos, const isti_frame_data *frame, int32_t iterations, void *stream);
+                                const isti_render_info *infos, const isti_frame_data *frame, int32_t iterations, int32_t chain_outputs,
+                                void *stream);
 isti_status isti_renderer_learned_stats(isti_renderer *r, int32_t *fallback_tiles, int32_t *tiles);
 
 #ifdef __cplusplus

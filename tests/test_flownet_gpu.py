@@ -53,12 +53,16 @@ def test_forward_and_gradients_match_oracle(cuda):
 
 
 def test_training_reduces_loss(cuda):
+    """Labels that are a learnable function of the input (a per-pixel linear map of the
+    first channels) must be fitted: the loss halves within 60 Adam steps."""
     import torch
     net = FlowNet(seed=4)
-    x, label = _batch(12)
+    x, _ = _batch(12)
+    mix = torch.tensor([[0.8, -0.3, 0.0, 0.5], [0.2, 0.6, -0.4, 0.0], [0.0, 0.1, 0.9, -0.2], [-0.5, 0.0, 0.3, 0.7]], device="cuda")
+    label = (x.float()[..., :4] @ mix).contiguous()
     net.backward(x, label)
     first = net.loss()
-    for _ in range(40):
+    for _ in range(60):
         net.backward(x, label)
         net.adam(3e-3)
     net.backward(x, label)

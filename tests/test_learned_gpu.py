@@ -1,0 +1,115 @@
+"""The learned render path (isti_render_learned) on the GPU.
+
+* Fallback exactness: with every tile sent to the plain method (iterations = -1)
+  the output equals isti_render_batch's bit for bit -- the fallback's key reset,
+  filtered splat, window initialisation, on-the-fly client flow and colour are the
+  plain path's.
+* Converged pixels: a learned frame differs from the plain frame only where the
+  plain and learned searches ended at different sources; at least 95 % of the
+  pixels the plain method writes are identical (main camera, 640x360).
+* The trained initialiser (committed weights) against no initialiser, at 1080p on
+  held-out seeds: fewer tiles go to the plain method, and the frames lose on average
+  at most 0.1 dB PSNR against the analytic ray-cast compared with the plain method
+  (no single keyframe pair more than 0.2 dB).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from imagebasedspatiotemporalinterpolation_gb300 import train_flownet as T
+from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame, Renderer
+from imagebasedspatiotemporalinterpolation_gb300.scene import Sequence
+
+pytestmark = pytest.mark.gpu
+
+
+def _frames(seq, k=0):
+    return DeviceFrame.from_host(seq.frame(k)), [seq.client(k, b) for b in (1, 2, 3)]
+
+
+def test_all_tiles_plain_equals_plain_path(cuda):
+    import torch
+    seq = Sequence(640, 360, 2, seed=515, max_speed=1.0, max_rot_deg=3.0)
+    frame, clients = _frames(seq)
+    prev = torch.full((360, 640, 4), 9, dtype=torch.uint8, device="cuda")
+    r = Renderer()
+    want = [prev.clone() for _ in clients]
+    r.render_batch(want, clients, frame, chain=False)
+    got = [prev.clone() for _ in clients]
+    r.render_learned(got, clients, frame, None, iterations=-1)
+    fb, tiles = r.learned_stats()
+    assert fb == tiles
+    for k, (a, b) in enumerate(zip(got, want)):
+        assert torch.equal(a, b), f"frame {k}: {int((a != b).any(-1).sum())} pixels differ"
+    r.close()
+
+
+def test_all_tiles_plain_chained_equals_plain_path(cuda):
+    """Chained outputs (one persistent buffer across the frames) through the fallback."""
+    import torch
+    seq = Sequence(640, 360, 2, seed=517, max_speed=1.0, max_rot_deg=3.0)
+    frame, clients = _frames(seq)
+    prev = torch.full((360, 640, 4), 9, dtype=torch.uint8, device="cuda")
+    r = Renderer()
+    want = [prev.clone() for _ in clients]
+    r.render_batch(want, clients, frame, chain=True)
+    got = [prev.clone() for _ in clients]
+    r.render_learned(got, clients, frame, None, iterations=-1, chain=True)
+    for k, (a, b) in enumerate(zip(got, want)):
+        assert torch.equal(a, b), f"frame {k}: {int((a != b).any(-1).sum())} pixels differ"
+    r.close()
+
+
+def test_learned_without_network_mostly_matches_plain(cuda):
+    import torch
+    seq = Sequence(640, 360, 2, seed=516, max_speed=0.5, max_rot_deg=1.0)
+    frame, clients = _frames(seq)
+    prev = torch.full((360, 640, 4), 9, dtype=torch.uint8, device="cuda")
+    r = Renderer()
+    want = [prev.clone() for _ in clients]
+    r.render_batch(want, clients, frame, chain=False)
+    got = [prev.clone() for _ in clients]
+    r.render_learned(got, clients, frame, None, iterations=3)
+    assert r.device_status() == 0
+    for a, b in zip(got, want):
+        written = (b != prev).any(-1)
+        same = (a == b).all(-1)
+        assert float(same[written].float().mean()) >= 0.95
+    r.close()
+
+
+@pytest.mark.skipif(not os.path.exists(T.DEFAULT_WEIGHTS), reason="trained weights not present")
+def test_trained_initialiser_beats_no_initialiser(cuda):
+    import torch
+    net = T.load()
+    fb_net, fb_none, dpsnr = [], [], []
+    for seed in range(2):
+        rng = np.random.default_rng(T.EVAL_SEED_BASE + 100 + seed)
+        seq = Sequence(1920, 1080, 2, seed=T.EVAL_SEED_BASE + 100 + seed, n_spheres=int(rng.integers(16, 257)), max_speed=1.0,
+                       max_rot_deg=5.0, max_step_m=0.1)
+        frame, clients = _frames(seq)
+        gts = [seq.ground_truth(0, b) for b in (1, 2, 3)]
+        prev = torch.from_numpy(seq.frame(0).fwd.color).cuda()
+        r = Renderer()
+
+        def psnr(outs):
+            vals = []
+            for o, g in zip(outs, gts):
+                mse = np.mean((o.cpu().numpy()[..., :3].astype(np.float64) - g[..., :3]) ** 2)
+                vals.append(10 * np.log10(255.0 ** 2 / mse))
+            return float(np.mean(vals))
+
+        plain = [prev.clone() for _ in clients]
+        r.render_batch(plain, clients, frame, chain=False)
+        learned = [prev.clone() for _ in clients]
+        r.render_learned(learned, clients, frame, net, iterations=1)
+        fb_net.append(r.learned_stats()[0])
+        none = [prev.clone() for _ in clients]
+        r.render_learned(none, clients, frame, None, iterations=1)
+        fb_none.append(r.learned_stats()[0])
+        dpsnr.append(psnr(plain) - psnr(learned))
+        r.close()
+    assert sum(fb_net) < sum(fb_none), (fb_net, fb_none)
+    assert float(np.mean(dpsnr)) <= 0.1 and max(dpsnr) <= 0.2, dpsnr
+    net.close()

@@ -314,3 +314,64 @@ def test_closing_an_idle_client_frees_its_budget_at_once():
     assert server.reserved == slot + need
     server.close_client(1)
     assert server.reserved == slot and not server.clients
+
+
+def _fold_chain(prev, infos_and_content):
+    v = prev
+    for info_v, content in infos_and_content:
+        v = fold(v, info_v, content)
+    return v
+
+
+def test_client_disconnecting_mid_batch():
+    """A client closes while one of its batches runs on the device: its requests already
+    submitted are completed (results equal sequential renders), new requests are refused,
+    its budget is released only after the batch finished, and another client is unaffected."""
+    rng = random.Random(5)
+    be = FakeBackend(rng, max_advance=0)          # nothing runs until waited for
+    results = {}
+    server = Server(be, hbm_budget=10**12, n_slots=2, max_batch=4, slot_pixels=64 * 36, clock=Clock(),
+                    on_complete=lambda r: results.__setitem__(r.rid, r.out.v))
+    for c in (0, 1):
+        assert server.open_client(c, 64, 36, 1, Pair(100))
+        server.push_pair(c, HostPair(10 + c))
+    reqs = {0: [], 1: []}
+    for i in range(3):
+        for c in (0, 1):
+            reqs[c].append((server.submit(c, 0, (i + 7 * c, (c, 0), 10 + c)), i + 7 * c))
+    server.step()
+    assert any(b is not None and b.client.cid == 0 for b in server.running), "client 0 has a batch in flight"
+    reserved = server.reserved
+    server.close_client(0)
+    assert server.admitted(0)                      # still draining its requests
+    with pytest.raises(ValueError):
+        server.submit(0, 0, (99, (0, 0), 10))
+    be.max_advance = 3                             # let the device run
+    server.drain(timeout_s=5.0)
+    assert not server.admitted(0) and server.admitted(1)
+    assert server.reserved < reserved
+    for c in (0, 1):
+        prev = 0
+        for r, info_v in reqs[c]:
+            prev = fold(prev, info_v, 10 + c)
+            assert results[r.rid] == prev
+
+
+def test_keyframe_missing_at_request_time():
+    """No keyframe pair yet: the request is refused.  A pair pushed but not yet uploaded on
+    the device: the request is accepted and its batch waits for the upload (the fake device
+    asserts that no batch runs before its pair's upload)."""
+    rng = random.Random(6)
+    be = FakeBackend(rng, max_advance=0)
+    results = {}
+    server = Server(be, hbm_budget=10**12, n_slots=1, max_batch=2, slot_pixels=64 * 36, clock=Clock(),
+                    on_complete=lambda r: results.__setitem__(r.rid, r.out.v))
+    assert server.open_client(0, 64, 36, 1, Pair(100))
+    with pytest.raises(ValueError):
+        server.submit(0, 0, (1, (0, 0), 21))
+    server.push_pair(0, HostPair(21))
+    r = server.submit(0, 0, (1, (0, 0), 21))      # the upload has not run on the device yet
+    server.step()
+    be.max_advance = 3
+    server.drain(timeout_s=5.0)
+    assert results[r.rid] == fold(0, 1, 21)
