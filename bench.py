@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-initialiser comparison")
     ap.add_argument("--no-config1", action="store_true", help="skip the 640x360 configuration")
     ap.add_argument("--no-reference-gpu", action="store_true", help="skip timing the reference's own GPU build")
+    ap.add_argument("--no-arith-compare", action="store_true",
+                    help="skip timing the same steps under the reference's GPU arithmetic (fast-math build)")
     ap.add_argument("--clock-log", default=None, help="write the raw nvidia-smi clock samples of the timed region to this CSV")
     return ap.parse_args()
 
@@ -232,7 +234,7 @@ def main_ours(args):
     import numpy as np
     import torch
 
-    from imagebasedspatiotemporalinterpolation_gb300 import _build
+    from imagebasedspatiotemporalinterpolation_gb300 import _build, native
     from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame, DeviceView, Renderer
     from imagebasedspatiotemporalinterpolation_gb300.scene import Sequence
 
@@ -312,6 +314,32 @@ def main_ours(args):
     step_ms = sorted(a.elapsed_time(b) for a, b in sev)
     n_frames = args.steps * len(TS)
     value = world * n_frames * W * H / 1e6 / (ms / 1e3)
+
+    # ---- the same steps under the reference's GPU arithmetic (ISTI_ARITH_REFERENCE_GPU: the
+    # kernels built with -use_fast_math, bit-exact against the reference's own sm_103a build)
+    arith = None
+    if not args.no_arith_compare:
+        r.set_arithmetic(native.ARITH_REFERENCE_GPU)
+        for s in range(args.warmup):
+            step(s)
+        torch.cuda.synchronize()
+        r.timing()
+        r.enable_timing(True)
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for s in range(args.steps):
+            step(s)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        r.enable_timing(False)
+        ftim = r.timing()
+        fcalls = max(1, ftim["frames"] // len(TS))
+        fms = f0.elapsed_time(f1)
+        arith = {"arithmetic": "reference GPU (fast-math)", "value": round(n_frames * W * H / 1e6 / (fms / 1e3), 2), "unit": "Mpix/s",
+                 "ms_per_step": round(fms / args.steps, 4),
+                 "kernels_ms_per_call": {"key_init": round(ftim["init_ms"] / fcalls, 4), "splat_kernel": round(ftim["splat_ms"] / fcalls, 4),
+                                         "reproj_kernel": round(ftim["reproj_ms"] / fcalls, 4)}}
+        r.set_arithmetic(native.ARITH_IEEE)
 
     # ---- the same frames through the single-frame call (isti_render), for comparison
     per_frame = None
@@ -437,6 +465,7 @@ def main_ours(args):
                                     "splat_kernel": round(per_launch_ms["splat_kernel"], 4),
                                     "reproj_kernel": round(per_launch_ms["reproj_kernel"], 4)},
             "per_frame_api": per_frame,
+            "arith_reference_gpu": arith,
             "learned_vs_plain": learned,
             "config1": config1,
             "reference_gpu": reference_gpu,
@@ -756,7 +785,51 @@ def run_graph_batch(args, dev, rank):
                 raise RuntimeError(f"graph batch: {w}x{h} frame {k} differs from the per-frame call")
     single.close()
     r.close()
+
+    # the same batch as ONE persistent launch (isti_render_pairs: a cooperative kernel over a
+    # device work queue of init / splat / reprojection units), captured once and replayed; its
+    # frames must equal the 48-launch graph's bit for bit
+    persistent = None
+    try:
+        rp = Renderer()
+        pouts = [[torch.zeros_like(o) for o in os_] for os_ in outs]
+        pjobs = [(po, infos, frame) for po, (w, h, frame, infos) in zip(pouts, jobs)]
+        with torch.cuda.stream(stream):
+            rp.render_pairs(pjobs, stream=stream)       # sizes the arena outside the capture
+        stream.synchronize()
+        pgraph = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(stream):
+            with torch.cuda.graph(pgraph, stream=stream):
+                rp.render_pairs(pjobs, stream=stream)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            for _ in range(max(args.warmup, 3)):
+                pgraph.replay()
+            pev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+            stream.synchronize()
+            p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            p0.record(stream)
+            for e0, e1 in pev:
+                e0.record(stream)
+                pgraph.replay()
+                e1.record(stream)
+            p1.record(stream)
+        stream.synchronize()
+        pms = p0.elapsed_time(p1) / args.steps
+        pb = sorted(a.elapsed_time(b) for a, b in pev)
+        same = all(torch.equal(a, b) for po, o in zip(pouts, outs) for a, b in zip(po, o))
+        if not same:
+            raise RuntimeError("persistent launch: frames differ from the per-pair launches")
+        if rp.device_status() != 0:
+            raise RuntimeError("persistent launch: a bounded wait gave up")
+        rp.close()
+        persistent = {"value": round(mpix / (pms / 1e3), 2), "unit": "Mpix/s", "ms_per_batch": round(pms, 4),
+                      "p50_batch_ms": round(pb[len(pb) // 2], 4), "p99_batch_ms": round(pb[min(len(pb) - 1, int(0.99 * len(pb)))], 4),
+                      "launches_per_batch": 1, "equal_to_per_pair_launches": True}
+    except Exception as ex:  # reported, not fatal: the per-pair graph is the reference line
+        persistent = {"error": str(ex)[:300]}
     return {"value": round(mpix / (ms / 1e3), 2), "unit": "Mpix/s", "mpix_per_batch": round(mpix, 2),
+            "persistent_single_launch": persistent,
             "frames_per_batch": sum(len(infos) for _, _, _, infos in jobs), "ms_per_batch": round(ms, 4),
             "p50_batch_ms": round(batch_ms[len(batch_ms) // 2], 4),
             "p99_batch_ms": round(batch_ms[min(len(batch_ms) - 1, int(0.99 * len(batch_ms)))], 4),

@@ -205,14 +205,14 @@ __device__ __forceinline__ float2 view_pixel2cs(const V &v, uint32_t x, uint32_t
 
 // ---- key initialisation (cudaMemset 0xfe, src/renderer.cu:632-638) + pixel->clip tables ----
 
-__global__ void __launch_bounds__(256) init_kernel(const __grid_constant__ FrameParams p)
+// Thread t of `stride` threads: keys t, t + stride, ... and table entry t of every view
+// (and, when asked, the status word).
+__device__ __forceinline__ void init_part(const FrameParams &p, size_t t, size_t stride, bool reset_status = true)
 {
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const ulonglong2 empty = make_ulonglong2(SPLAT_EMPTY, SPLAT_EMPTY);
     for (size_t i = t; i < p.key_units; i += stride)
         p.keys[i] = empty;
-    if (t == 0)
+    if (t == 0 && reset_status)
         *p.status = 0;
     if (t < 65536)
         for (int k = 0; k < p.n_views; k++)
@@ -225,15 +225,19 @@ __global__ void __launch_bounds__(256) init_kernel(const __grid_constant__ Frame
         }
 }
 
+__global__ void __launch_bounds__(256) init_kernel(const __grid_constant__ FrameParams p)
+{
+    init_part(p, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
+}
+
 // ---- computeFlowFields_sortedSplatting_kernel, src/renderer.cu:76-146 ----
 
 // 8 blocks of 256 threads per SM (32 registers, a few spilled words): 64 resident warps
 // instead of 56 at the natural 36 registers, 3-8 % faster (1080p, 3 frames, 2-6 views).
-__global__ void __launch_bounds__(256, 8) splat_kernel(const __grid_constant__ FrameParams p)
+// One source pixel (x, y) of view `view`: the keyframe part, then every frame's client part.
+__device__ __forceinline__ void splat_pixel(const FrameParams &p, int view, uint32_t x, uint32_t y)
 {
-    const DevView &v = p.v[blockIdx.z];
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
+    const DevView &v = p.v[view];
     if (x >= v.w || y >= v.h)
         return;
     const uint32_t idx = y * v.w + x;
@@ -288,6 +292,11 @@ __global__ void __launch_bounds__(256, 8) splat_kernel(const __grid_constant__ F
             atomicMin(keys + idx, encode_key(z_to_depth(z_from), x, y));
         }
     }
+}
+
+__global__ void __launch_bounds__(256, 8) splat_kernel(const __grid_constant__ FrameParams p)
+{
+    splat_pixel(p, blockIdx.z, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
 }
 
 // ---- colour: colorFromShadow / secondChanceAndBlend_kernel, src/renderer.cu:217-327 ----
@@ -677,31 +686,30 @@ __device__ __forceinline__ unsigned long long window_key(const unsigned long lon
 // view.  The block works through units (frame k, row pair): phase 1 runs one unit at a time
 // on every warp; phases 2-3 spread the units' rows over the warps.  More row pairs per block
 // (for single frames) keep every warp busy in phase 2.
+// One reprojection block (bx, by) of frame batch p, executed by a block of (32, n_views)
+// threads: the body of reproj_kernel, also run as a work unit of batch_kernel.  `maps`: the
+// views' key-tile tensor maps; `bar`: the block's TMA completion barrier, initialised once per
+// thread block; `round`: TMA rounds that barrier has completed so far (its phase carries over
+// from unit to unit); `block_id`: the index the test hook `withhold_block` refers to.  Every
+// thread returns together (early exits are block-uniform or come after the last barrier).
 template <int SW, int SI, bool MAV, int REGS>
-__global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FrameParams p, const __grid_constant__ KeyMaps km)
+__device__ __forceinline__ void reproj_block(const FrameParams &p, const CUtensorMap *maps, uint32_t bx, uint32_t by, uint32_t block_id,
+                                             unsigned char *smem, unsigned long long &bar, int &round)
 {
     using T = Tile<SW>;
-    // dynamic shared memory only (no static __shared__ in front of it): the key tiles start at
-    // the 1 KiB-aligned window base, so every TMA destination is 128-byte aligned
-    extern __shared__ __align__(1024) unsigned char smem[];
     const int nv = p.n_views, nf = p.n_frames, np = p.row_pairs, nu = nf * np;
     // [key tiles, phase 1 | chained colours and flags, phases 2-3 (same bytes)][results][barrier]
     unsigned long long *tiles = reinterpret_cast<unsigned long long *>(smem);                 // [nv][H][W]
     uint32_t *cols = reinterpret_cast<uint32_t *>(smem);                                      // [nu][ROWS][32]
     uint32_t *valid = cols + nu * ROWS * 32;                                                 // [nu][ROWS][32]
     DirRes *res = reinterpret_cast<DirRes *>(smem + reproj_tile_region<SW>(nv, nu));         // [nu][ROWS][nv][32]
-    unsigned long long &bar = *reinterpret_cast<unsigned long long *>(res + nu * ROWS * nv * 32); // TMA completion barrier
 
     const int lane = threadIdx.x, vw = threadIdx.y;
-    const uint32_t x0 = blockIdx.x * 32, x = x0 + lane, yb = blockIdx.y * (ROWS * np);
+    const uint32_t x0 = bx * 32, x = x0 + lane, yb = by * (ROWS * np);
     const bool xok = x < p.out_w;
     const bool leader = lane == 0 && vw == 0;
-    if (p.use_tma)
-    {
-        if (leader)
-            mbar_init(&bar, 1);
-        __syncthreads();
-    }
+    const int round0 = round;
+    bool failed = false; // this thread's wait for the key tiles gave up (status word set)
     {
         const DevView &v = p.v[vw];
         const uint32_t ix = v.sx == 1 ? x : x / v.sx, tx0 = v.sx == 1 ? x0 : x0 / v.sx;
@@ -714,7 +722,6 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
         const float qx = __ldg(v0.lut + xc);
         const float pcx = __ldg(v.lut + min(ix, v.w - 1));
         const uint32_t vwid = v.w, vhei = v.h;
-        int round = 0; // TMA rounds so far (mbarrier phase parity)
 #pragma unroll 1
         for (int rp = 0; rp < np; rp++)
         {
@@ -729,27 +736,27 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
         for (int k = 0; k < nf; k++, round++)
         {
             const int u = k * np + rp;
-            if (round > 0)
-                __syncthreads(); // every warp is done with the previous unit's tiles
+            // every warp is done with the previous unit's tiles; a block in which any thread's wait
+            // gave up leaves here, every thread together, having written nothing
+            if (round > round0 && __syncthreads_or(failed ? 1 : 0))
+                return;
             if (p.use_tma)
             {
                 if (leader)
                 {
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     mbar_expect_tx(&bar, (uint32_t)(nv * T::BYTES));
-                    if (p.withhold_block != (int32_t)(blockIdx.y * gridDim.x + blockIdx.x))
+                    if (p.withhold_block != (int32_t)block_id)
                         for (int w = 0; w < nv; w++)
                         {
                             const DevView &vv = p.v[w];
                             const uint32_t wx0 = vv.sx == 1 ? x0 : x0 / vv.sx, wy0 = vv.sy == 1 ? y0 : y0 / vv.sy;
-                            tma_load_3d(tiles + (size_t)w * T::ELEMS, &km.m[w], tile_x0(wx0, SW), (int)wy0 - SW, k, &bar);
+                            tma_load_3d(tiles + (size_t)w * T::ELEMS, &maps[w], tile_x0(wx0, SW), (int)wy0 - SW, k, &bar);
                         }
                 }
-                // A block whose copies did not arrive (status word set) reads none of its tiles
-                // and writes nothing; the decision is block-wide, so every thread leaves together.
-                const bool arrived = mbar_wait_bounded(&bar, (uint32_t)(round & 1), p.status, p.wait_limit);
-                if (__syncthreads_or(arrived ? 0 : 1))
-                    return;
+                // a thread whose copies did not arrive reads none of the tiles; the block leaves at
+                // its next barrier (the next unit's, or the one before phase 2)
+                failed = !mbar_wait_bounded(&bar, (uint32_t)(round & 1), p.status, p.wait_limit);
             }
             else
             {
@@ -768,6 +775,7 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
                 }
                 __syncwarp();
             }
+            if (!failed)
             {
                 const unsigned long long *tg = tiles + (size_t)vw * T::ELEMS;
                 const float4 *cam = v.cam_ff + k * p.cam_stride;
@@ -857,7 +865,8 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
         }
         }
     }
-    __syncthreads();
+    if (__syncthreads_or(failed ? 1 : 0))
+        return;
 
     // phase 2: (unit, row) tasks over the warps
 #pragma unroll 1
@@ -904,6 +913,28 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
         else if (k > 0)
             *o = run;
     }
+}
+
+// bidirectionalReprojection_kernel<SW, SI, MAIN_ALWAYS_VALID>, src/renderer.cu:400-465
+// block = (32, n_views): 32 output columns x (2 * row_pairs) output rows, one warp per source
+// view (reproj_block).
+template <int SW, int SI, bool MAV, int REGS>
+__global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FrameParams p, const __grid_constant__ KeyMaps km)
+{
+    // dynamic shared memory only (no static __shared__ in front of it): the key tiles start at
+    // the 1 KiB-aligned window base, so every TMA destination is 128-byte aligned
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned long long &bar = *reinterpret_cast<unsigned long long *>(
+        smem + reproj_tile_region<SW>(p.n_views, p.n_frames * p.row_pairs) +
+        (size_t)p.n_frames * p.row_pairs * ROWS * p.n_views * 32 * sizeof(DirRes)); // TMA completion barrier
+    if (p.use_tma)
+    {
+        if (threadIdx.x == 0 && threadIdx.y == 0)
+            mbar_init(&bar, 1);
+        __syncthreads();
+    }
+    int round = 0;
+    reproj_block<SW, SI, MAV, REGS>(p, km.m, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x, smem, bar, round);
 }
 
 // ---- timewarp (mode 4), src/renderer.cu:467-522, 615-629 ----

@@ -15,6 +15,7 @@
 #include "isti_kernels.cuh"
 #include "isti_launch.cuh"
 #include "isti_learned.cuh"
+#include "isti_batch.cuh"
 #include "isti_unet.h"
 #include "isti_train.h"
 #include "host/isti_error.hpp"
@@ -58,6 +59,13 @@ struct isti_renderer
     // failure-detection test hook (isti_renderer_test_withhold_tile)
     int32_t withhold_x = -1, withhold_y = -1;
     uint32_t wait_limit = 0;
+    // isti_render_pairs: device arena (every pair's intermediates, then the parameter block),
+    // pinned staging of the parameter block and the event of its last copy
+    void *multi_arena = nullptr;
+    size_t multi_bytes = 0;
+    void *multi_host = nullptr;
+    size_t multi_host_bytes = 0;
+    cudaEvent_t multi_copied = nullptr;
 };
 
 namespace
@@ -489,6 +497,12 @@ isti_status isti_renderer_destroy(isti_renderer *r)
         cudaEventDestroy(ev);
     if (r->learned_arena)
         cudaFree(r->learned_arena);
+    if (r->multi_arena)
+        cudaFree(r->multi_arena);
+    if (r->multi_host)
+        cudaFreeHost(r->multi_host);
+    if (r->multi_copied)
+        cudaEventDestroy(r->multi_copied);
     if (r->arena)
     {
         cudaError_t e = cudaFree(r->arena);
@@ -639,6 +653,243 @@ isti_status isti_renderer_view_buffers(const isti_renderer *r, int32_t view, con
 }
 
 } // extern "C"
+
+// ============================ many keyframe pairs, one persistent launch ============================
+
+namespace
+{
+template <int SW, int SI, bool MAV, int REGS>
+cudaError_t launch_pairs_kernel(const isti::BatchParams &bp, size_t smem, unsigned threads_y, cudaStream_t stream)
+{
+    auto kernel = isti::batch_kernel<SW, SI, MAV, REGS>;
+    static std::mutex mu;
+    static size_t set_bytes[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    if (smem > 48 * 1024)
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (smem > set_bytes[dev & 63])
+        {
+            e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess)
+                return e;
+            set_bytes[dev & 63] = smem;
+        }
+    }
+    int per_sm = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, (int)(32 * threads_y), smem);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess)
+        return e;
+    if (per_sm < 1)
+        return cudaErrorInvalidConfiguration;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)(per_sm * sms));
+    cfg.blockDim = dim3(32, threads_y);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative; // every CTA resident: the units' waits always end
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, bp);
+}
+
+cudaError_t launch_pairs_mode(int mode, int regs, const isti::BatchParams &bp, size_t smem, unsigned threads_y, cudaStream_t stream)
+{
+    switch (mode)
+    {
+    case ISTI_MODE_OURS:
+    case ISTI_MODE_BACKWARD_UNIDIRECTIONAL:
+        return regs == isti::REPROJ_REGS_MANY_VIEWS ? launch_pairs_kernel<1, 3, false, isti::REPROJ_REGS_MANY_VIEWS>(bp, smem, threads_y, stream)
+                                                    : launch_pairs_kernel<1, 3, false, isti::REPROJ_REGS>(bp, smem, threads_y, stream);
+    case ISTI_MODE_SPLATTING:
+        return regs == isti::REPROJ_REGS_MANY_VIEWS ? launch_pairs_kernel<1, 0, false, isti::REPROJ_REGS_MANY_VIEWS>(bp, smem, threads_y, stream)
+                                                    : launch_pairs_kernel<1, 0, false, isti::REPROJ_REGS>(bp, smem, threads_y, stream);
+    case ISTI_MODE_BACKWARD_BIDIRECTIONAL:
+        return launch_pairs_kernel<3, 5, true, isti::REPROJ_REGS_WIDE_WINDOW>(bp, smem, threads_y, stream);
+    }
+    return cudaErrorInvalidValue;
+}
+
+template <int SW>
+bool pair_maps(const isti::FrameParams &p, isti::KeyMaps &km)
+{
+    return isti::make_key_maps<SW>(p, km);
+}
+} // namespace
+
+extern "C" isti_status isti_render_pairs(isti_renderer *r, int32_t n_pairs, const isti_pair_frames *pairs, void *stream_ptr)
+{
+    if (!r || !pairs)
+        return fail(ISTI_ERR_INVALID_ARG, "NULL argument");
+    if (n_pairs < 1 || n_pairs > ISTI_MAX_PAIRS)
+        return fail(ISTI_ERR_INVALID_ARG, "n_pairs must be 1..ISTI_MAX_PAIRS");
+    if (r->arith != ISTI_ARITH_IEEE)
+        return fail(ISTI_ERR_UNSUPPORTED, "isti_render_pairs runs the IEEE kernels");
+    const cudaStream_t stream = static_cast<cudaStream_t>(stream_ptr);
+    int cur = 0;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaGetDevice");
+    if (cur != r->device)
+        return fail(ISTI_ERR_INVALID_ARG, "renderer was created on another device");
+    // validation and the arena layout: every pair's intermediates, then the parameter block
+    std::vector<Layout> layouts(n_pairs);
+    std::vector<std::vector<const isti_view *>> views(n_pairs);
+    int mode = -1, nv = 0;
+    size_t data_bytes = 0;
+    for (int i = 0; i < n_pairs; i++)
+    {
+        const isti_pair_frames &pf = pairs[i];
+        if (!pf.frame || !pf.out_rgba || !pf.infos)
+            return fail(ISTI_ERR_INVALID_ARG, "NULL pair argument");
+        const isti_view *vv[isti::MAX_VIEWS];
+        int n_views = 0;
+        isti_status st = validate(pf.n_frames, pf.out_rgba, pf.infos, pf.frame, vv, n_views);
+        if (st != ISTI_OK)
+            return st;
+        if (i == 0)
+        {
+            mode = pf.infos[0].mode;
+            nv = n_views;
+        }
+        if (pf.infos[0].mode != mode || n_views != nv)
+            return fail(ISTI_ERR_INVALID_ARG, "all pairs of isti_render_pairs need the same mode and number of views");
+        if (mode == ISTI_MODE_TIMEWARP)
+            return fail(ISTI_ERR_UNSUPPORTED, "isti_render_pairs does not render timewarp frames");
+        views[i].assign(vv, vv + n_views);
+        layouts[i] = layout_of(vv, n_views, pf.n_frames);
+        data_bytes += align_up(layouts[i].total, 256);
+    }
+    const size_t fp_bytes = align_up(sizeof(isti::FrameParams) * n_pairs, 256);
+    const size_t map_bytes = align_up(sizeof(CUtensorMap) * isti::MAX_VIEWS * n_pairs, 256);
+    const size_t pair_bytes = align_up(sizeof(isti::BatchPair) * n_pairs, 256);
+    const size_t seg_bytes = align_up(sizeof(isti::BatchSeg) * 3 * n_pairs, 256);
+    const size_t cnt_bytes = align_up(sizeof(uint32_t) * (2 + 2 * n_pairs), 256);
+    const size_t block_bytes = fp_bytes + map_bytes + pair_bytes + seg_bytes + cnt_bytes;
+    const size_t total = data_bytes + block_bytes;
+    if (total > r->multi_bytes)
+    {
+        if (r->multi_arena)
+            cudaFree(r->multi_arena);
+        r->multi_arena = nullptr;
+        r->multi_bytes = 0;
+        e = cudaMalloc(&r->multi_arena, total);
+        if (e != cudaSuccess)
+            return e == cudaErrorMemoryAllocation ? fail(ISTI_ERR_OOM, "cudaMalloc of the multi-pair arena failed") : cuda_fail(e, "cudaMalloc");
+        r->multi_bytes = total;
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if ((e = cudaStreamIsCapturing(stream, &cs)) != cudaSuccess)
+        return cuda_fail(e, "cudaStreamIsCapturing");
+    if (!r->multi_copied && (e = cudaEventCreateWithFlags(&r->multi_copied, cudaEventDisableTiming)) != cudaSuccess)
+        return cuda_fail(e, "cudaEventCreate");
+    if (cs == cudaStreamCaptureStatusNone && r->multi_host && (e = cudaEventSynchronize(r->multi_copied)) != cudaSuccess)
+        return cuda_fail(e, "waiting for the previous parameter copy");
+    if (block_bytes > r->multi_host_bytes)
+    {
+        if (r->multi_host)
+            cudaFreeHost(r->multi_host);
+        r->multi_host = nullptr;
+        r->multi_host_bytes = 0;
+        if ((e = cudaHostAlloc(&r->multi_host, block_bytes, cudaHostAllocDefault)) != cudaSuccess)
+            return cuda_fail(e, "cudaHostAlloc of the parameter staging");
+        r->multi_host_bytes = block_bytes;
+    }
+    char *dbase = static_cast<char *>(r->multi_arena);
+    char *dblock = dbase + data_bytes;
+    char *h = static_cast<char *>(r->multi_host);
+    std::memset(h, 0, block_bytes);
+    auto *hfp = reinterpret_cast<isti::FrameParams *>(h);
+    auto *hmaps = reinterpret_cast<CUtensorMap *>(h + fp_bytes);
+    auto *hpairs = reinterpret_cast<isti::BatchPair *>(h + fp_bytes + map_bytes);
+    auto *hsegs = reinterpret_cast<isti::BatchSeg *>(h + fp_bytes + map_bytes + pair_bytes);
+    const auto *dfp = reinterpret_cast<const isti::FrameParams *>(dblock);
+    const auto *dmaps = reinterpret_cast<const CUtensorMap *>(dblock + fp_bytes);
+    auto *dcnt = reinterpret_cast<uint32_t *>(dblock + fp_bytes + map_bytes + pair_bytes + seg_bytes);
+    int32_t *dstatus = reinterpret_cast<int32_t *>(dcnt + 1 + 2 * n_pairs);
+    const int sw = isti::mode_window(mode);
+    const int regs = isti::rule_regs(sw, nv);
+    const unsigned nthreads = 32u * (unsigned)nv;
+    size_t region = 0, off = 0;
+    for (int i = 0; i < n_pairs; i++)
+    {
+        const isti_pair_frames &pf = pairs[i];
+        isti::FrameParams &p = hfp[i];
+        fill_params(p, pf.n_frames, pf.out_rgba, pf.infos, pf.frame, views[i].data(), nv, layouts[i], dbase + off, pf.chain_outputs != 0);
+        off += align_up(layouts[i].total, 256);
+        p.status = dstatus;
+        p.row_pairs = isti::rule_row_pairs(nv, pf.n_frames);
+        isti::KeyMaps km;
+        p.use_tma = (sw == 1 ? pair_maps<1>(p, km) : pair_maps<3>(p, km)) ? 1 : 0;
+        std::memcpy(hmaps + (size_t)i * isti::MAX_VIEWS, km.m, sizeof(CUtensorMap) * nv);
+        const int nu = pf.n_frames * p.row_pairs;
+        const size_t reg = (sw == 1 ? isti::reproj_tile_region<1>(nv, nu) : isti::reproj_tile_region<3>(nv, nu)) +
+                           (size_t)nu * isti::ROWS * nv * 32 * sizeof(isti::DirRes);
+        region = std::max(region, align_up(reg, 16));
+        uint32_t max_w = 0, max_h = 0;
+        for (int k = 0; k < nv; k++)
+        {
+            max_w = std::max(max_w, p.v[k].w);
+            max_h = std::max(max_h, p.v[k].h);
+        }
+        isti::BatchPair &bpair = hpairs[i];
+        bpair.fp = dfp + i;
+        bpair.maps = dmaps + (size_t)i * isti::MAX_VIEWS;
+        const size_t lut_need = (std::max(max_w, max_h) + nthreads - 1) / nthreads;
+        bpair.init_units = (uint32_t)std::max<size_t>((p.key_units + isti::BATCH_INIT_UNIT_KEYS - 1) / isti::BATCH_INIT_UNIT_KEYS, lut_need);
+        bpair.splat_gx = (max_w + 31) / 32;
+        bpair.splat_gy = (max_h + isti::BATCH_SPLAT_ROWS - 1) / isti::BATCH_SPLAT_ROWS;
+        bpair.splat_units = (uint32_t)nv * bpair.splat_gx * bpair.splat_gy;
+        bpair.reproj_gx = (p.out_w + 31) / 32;
+        const uint32_t block_rows = (uint32_t)(isti::ROWS * p.row_pairs);
+        bpair.reproj_units = bpair.reproj_gx * ((p.out_h + block_rows - 1) / block_rows);
+    }
+    // the queue: I0 S0 I1 S1 R0 I2 S2 R1 ... R(n-1)
+    int ns = 0;
+    uint32_t first = 0;
+    auto seg = [&](int pair, int phase) {
+        const isti::BatchPair &bpair = hpairs[pair];
+        hsegs[ns++] = isti::BatchSeg{(uint32_t)pair, (uint32_t)phase, first};
+        first += phase == 0 ? bpair.init_units : (phase == 1 ? bpair.splat_units : bpair.reproj_units);
+    };
+    for (int i = 0; i < n_pairs; i++)
+    {
+        seg(i, 0);
+        seg(i, 1);
+        if (i > 0)
+            seg(i - 1, 2);
+    }
+    seg(n_pairs - 1, 2);
+    isti::BatchParams bp{};
+    bp.pairs = reinterpret_cast<const isti::BatchPair *>(dblock + fp_bytes + map_bytes);
+    bp.segs = reinterpret_cast<const isti::BatchSeg *>(dblock + fp_bytes + map_bytes + pair_bytes);
+    bp.n_segs = ns;
+    bp.total = first;
+    bp.ticket = dcnt;
+    bp.done = dcnt + 1;
+    bp.status = dstatus;
+    bp.spin_limit = 1u << 24; // with 128 ns sleeps: about two seconds
+    bp.region_bytes = (uint32_t)region;
+    const size_t smem = region + 32; // + TMA barrier (8 bytes) and the block's three control words
+    // counters to zero (in the staged block), then the block to the device, then the launch
+    e = cudaMemcpyAsync(dblock, h, block_bytes, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(r->multi_copied, stream);
+    if (e == cudaSuccess)
+        e = launch_pairs_mode(mode, regs, bp, smem, (unsigned)nv, stream);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "isti_render_pairs launch");
+    r->last = hfp[0];
+    r->has_frame = true;
+    return ISTI_OK;
+}
 
 // ============================ learned initialisation ============================
 

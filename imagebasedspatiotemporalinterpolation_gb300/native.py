@@ -73,6 +73,13 @@ class IstiTuning(C.Structure):
                 ("best_ms", C.c_float), ("rule_ms", C.c_float)]
 
 
+class IstiPairFrames(C.Structure):
+    _fields_ = [("frame", C.POINTER(IstiFrameData)), ("n_frames", C.c_int32), ("out_rgba", C.POINTER(C.c_void_p)),
+                ("infos", C.POINTER(IstiRenderInfo)), ("chain_outputs", C.c_int32)]
+
+
+MAX_PAIRS = 64  # ISTI_MAX_PAIRS
+
 # Every function include/isti.h declares: name -> (restype, argtypes)
 SIGNATURES = {
     "isti_abi_version": (C.c_int32, []),
@@ -95,6 +102,7 @@ SIGNATURES = {
     "isti_renderer_test_withhold_tile": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_uint32]),
     "isti_render_batch": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(IstiRenderInfo),
                                     C.POINTER(IstiFrameData), C.c_int32, C.c_void_p]),
+    "isti_render_pairs": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(IstiPairFrames), C.c_void_p]),
 }
 
 

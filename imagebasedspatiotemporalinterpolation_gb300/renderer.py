@@ -191,6 +191,29 @@ class Renderer:
         s = (stream or torch.cuda.current_stream()).cuda_stream
         check(self._lib.isti_render_batch(self._h, n, outs, ris, C.byref(frame_data.to_c()), int(chain), C.c_void_p(s)))
 
+    def render_pairs(self, jobs, chain: bool = False, stream=None) -> None:
+        """isti_render_pairs: jobs = [(render_buffers, infos, frame_data), ...], the frames of
+        several keyframe pairs in one persistent launch; each job's result equals
+        render_batch(render_buffers, infos, frame_data, chain)."""
+        torch = _torch()
+        if not 1 <= len(jobs) <= native.MAX_PAIRS:
+            raise ValueError(f"need 1..{native.MAX_PAIRS} keyframe pairs")
+        keep = []
+        arr = (native.IstiPairFrames * len(jobs))()
+        for i, (bufs, infos, fd) in enumerate(jobs):
+            n = len(infos)
+            if n != len(bufs) or not 1 <= n <= native.MAX_BATCH_FRAMES:
+                raise ValueError(f"need 1..{native.MAX_BATCH_FRAMES} frames and one buffer per frame")
+            ris = (IstiRenderInfo * n)(*[x if isinstance(x, IstiRenderInfo) else render_info(x) for x in infos])
+            outs = (C.c_void_p * n)(*[_dptr(b) for b in bufs])
+            fdc = fd.to_c()
+            keep += [ris, outs, fdc]
+            arr[i] = native.IstiPairFrames(C.pointer(fdc), n, C.cast(outs, C.POINTER(C.c_void_p)), C.cast(ris, C.POINTER(IstiRenderInfo)),
+                                           int(chain))
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        self._keep_pairs = (arr, keep)  # the structs must outlive the call
+        check(self._lib.isti_render_pairs(self._h, len(jobs), arr, C.c_void_p(s)))
+
     def render_learned(self, render_buffers, infos, frame_data: DeviceFrame, net=None, iterations: int = 1, chain: bool = False,
                        stream=None) -> None:
         """isti_render_learned: the frames of one keyframe pair (main camera only) with the

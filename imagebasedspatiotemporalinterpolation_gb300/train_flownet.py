@@ -180,10 +180,11 @@ def main() -> int:
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    ap.add_argument("--time-limit", type=float, default=None, help="stop after this many seconds (the schedule keeps --pairs)")
     args = ap.parse_args()
-    net, hist = train(args.pairs, args.batch, args.width, args.height, args.lr, args.seed)
+    net, hist = train(args.pairs, args.batch, args.width, args.height, args.lr, args.seed, time_limit_s=args.time_limit)
     save(net, args.out, {"pairs": args.pairs, "batch": args.batch, "width": args.width, "height": args.height, "lr": args.lr,
-                         "seed": args.seed, "loss_history": np.array(hist)})
+                         "seed": args.seed, "steps_run": hist[-1][0] if hist else 0, "loss_history": np.array(hist)})
     print(f"saved {args.out}")
     return 0
 

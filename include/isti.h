@@ -153,6 +153,28 @@ isti_status isti_render(isti_renderer *r, void *out_rgba, const isti_render_info
 isti_status isti_render_batch(isti_renderer *r, int32_t n_frames, void *const *out_rgba, const isti_render_info *infos,
                               const isti_frame_data *frame, int32_t chain_outputs, void *stream);
 
+/* The frames of several keyframe pairs in ONE persistent launch (no counterpart in the
+ * reference, which renders frame by frame, src/main.cu:152-190).  pairs[i] renders
+ * n_frames client frames of pairs[i].frame exactly as isti_render_batch would (same
+ * chain_outputs meaning, same bits): key initialisation, splatting and reprojection of every
+ * pair are units of one cooperative kernel that takes them from a device work queue, the
+ * next pair's initialisation and splatting ahead of the previous pair's reprojection.  All
+ * pairs share the render mode (not timewarp) and the number of source views.
+ * 1 <= n_pairs <= ISTI_MAX_PAIRS.  The kernel parameters travel through a pinned staging
+ * buffer of the renderer: a call captured into a CUDA graph reads that buffer when the graph
+ * runs, so make no other isti_render_pairs call on that renderer while the graph is in use.
+ * isti_renderer_device_status reports the call's status word. */
+#define ISTI_MAX_PAIRS 64
+typedef struct isti_pair_frames
+{
+    const isti_frame_data *frame;
+    int32_t n_frames;               /* 1..ISTI_MAX_BATCH_FRAMES */
+    void *const *out_rgba;          /* n_frames device RGBA8 buffers */
+    const isti_render_info *infos;  /* n_frames */
+    int32_t chain_outputs;
+} isti_pair_frames;
+isti_status isti_render_pairs(isti_renderer *r, int32_t n_pairs, const isti_pair_frames *pairs, void *stream);
+
 /* Device pointers to the intermediates of the last render call for view
  * `view` (0 fwd, 1 bwd, 2+2i aux i curr, 3+2i aux i next; after a batch,
  * frame k's views follow at k * (2 + 2 * num_aux)): 64-bit splat keys

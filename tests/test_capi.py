@@ -47,7 +47,8 @@ def test_struct_layout_matches_header(built, tmp_path):
     structs = {"isti_view": native.IstiView, "isti_frame_data": native.IstiFrameData,
                "isti_render_info": native.IstiRenderInfo, "isti_timing": native.IstiTiming,
                "isti_camera_info": native.IstiCameraInfo, "isti_camera_frame": native.IstiCameraFrame,
-               "isti_quality": native.IstiQuality, "isti_tuning": native.IstiTuning}
+               "isti_quality": native.IstiQuality, "isti_tuning": native.IstiTuning,
+               "isti_pair_frames": native.IstiPairFrames}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "isti.h"', '#include "isti_dataset.h"',
              '#include "isti_metrics.h"', "int main(void){"]
     for cname, cls in structs.items():

@@ -1,0 +1,87 @@
+"""isti_render_pairs: many keyframe pairs in one persistent launch.
+
+The batched workload of the benchmark list -- 16 keyframe pairs x 3 t values x 2 eyes,
+the pairs at 1280x720, 1920x1080 and 2064x2208 in turn, main camera only, no shadows,
+mode 0 -- rendered by ONE isti_render_pairs call (a cooperative kernel over a device work
+queue of key-initialisation, splat and reprojection units) must equal per-frame
+isti_render calls bit for bit, frame by frame; a smaller mixed case checks chained
+outputs, aux cameras with soft shadows and mode 1 against isti_render_batch.
+"""
+import numpy as np
+import pytest
+
+from imagebasedspatiotemporalinterpolation_gb300 import native, scene
+from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame, Renderer
+
+pytestmark = pytest.mark.gpu
+
+RES = ((1280, 720), (1920, 1080), (2064, 2208))
+EYES = (-0.032, 0.032)
+
+
+def eye_client(seq, k, b, offset, mode=0):
+    t = b / seq.fpa
+    pose = seq.poses[k].lerp(seq.poses[k + 1], t)
+    eye = pose.eye + scene.right_vector(pose.yaw, pose.pitch) * offset
+    vp = seq.proj_main @ scene.view_matrix(eye, pose.yaw, pose.pitch)
+    return scene.Client(seq.width, seq.height, float(np.float32(t)), vp.astype(np.float32), np.linalg.inv(vp).astype(np.float32),
+                        seq.fpa, seq.sfpa, False, mode)
+
+
+def test_sixteen_pairs_one_launch_equal_per_frame_calls(cuda):
+    import torch
+    jobs, per_res = [], {}
+    for j, (w, h) in enumerate(RES):
+        n = len(range(j, 16, 3))
+        per_res[(w, h)] = scene.Sequence(w, h, n + 1, seed=4100 + j)
+    counters = {r: 0 for r in RES}
+    for i in range(16):
+        w, h = RES[i % 3]
+        seq = per_res[(w, h)]
+        k = counters[(w, h)]
+        counters[(w, h)] += 1
+        clients = [eye_client(seq, k, b, e) for b in (1, 2, 3) for e in EYES]
+        frame = DeviceFrame.from_host(seq.frame(k))
+        outs = [torch.full((h, w, 4), 3, dtype=torch.uint8, device="cuda") for _ in clients]
+        jobs.append((outs, clients, frame))
+    r = Renderer()
+    r.render_pairs(jobs)
+    torch.cuda.synchronize()
+    assert r.device_status() == native.ISTI_OK
+    ref = Renderer()
+    for i, (outs, clients, frame) in enumerate(jobs):
+        for k, (o, c) in enumerate(zip(outs, clients)):
+            want = torch.full_like(o, 3)
+            ref.render(want, c, frame)
+            torch.cuda.synchronize()
+            assert torch.equal(o, want), f"pair {i} frame {k}: {int((o != want).any(-1).sum())} pixels differ"
+    r.close()
+    ref.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_mixed_pairs_chained_equal_render_batch(cuda, mode):
+    import torch
+    seqs = [scene.Sequence(320, 180, 3, seed=4200, aux_offsets=(-0.3, 0.3), shadows=True, max_speed=2.0),
+            scene.Sequence(400, 240, 3, seed=4201, aux_offsets=(-0.3, 0.3), shadows=True, max_speed=2.0)]
+    jobs, wants = [], []
+    ref = Renderer()
+    for i in range(4):
+        seq = seqs[i % 2]
+        k = i // 2
+        clients = [seq.client(k, b, mode=mode) for b in (1, 2, 3)]
+        frame = DeviceFrame.from_host(seq.frame(k))
+        prev = torch.full((seq.height, seq.width, 4), 11, dtype=torch.uint8, device="cuda")
+        want = [prev.clone() for _ in clients]
+        ref.render_batch(want, clients, frame, chain=True)
+        jobs.append(([prev.clone() for _ in clients], clients, frame))
+        wants.append(want)
+    r = Renderer()
+    r.render_pairs(jobs, chain=True)
+    torch.cuda.synchronize()
+    assert r.device_status() == native.ISTI_OK
+    for i, ((outs, _, _), want) in enumerate(zip(jobs, wants)):
+        for k, (a, b) in enumerate(zip(outs, want)):
+            assert torch.equal(a, b), f"pair {i} frame {k}: {int((a != b).any(-1).sum())} pixels differ"
+    r.close()
+    ref.close()
