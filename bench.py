@@ -71,6 +71,9 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="real time of the serving loop (the configuration's 60 s)")
     ap.add_argument("--serve-learned", type=int, default=1, help="serve with the learned initialiser when its weights exist")
     ap.add_argument("--serve-slots", type=int, default=4, help="concurrent batches (streams) of the serving loop")
+    ap.add_argument("--pressure-seconds", type=float, default=20.0,
+                    help="real time of the serving loop under pressure (more clients than the budget admits)")
+    ap.add_argument("--no-pressure", action="store_true", help="skip the serving loop under pressure")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-initialiser comparison")
     ap.add_argument("--no-config1", action="store_true", help="skip the 640x360 configuration")
     ap.add_argument("--no-reference-gpu", action="store_true", help="skip timing the reference's own GPU build")
@@ -377,6 +380,8 @@ def main_ours(args):
     serving = None
     if not args.no_serving:
         serving = run_serving(args, dev, rank)
+        if not args.no_pressure:
+            serving["pressure"] = run_serving(args, dev, rank, pressure=True)
 
     # ---- learned initialiser vs plain at 1080p, configuration 1, the reference's own GPU build
     learned = None if args.no_learned else run_learned(args, dev, rank)
@@ -650,17 +655,25 @@ GB_RES = ((1280, 720), (1920, 1080), (2064, 2208))
 GB_PAIRS = 16
 GB_EYES = (-0.032, 0.032)  # half the interpupillary distance, metres
 SV_CLIENTS = 16
+PRESSURE_CLIENTS = 256        # open sessions under pressure: more than the 120 GB budget admits
+PRESSURE_SESSION_S = 8.0      # mean session length under pressure (a closing client is replaced)
+PRESSURE_MAX_WAITING = 8      # back-pressure: waiting requests per eye before refusing
 
 
-def run_serving(args, dev, rank):
+def run_serving(args, dev, rank, pressure=False):
     """The serving workload of the benchmark list: 16 simulated clients, each sending stereo
     frame requests as a Poisson process at a rate drawn from U[90, 120] Hz and receiving a
     new keyframe pair every 1/30 s, at 1280x720 / 1920x1080 / 2064x2208 per eye in turn,
-    main camera only, no shadows, plain method; keyframes resident on the device, admission
-    against a 120 GB budget, 4 slots, batches of up to 8 frames.  Runs in real time for
+    main camera only, no shadows; keyframes resident on the device, admission against a
+    120 GB budget, 4 slots, batches of up to 8 frames.  Runs in real time for
     --serve-seconds, then drains; latency is from a request's scheduled arrival to the loop
     seeing its batch done.  Keyframe pairs are uploaded from pinned host memory as they
-    arrive (each client cycles through two pre-rendered pairs of its resolution)."""
+    arrive (each client cycles through two pre-rendered pairs of its resolution).
+
+    pressure=True: 256 open sessions of the same kind for --pressure-seconds, each ending
+    after an exponential session (mean 8 s) and replaced by a new client: more clients than
+    the budget admits (the rest wait, deferred, in arrival order) and more frames than the
+    device renders (an eye with 8 requests waiting refuses the next)."""
     import numpy as np
     import torch
 
@@ -678,7 +691,7 @@ def run_serving(args, dev, rank):
     weights = train_flownet.DEFAULT_WEIGHTS if (args.serve_learned and os.path.exists(train_flownet.DEFAULT_WEIGHTS)) else None
     backend = CudaBackend(dev, learned_weights=weights)
     server = Server(backend, hbm_budget=120 << 30, n_slots=args.serve_slots, max_batch=8,
-                    slot_pixels=max_w * max_h, slot_views=2)
+                    slot_pixels=max_w * max_h, slot_views=2, max_waiting=PRESSURE_MAX_WAITING if pressure else None)
     # every slot's renderer (and network) sized once for the largest batch (no allocation while serving)
     big_seq = seqs[(max_w, max_h)][0]
     big = DeviceFrame.from_host(big_seq.frame(0), dev)
@@ -692,22 +705,39 @@ def run_serving(args, dev, rank):
     torch.cuda.synchronize()
     del outs, big
     sims = []
-    for c in range(SV_CLIENTS):
+    n_clients = PRESSURE_CLIENTS if pressure else SV_CLIENTS
+    seconds = args.pressure_seconds if pressure else args.serve_seconds
+    for c in range(n_clients):
         w, h = GB_RES[c % len(GB_RES)]
         seq, pairs = seqs[(w, h)]
         server.open_client(c, w, h, len(GB_EYES), pairs[0])
         sims.append(SimClient(c, seq, pairs, rate_hz=float(rng.uniform(90.0, 120.0)), phase_s=float(rng.uniform(0.0, 1.0 / 30))))
-    st = simulate(server, sims, seconds=args.serve_seconds, eyes=GB_EYES, seed=args.seed + rank)
     torch.cuda.synchronize()
-    return {"mpix_per_s": round(st["mpix_per_s"], 1), "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
-            "requests": st["requests"], "offered_requests": st["offered_requests"], "refused_requests": st["refused_requests"],
-            "batches": st["batches"], "frames_per_batch": round(st["frames_per_batch"], 2), "keyframe_uploads": st["uploads"],
-            "clients": st["clients"], "admitted": st["admitted"], "seconds": args.serve_seconds,
-            "reserved_gb": round(st["peak_reserved_bytes"] / 2**30, 2), "budget_gb": 120, "slots": args.serve_slots,
-            "method": "learned initialiser (1 iteration) + per-tile plain fallback" if weights else "plain",
-            "learned_batches": backend.learned_batches, "plain_batches": backend.plain_batches,
-            "workload": "16 clients, stereo requests Poisson U[90,120] Hz, keyframe pairs 30 Hz, 1280x720 / 1920x1080 / "
-                        "2064x2208 per eye, main camera only, continuous batching"}
+    st = simulate(server, sims, seconds=seconds, eyes=GB_EYES, seed=args.seed + rank,
+                  session_mean_s=PRESSURE_SESSION_S if pressure else None,
+                  rate_hz=(lambda g: g.uniform(90.0, 120.0)) if pressure else None)
+    torch.cuda.synchronize()
+    out = {"mpix_per_s": round(st["mpix_per_s"], 1), "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+           "requests": st["requests"], "offered_requests": st["offered_requests"], "refused_requests": st["refused_requests"],
+           "batches": st["batches"], "frames_per_batch": round(st["frames_per_batch"], 2), "keyframe_uploads": st["uploads"],
+           "clients": st["clients"], "admitted": st["admitted"], "seconds": seconds,
+           "reserved_gb": round(st["peak_reserved_bytes"] / 2**30, 2), "budget_gb": 120, "slots": args.serve_slots,
+           "method": "learned initialiser (1 iteration) + per-tile plain fallback" if weights else "plain",
+           "learned_batches": backend.learned_batches, "plain_batches": backend.plain_batches,
+           "workload": f"{n_clients} clients, stereo requests Poisson U[90,120] Hz, keyframe pairs 30 Hz, 1280x720 / 1920x1080 / "
+                       "2064x2208 per eye, main camera only, continuous batching"}
+    if pressure:
+        out.update({"refused_not_admitted": st["refused_not_admitted"], "refused_queue_full": st["refused_queue_full"],
+                    "max_waiting_per_eye": PRESSURE_MAX_WAITING, "sessions_closed": st["sessions_closed"],
+                    "clients_opened": st["clients_opened"], "deferred_clients": st["deferred_clients"],
+                    "peak_waiting_clients": st["peak_waiting_clients"],
+                    "admission_wait_p50_ms": round(st["admission_wait_p50_ms"], 1),
+                    "admission_wait_p99_ms": round(st["admission_wait_p99_ms"], 1),
+                    "session_mean_s": PRESSURE_SESSION_S})
+    del server, backend
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_graph_batch(args, dev, rank):

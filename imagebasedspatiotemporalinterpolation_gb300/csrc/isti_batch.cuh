@@ -49,7 +49,16 @@ struct BatchParams
     int32_t *status;
     uint32_t spin_limit;
     uint32_t region_bytes;     // reprojection shared memory of the largest pair; the barrier follows
+    uint32_t param_bytes;      // params_prefix(n_views): the staged part of a pair's FrameParams
 };
+
+// Shared memory of a batch_kernel block: [the current pair's FrameParams prefix, padded to
+// batch_param_space][reprojection region][TMA barrier][control words][the current BatchPair].
+// The parameters sit at offset 0, so their fields are read at constant shared addresses.
+constexpr size_t BATCH_CTRL_BYTES = 8 + 32 + 48; // barrier, 8 control words, the current BatchPair
+__host__ __device__ constexpr size_t batch_param_space(size_t param_bytes) { return (param_bytes + 1023) & ~(size_t)1023; }
+static_assert(sizeof(FrameParams) % 16 == 0, "FrameParams is staged in 16-byte words");
+static_assert(sizeof(BatchPair) <= 48, "BatchPair is staged in 48 bytes");
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p)
 {
@@ -62,41 +71,76 @@ template <int SW, int SI, bool MAV, int REGS>
 __global__ void __maxnreg__(REGS) batch_kernel(const __grid_constant__ BatchParams bp)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned long long &bar = *reinterpret_cast<unsigned long long *>(smem + bp.region_bytes);
-    uint32_t *ctrl = reinterpret_cast<uint32_t *>(smem + bp.region_bytes + 8); // [ticket, dependency satisfied, status]
+    // the pair's kernel parameters, copied from global memory whenever the block moves to
+    // another pair: read from shared memory like the per-call kernels read their constant bank
+    uint4 *staged = reinterpret_cast<uint4 *>(smem);
+    const FrameParams &p = *reinterpret_cast<const FrameParams *>(smem);
+    unsigned char *region = smem + batch_param_space(bp.param_bytes);
+    unsigned long long &bar = *reinterpret_cast<unsigned long long *>(region + bp.region_bytes);
+    // [0, 1] ticket of the current / next unit (alternating), [2] status seen, [3] dependency met
+    uint32_t *ctrl = reinterpret_cast<uint32_t *>(region + bp.region_bytes + 8);
+    BatchPair &bpair = *reinterpret_cast<BatchPair *>(region + bp.region_bytes + 8 + 32);
     const uint32_t tid = threadIdx.y * blockDim.x + threadIdx.x, nthreads = blockDim.x * blockDim.y;
     if (tid == 0)
+    {
         mbar_init(&bar, 1);
+        ctrl[0] = atomicAdd(bp.ticket, 1u);
+        ctrl[2] = 0u;
+    }
     __syncthreads();
-    int round = 0; // TMA rounds of this block's barrier (its phase carries across units)
+    int round = 0;        // TMA rounds of this block's barrier (its phase carries across units)
+    uint32_t slot = 0;    // ctrl word holding the current ticket
+    // the segment of the current ticket; a block's tickets only grow, so the search resumes
+    // where the previous unit's ended
+    int si = -1;
+    uint32_t seg_first = 0, seg_end = 0, seg_pair = 0xffffffffu, seg_phase = 0;
+    uint32_t met_pair = 0xffffffffu, met_phase = 0; // the last dependency found satisfied
     for (;;)
     {
-        if (tid == 0)
-        {
-            ctrl[0] = atomicAdd(bp.ticket, 1u);
-            ctrl[2] = (uint32_t)*(volatile int32_t *)bp.status;
-        }
-        __syncthreads();
-        const uint32_t t = ctrl[0];
+        const uint32_t t = ctrl[slot];
         if (t >= bp.total)
             break;
+        // the next ticket and the status word are fetched while this unit runs, by the block's
+        // last thread (not the TMA leader, tid 0, whose fences would wait for the atomic); it
+        // waits for them only when it publishes them after the unit
+        const bool helper = tid == nthreads - 1;
+        uint32_t next_t = 0;
+        int32_t status_seen = 0;
+        if (helper)
+        {
+            next_t = atomicAdd(bp.ticket, 1u);
+            status_seen = *(volatile int32_t *)bp.status;
+        }
         // once a wait has given up (status word set) the remaining units only count themselves
         // done: the failed block's TMA barrier is out of step, and the call's outputs are void
         const bool failed = ctrl[2] != 0;
-        int si = 0;
-        while (si + 1 < bp.n_segs && bp.segs[si + 1].first <= t)
+        const uint32_t old_pair = seg_pair;
+        while (t >= seg_end)
+        {
             si++;
-        const BatchSeg sg = bp.segs[si];
-        const BatchPair &bpair = bp.pairs[sg.pair];
-        const FrameParams &p = *bpair.fp;
-        const uint32_t u = t - sg.first;
+            const BatchSeg sg = bp.segs[si];
+            seg_first = sg.first;
+            seg_pair = sg.pair;
+            seg_phase = sg.phase;
+            seg_end = si + 1 < bp.n_segs ? bp.segs[si + 1].first : bp.total;
+        }
+        if (seg_pair != old_pair) // block-uniform; every thread is past the previous unit (barrier below)
+        {
+            const uint4 *src = reinterpret_cast<const uint4 *>(bp.pairs[seg_pair].fp);
+            for (uint32_t i = tid; i < bp.param_bytes / 16; i += nthreads)
+                staged[i] = src[i];
+            if (tid == 0)
+                bpair = bp.pairs[seg_pair];
+            __syncthreads();
+        }
+        const uint32_t u = t - seg_first;
         bool run = !failed;
-        if (run && sg.phase > 0)
+        if (run && seg_phase > 0 && !(met_pair == seg_pair && met_phase == seg_phase))
         {
             if (tid == 0)
             {
-                const uint32_t need = sg.phase == 1 ? bpair.init_units : bpair.splat_units;
-                const uint32_t *cnt = bp.done + 2 * sg.pair + (sg.phase - 1);
+                const uint32_t need = seg_phase == 1 ? bpair.init_units : bpair.splat_units;
+                const uint32_t *cnt = bp.done + 2 * seg_pair + (seg_phase - 1);
                 uint32_t ok = 0;
                 for (uint32_t i = 0; i < bp.spin_limit; i++)
                 {
@@ -111,16 +155,21 @@ __global__ void __maxnreg__(REGS) batch_kernel(const __grid_constant__ BatchPara
                     atomicExch(bp.status, (int32_t)ISTI_ERR_TIMEOUT);
                 __threadfence();
                 asm volatile("fence.proxy.async.global;" ::: "memory"); // key tiles are read by TMA
-                ctrl[1] = ok;
+                ctrl[3] = ok;
             }
             __syncthreads();
-            run = ctrl[1] != 0;
+            run = ctrl[3] != 0;
+            if (run)
+            {
+                met_pair = seg_pair;
+                met_phase = seg_phase;
+            }
         }
         if (run)
         {
-            if (sg.phase == 0)
+            if (seg_phase == 0)
                 init_part(p, (size_t)u * nthreads + tid, (size_t)bpair.init_units * nthreads, false); // the call's status word is reset by the host
-            else if (sg.phase == 1)
+            else if (seg_phase == 1)
             {
                 const uint32_t per_view = bpair.splat_gx * bpair.splat_gy;
                 const int view = (int)(u / per_view);
@@ -133,13 +182,20 @@ __global__ void __maxnreg__(REGS) batch_kernel(const __grid_constant__ BatchPara
             else
             {
                 const uint32_t bx = u % bpair.reproj_gx, by = u / bpair.reproj_gx;
-                reproj_block<SW, SI, MAV, REGS>(p, bpair.maps, bx, by, u, smem, bar, round);
+                reproj_block<SW, SI, MAV, REGS>(p, bpair.maps, bx, by, u, region, bar, round);
             }
         }
         __threadfence();
         __syncthreads();
-        if (tid == 0 && sg.phase < 2)
-            atomicAdd(bp.done + 2 * sg.pair + sg.phase, 1u);
+        if (helper)
+        {
+            if (seg_phase < 2)
+                atomicAdd(bp.done + 2 * seg_pair + seg_phase, 1u);
+            ctrl[slot ^ 1u] = next_t;
+            ctrl[2] = (uint32_t)status_seen;
+        }
+        __syncthreads();
+        slot ^= 1u;
     }
 }
 } // namespace isti

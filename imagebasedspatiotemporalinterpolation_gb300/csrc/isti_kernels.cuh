@@ -34,6 +34,8 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <cstddef>
+
 #include <utility>
 
 namespace isti
@@ -82,9 +84,10 @@ struct FrameCfg
     int32_t fpa, sfpa, no_shadows;
 };
 
+// The views come last: a copy of the first params_prefix(n) bytes holds every field a
+// launch over n views reads (the persistent kernel stages that much in shared memory).
 struct FrameParams
 {
-    DevView v[MAX_VIEWS];
     float cam_vp[MAX_FRAMES][16];
     float cam_ivp[MAX_FRAMES][16]; // client inverse viewproj (timewarp rays)
     double *tw_rows;               // timewarp: per-row sums of the forward keyframe's z
@@ -107,7 +110,13 @@ struct FrameParams
     int32_t withhold_block;
     uint32_t wait_limit;
     int32_t withhold_x, withhold_y;
+    DevView v[MAX_VIEWS];
 };
+
+__host__ __device__ constexpr size_t params_prefix(int n_views)
+{
+    return (offsetof(FrameParams, v) + (size_t)n_views * sizeof(DevView) + 15) & ~(size_t)15;
+}
 
 // One 3-D tensor map per source view over its splat keys: (x, y, frame), u64 elements.
 struct KeyMaps

@@ -877,7 +877,8 @@ extern "C" isti_status isti_render_pairs(isti_renderer *r, int32_t n_pairs, cons
     bp.status = dstatus;
     bp.spin_limit = 1u << 24; // with 128 ns sleeps: about two seconds
     bp.region_bytes = (uint32_t)region;
-    const size_t smem = region + 32; // + TMA barrier (8 bytes) and the block's three control words
+    bp.param_bytes = (uint32_t)isti::params_prefix(nv);
+    const size_t smem = isti::batch_param_space(bp.param_bytes) + region + isti::BATCH_CTRL_BYTES;
     // counters to zero (in the staged block), then the block to the device, then the launch
     e = cudaMemcpyAsync(dblock, h, block_bytes, cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess)

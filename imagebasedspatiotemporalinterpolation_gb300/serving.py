@@ -16,8 +16,10 @@ many clients at once:
 
 Admission: a client is admitted when its device footprint (two keyframe pairs and the
 output rings of its eyes) fits into the budget beside the clients already admitted and
-the slots' renderer arenas; otherwise it waits until clients close.  A request waits
-while its eye has no free output buffer.
+the slots' renderer arenas; otherwise it waits (deferred, in arrival order) until clients
+close.  A request waits while its eye has no free output buffer.  Back-pressure: with
+`max_waiting`, a request is refused when its eye already has that many requests waiting
+(the device is behind; the client renders that frame itself or drops it).
 
 Continuous batching: whenever a slot is free, the eye with the oldest waiting request
 (among eyes with no batch in flight whose pair is uploaded) takes it; up to `max_batch`
@@ -131,7 +133,7 @@ class Server:
 
     def __init__(self, backend, hbm_budget: int, n_slots: int = 4, max_batch: int = 8, out_ring: int | None = None,
                  slot_pixels: int = 2064 * 2208, slot_views: int = 2, clock=time.perf_counter, on_complete=None,
-                 multi_eye: bool = True):
+                 multi_eye: bool = True, max_waiting: int | None = None):
         if n_slots < 1 or not 1 <= max_batch <= backend.max_batch:
             raise ValueError(f"need n_slots >= 1 and 1 <= max_batch <= {backend.max_batch}")
         self.be = backend
@@ -143,6 +145,16 @@ class Server:
         self.clock = clock
         self.on_complete = on_complete
         self.multi_eye = multi_eye
+        if max_waiting is not None and max_waiting < 1:
+            raise ValueError("max_waiting must be at least 1")
+        self.max_waiting = max_waiting
+        self.refused_full = 0            # requests refused by back-pressure (max_waiting)
+        self.deferred = 0                # clients that had to wait for budget when they opened
+        self.admission_waits: list = []  # seconds from open_client to admission, deferred clients
+        self.peak_waiting_clients = 0
+        self.clients_opened = 0
+        self._opened_at: dict[int, float] = {}
+        self._deferred_cids: set = set()
         self.slot_bytes = backend.slot_bytes(slot_pixels, slot_views, max_batch)
         self.reserved = n_slots * self.slot_bytes
         if self.reserved > self.budget:
@@ -179,8 +191,15 @@ class Server:
             raise ValueError(f"client {cid} needs {need} bytes, more than the budget leaves beside the slots")
         self.admit_queue.append((cid, width, height, n_eyes, template, need))
         self.waiting_pairs.setdefault(cid, collections.deque())
+        self.clients_opened += 1
+        self._opened_at[cid] = self.clock()
         self._admit()
-        return cid in self.clients
+        if cid not in self.clients:
+            self.deferred += 1
+            self._deferred_cids.add(cid)
+            self.peak_waiting_clients = max(self.peak_waiting_clients, len(self.admit_queue))
+            return False
+        return True
 
     def admitted(self, cid: int) -> bool:
         return cid in self.clients
@@ -196,6 +215,8 @@ class Server:
         else:
             self.admit_queue = collections.deque(q for q in self.admit_queue if q[0] != cid)
             self.waiting_pairs.pop(cid, None)
+            self._opened_at.pop(cid, None)
+            self._deferred_cids.discard(cid)
 
     def _admit(self) -> int:
         n = 0
@@ -211,7 +232,13 @@ class Server:
             self.clients[cid] = c
             self.reserved += need
             self.peak_reserved = max(self.peak_reserved, self.reserved)
+            t_open = self._opened_at.pop(cid, None)
+            if cid in self._deferred_cids:
+                self._deferred_cids.discard(cid)
+                self.admission_waits.append(self.clock() - t_open)
             n += 1
+        if n and hasattr(self.be, "settle"):
+            self.be.settle()       # the new clients' buffers are initialised before any batch uses them
         return n
 
     def _release(self, c: _Client) -> None:
@@ -240,9 +267,10 @@ class Server:
             q.popleft()
         return seq
 
-    def submit(self, cid: int, eye: int, info, pixels: int = 0, t_submit: float | None = None) -> Request:
+    def submit(self, cid: int, eye: int, info, pixels: int = 0, t_submit: float | None = None) -> Request | None:
         """Queues one eye's frame in the client's newest pair.  Its latency runs from
-        t_submit (the server clock; default now)."""
+        t_submit (the server clock; default now).  None: refused by back-pressure (the eye
+        already has max_waiting requests waiting)."""
         c = self.clients.get(cid)
         if c is None:
             raise KeyError(f"client {cid} is not admitted")
@@ -252,6 +280,9 @@ class Server:
             raise ValueError(f"client {cid} has no keyframe pair yet")
         if not 0 <= eye < len(c.eyes):
             raise ValueError(f"client {cid} has {len(c.eyes)} eyes")
+        if self.max_waiting is not None and len(c.eyes[eye].waiting) >= self.max_waiting:
+            self.refused_full += 1
+            return None
         now = self.clock() if t_submit is None else t_submit
         self._rid += 1
         r = Request(cid, eye, info, c.newest, self._rid, pixels or c.width * c.height, now)
@@ -424,7 +455,11 @@ class Server:
                 "uploads": self.uploads, "p50_ms": percentile(self.latencies, 50), "p99_ms": percentile(self.latencies, 99),
                 "mpix_per_s": self.pixels_done / span / 1e6 if span > 0 else 0.0, "span_s": span,
                 "admitted": len(self.clients), "waiting_clients": len(self.admit_queue),
-                "reserved_bytes": self.reserved, "peak_reserved_bytes": self.peak_reserved, "budget_bytes": self.budget}
+                "reserved_bytes": self.reserved, "peak_reserved_bytes": self.peak_reserved, "budget_bytes": self.budget,
+                "refused_queue_full": self.refused_full, "clients_opened": self.clients_opened,
+                "deferred_clients": self.deferred, "peak_waiting_clients": self.peak_waiting_clients,
+                "admission_wait_p50_ms": percentile([w * 1e3 for w in self.admission_waits], 50),
+                "admission_wait_p99_ms": percentile([w * 1e3 for w in self.admission_waits], 99)}
 
 
 # ------------------------------------------------------------------ CUDA backend
@@ -510,6 +545,11 @@ class CudaBackend:
     def alloc_output(self, width: int, height: int):
         return self.torch.zeros((height, width, 4), dtype=self.torch.uint8, device=self.device)
 
+    def settle(self) -> None:
+        """Waits for the zero fills of newly allocated outputs (issued on the current stream,
+        which the slot streams do not order against)."""
+        self.torch.cuda.current_stream(self.device).synchronize()
+
     def _wait(self, stream, events) -> None:
         for ev in events:
             if ev is not None:
@@ -575,6 +615,7 @@ class SimClient:
     pairs: list               # PinnedPair per pair index of seq
     rate_hz: float
     phase_s: float
+    closed: bool = False
 
 
 _INFO_STEPS = 32   # client cameras are taken at alpha quantised to 1/32 (cached)
@@ -598,22 +639,37 @@ def eye_info(seq, k: int, alpha: float, offset: float, mode: int = 0):
 
 
 def simulate(server: Server, sims: list, seconds: float, keyframe_hz: float = 30.0, eyes=(-0.032, 0.032),
-             seed: int = 0) -> dict:
+             seed: int = 0, session_mean_s: float | None = None, rate_hz=None, make_info=None) -> dict:
     """Runs the clients against the server in real time for `seconds`, then drains.
-    Latency runs from a request's scheduled arrival to the loop seeing its batch done."""
+    Latency runs from a request's scheduled arrival to the loop seeing its batch done.
+
+    session_mean_s: every client leaves after an exponentially distributed session of this
+    mean and a new client (next free id, same scene and resolution, request rate drawn by
+    `rate_hz(rng)`) opens in its place, admitted when the budget allows.  The clients must
+    have been opened on the server by the caller.  make_info(sim, pair index, alpha, eye
+    index, eye offset) gives a request's render info (default: eye_info of the sim's scene)."""
     import heapq
     rng = np.random.default_rng(seed)
     heap, order = [], 0
-    for s in sims:
-        heap.append((s.phase_s, order, "kf", s))
-        heap.append((s.phase_s + rng.exponential(1.0 / s.rate_hz), order + 1, "req", s))
+    next_cid = max((s.cid for s in sims), default=-1) + 1
+
+    def schedule(s, t_start):
+        nonlocal order
+        heap.append((t_start + s.phase_s, order, "kf", s))
+        heap.append((t_start + s.phase_s + rng.exponential(1.0 / s.rate_hz), order + 1, "req", s))
         order += 2
+        if session_mean_s is not None:
+            heap.append((t_start + rng.exponential(session_mean_s), order, "end", s))
+            order += 1
+
+    for s in sims:
+        schedule(s, 0.0)
     heapq.heapify(heap)
     kf_count = {s.cid: 0 for s in sims}
     kf_time = {s.cid: 0.0 for s in sims}
     pair_of = {s.cid: 0 for s in sims}
     infos = {}
-    offered = refused = 0
+    offered = refused = closed = 0
     t0 = server.clock()
     while True:
         now = server.clock() - t0
@@ -621,7 +677,22 @@ def simulate(server: Server, sims: list, seconds: float, keyframe_hz: float = 30
             break
         while heap and heap[0][0] <= now:
             t, _, kind, s = heapq.heappop(heap)
-            if kind == "kf":
+            if s.closed:
+                continue
+            if kind == "end":
+                server.close_client(s.cid)
+                s.closed = True
+                closed += 1
+                n = SimClient(next_cid, s.seq, s.pairs, rate_hz=float(rate_hz(rng)) if rate_hz else s.rate_hz,
+                              phase_s=float(rng.uniform(0.0, 1.0 / keyframe_hz)))
+                next_cid += 1
+                server.open_client(n.cid, n.seq.width, n.seq.height, len(eyes), n.pairs[0])
+                kf_count[n.cid], kf_time[n.cid], pair_of[n.cid] = 0, 0.0, 0
+                for ev in ((t + n.phase_s, "kf"), (t + n.phase_s + rng.exponential(1.0 / n.rate_hz), "req"),
+                           (t + rng.exponential(session_mean_s), "end")):
+                    heapq.heappush(heap, (ev[0], order, ev[1], n))
+                    order += 1
+            elif kind == "kf":
                 p = kf_count[s.cid] % len(s.pairs)
                 server.push_pair(s.cid, s.pairs[p])
                 pair_of[s.cid], kf_time[s.cid] = p, t
@@ -632,10 +703,14 @@ def simulate(server: Server, sims: list, seconds: float, keyframe_hz: float = 30
                 if server.admitted(s.cid) and kf_count[s.cid] > 0:
                     q = min(_INFO_STEPS, int((t - kf_time[s.cid]) * keyframe_hz * _INFO_STEPS))
                     for e, off in enumerate(eyes):
-                        key = (id(s.seq), pair_of[s.cid], q, e)
-                        if key not in infos:
-                            infos[key] = eye_info(s.seq, pair_of[s.cid], q / _INFO_STEPS, off)
-                        server.submit(s.cid, e, infos[key], t_submit=t0 + t)
+                        if make_info is not None:
+                            info = make_info(s, pair_of[s.cid], q / _INFO_STEPS, e, off)
+                        else:
+                            key = (id(s.seq), pair_of[s.cid], q, e)
+                            if key not in infos:
+                                infos[key] = eye_info(s.seq, pair_of[s.cid], q / _INFO_STEPS, off)
+                            info = infos[key]
+                        server.submit(s.cid, e, info, t_submit=t0 + t)
                 else:
                     refused += len(eyes)
                 heapq.heappush(heap, (t + rng.exponential(1.0 / s.rate_hz), order, "req", s))
@@ -643,6 +718,8 @@ def simulate(server: Server, sims: list, seconds: float, keyframe_hz: float = 30
         server.step()
     server.drain()
     st = server.stats()
-    st.update({"offered_requests": offered, "refused_requests": refused, "seconds": seconds, "clients": len(sims),
+    st.update({"offered_requests": offered, "refused_requests": refused, "refused_not_admitted": refused,
+               "seconds": seconds, "clients": len(sims), "sessions_closed": closed,
                "keyframe_pairs_pushed": sum(kf_count.values())})
+    st["refused_requests"] = refused + st["refused_queue_full"]
     return st

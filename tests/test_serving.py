@@ -247,8 +247,6 @@ def test_admission_waits_for_budget_and_follows_closing_clients():
     be = FakeBackend(rng)
     slot = FakeBackend.slot_bytes(64 * 36, 2, 2)
     pair = Pair(5000)
-    server = Server(be, hbm_budget=0, n_slots=1, max_batch=2, slot_pixels=64 * 36, clock=Clock()) \
-        if False else None
     need = 2 * 5000 + 2 * 5 * 64 * 36 * 4
     server = Server(be, hbm_budget=slot + need + need // 2, n_slots=1, max_batch=2, slot_pixels=64 * 36, clock=Clock())
     assert server.open_client(0, 64, 36, 2, pair)
@@ -375,3 +373,64 @@ def test_keyframe_missing_at_request_time():
     be.max_advance = 3
     server.drain(timeout_s=5.0)
     assert results[r.rid] == fold(0, 1, 21)
+
+
+def test_back_pressure_refuses_requests_beyond_max_waiting():
+    """With max_waiting = 2 an eye holds at most two waiting requests; further submits are
+    refused (None) and counted, and the accepted ones still equal sequential renders."""
+    rng = random.Random(11)
+    be = FakeBackend(rng, max_advance=2)          # nothing runs before the loop steps
+    results = {}
+    server = Server(be, hbm_budget=10**12, n_slots=1, max_batch=2, slot_pixels=64 * 36, clock=Clock(),
+                    on_complete=lambda r: results.__setitem__(r.rid, r.out.v), max_waiting=2)
+    assert server.open_client(0, 64, 36, 1, Pair(1000))
+    server.push_pair(0, HostPair(5))
+    got = [server.submit(0, 0, (v, (0, 0), 5)) for v in range(5)]
+    assert [r is not None for r in got] == [True, True, False, False, False]
+    assert server.stats()["refused_queue_full"] == 3
+    server.drain(timeout_s=5.0)
+    prev = 0
+    for r, v in zip(got[:2], range(2)):
+        prev = fold(prev, v, 5)
+        assert results[r.rid] == prev
+    # once the queue has drained the eye accepts requests again
+    assert server.submit(0, 0, (9, (0, 0), 5)) is not None
+    server.drain(timeout_s=5.0)
+
+
+class FakeSeq:
+    def __init__(self, w, h):
+        self.width, self.height = w, h
+
+
+def test_sessions_defer_admission_and_every_accepted_request_completes():
+    """Client churn under a budget that admits only some clients at a time: clients leave
+    after their sessions and replacements open; the ones that do not fit wait (deferred)
+    and are admitted as others close.  Every request accepted from an admitted client is
+    rendered; requests of waiting clients and beyond max_waiting are refused."""
+    from imagebasedspatiotemporalinterpolation_gb300.serving import SimClient, simulate
+    rng = random.Random(4)
+    be = FakeBackend(rng, max_advance=2)
+    slot = FakeBackend.slot_bytes(64 * 36, 2, 2)
+    need = 2 * 1000 + 2 * 5 * 64 * 36 * 4
+    server = Server(be, hbm_budget=slot + 3 * need, n_slots=1, max_batch=2, slot_pixels=64 * 36, clock=Clock(),
+                    max_waiting=2)
+    seq = FakeSeq(64, 36)
+    pairs = [HostPair(11), HostPair(12)]
+    sims = [SimClient(c, seq, pairs, rate_hz=400.0, phase_s=0.0) for c in range(6)]
+    for s in sims:
+        server.open_client(s.cid, 64, 36, 2, pairs[0])
+    assert server.stats()["admitted"] == 3 and server.stats()["waiting_clients"] == 3
+
+    def make_info(sim, p, alpha, e, off):
+        return (int(alpha * 32), (sim.cid, e), sim.pairs[p].content)
+
+    st = simulate(server, sims, seconds=0.6, keyframe_hz=30.0, eyes=(-0.03, 0.03), seed=3, session_mean_s=0.1,
+                  rate_hz=lambda g: 400.0, make_info=make_info)
+    assert st["sessions_closed"] > 3
+    assert st["clients_opened"] == 6 + st["sessions_closed"]
+    assert st["deferred_clients"] >= 3
+    assert st["admission_wait_p50_ms"] > 0.0
+    assert st["refused_not_admitted"] > 0
+    assert st["peak_reserved_bytes"] <= server.budget
+    assert st["requests"] == st["offered_requests"] - st["refused_requests"]
