@@ -77,7 +77,10 @@ __global__ void __maxnreg__(REGS) batch_kernel(const __grid_constant__ BatchPara
     const FrameParams &p = *reinterpret_cast<const FrameParams *>(smem);
     unsigned char *region = smem + batch_param_space(bp.param_bytes);
     unsigned long long &bar = *reinterpret_cast<unsigned long long *>(region + bp.region_bytes);
-    // [0, 1] ticket of the current / next unit (alternating), [2] status seen, [3] dependency met
+    // [0, 1] ticket of the current / next unit and [2, 3] the status word seen for it (both
+    // alternating: the entry for the next unit is written before the barrier that ends this
+    // one, while some threads may not have read this unit's entry yet), [4] dependency met,
+    // [5] a reprojection unit's wait for its key tiles gave up (reproj_block's `aborted`)
     uint32_t *ctrl = reinterpret_cast<uint32_t *>(region + bp.region_bytes + 8);
     BatchPair &bpair = *reinterpret_cast<BatchPair *>(region + bp.region_bytes + 8 + 32);
     const uint32_t tid = threadIdx.y * blockDim.x + threadIdx.x, nthreads = blockDim.x * blockDim.y;
@@ -86,6 +89,7 @@ __global__ void __maxnreg__(REGS) batch_kernel(const __grid_constant__ BatchPara
         mbar_init(&bar, 1);
         ctrl[0] = atomicAdd(bp.ticket, 1u);
         ctrl[2] = 0u;
+        ctrl[5] = 0u;
     }
     __syncthreads();
     int round = 0;        // TMA rounds of this block's barrier (its phase carries across units)
@@ -113,7 +117,7 @@ __global__ void __maxnreg__(REGS) batch_kernel(const __grid_constant__ BatchPara
         }
         // once a wait has given up (status word set) the remaining units only count themselves
         // done: the failed block's TMA barrier is out of step, and the call's outputs are void
-        const bool failed = ctrl[2] != 0;
+        const bool failed = ctrl[2 + slot] != 0;
         const uint32_t old_pair = seg_pair;
         while (t >= seg_end)
         {
@@ -155,10 +159,10 @@ __global__ void __maxnreg__(REGS) batch_kernel(const __grid_constant__ BatchPara
                     atomicExch(bp.status, (int32_t)ISTI_ERR_TIMEOUT);
                 __threadfence();
                 asm volatile("fence.proxy.async.global;" ::: "memory"); // key tiles are read by TMA
-                ctrl[3] = ok;
+                ctrl[4] = ok;
             }
             __syncthreads();
-            run = ctrl[3] != 0;
+            run = ctrl[4] != 0;
             if (run)
             {
                 met_pair = seg_pair;
@@ -182,19 +186,23 @@ __global__ void __maxnreg__(REGS) batch_kernel(const __grid_constant__ BatchPara
             else
             {
                 const uint32_t bx = u % bpair.reproj_gx, by = u / bpair.reproj_gx;
-                reproj_block<SW, SI, MAV, REGS>(p, bpair.maps, bx, by, u, region, bar, round);
+                reproj_block<SW, SI, MAV, REGS>(p, bpair.maps, bx, by, u, region, bar, round, *reinterpret_cast<volatile uint32_t *>(ctrl + 5));
             }
         }
-        __threadfence();
-        __syncthreads();
         if (helper)
         {
-            if (seg_phase < 2)
-                atomicAdd(bp.done + 2 * seg_pair + seg_phase, 1u);
-            ctrl[slot ^ 1u] = next_t;
-            ctrl[2] = (uint32_t)status_seen;
+            ctrl[slot ^ 1u] = next_t; // every thread read both entries before the previous barrier
+            ctrl[2 + (slot ^ 1u)] = (uint32_t)status_seen;
         }
         __syncthreads();
+        // the unit's writes (every thread's, ordered by the barrier) are published by one
+        // release: a fence and the counter increment, as a grid-wide barrier does; a
+        // reprojection unit's outputs are read by no other unit
+        if (helper && seg_phase < 2)
+        {
+            __threadfence();
+            atomicAdd(bp.done + 2 * seg_pair + seg_phase, 1u);
+        }
         slot ^= 1u;
     }
 }

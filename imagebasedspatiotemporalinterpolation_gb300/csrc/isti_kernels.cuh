@@ -62,7 +62,12 @@ struct DevView
     const void *motion;
     const uint32_t *sha, *shb, *shi;
     unsigned long long *splat; // frame 0; frame k at + k * FrameParams::key_stride
-    float4 *cam_ff;            // frame 0; frame k at + k * FrameParams::cam_stride
+    // The client-camera flow of each source pixel (full_motion_cam, src/renderer.cu:117), split
+    // by use: (x, y), read at every search step, and the depth the reprojection derives from
+    // its z, z_to_depth(z + dz) (src/renderer.cu:339), read once after the search.
+    float2 *cam_xy;            // frame 0; frame k at + k * FrameParams::cam_stride
+    float *cam_depth;          // frame 0; frame k at + k * FrameParams::depth_stride
+    uint8_t *vis;              // visible_in_main per source pixel (the flow's w), shared by the frames
     float4 *full_ff;
     float *lut;                // pixel2CS tables: x at [0, w), y at [w, w + h)
     uint32_t w, h;
@@ -85,8 +90,9 @@ struct FrameCfg
 };
 
 // The views come last: a copy of the first params_prefix(n) bytes holds every field a
-// launch over n views reads (the persistent kernel stages that much in shared memory).
-struct FrameParams
+// launch over n views reads (the persistent kernel stages that much in shared memory, in
+// 16-byte words).
+struct alignas(16) FrameParams
 {
     float cam_vp[MAX_FRAMES][16];
     float cam_ivp[MAX_FRAMES][16]; // client inverse viewproj (timewarp rays)
@@ -95,7 +101,8 @@ struct FrameParams
     uint32_t *out[MAX_FRAMES];
     FrameCfg f[MAX_FRAMES];
     size_t key_stride; // elements between frames in the key block
-    size_t cam_stride; // elements between frames in the cam-flow block
+    size_t cam_stride;   // float2 elements between frames in the cam-flow (x, y) block
+    size_t depth_stride; // float elements between frames in the cam-flow depth block
     ulonglong2 *keys;  // the whole key block (16-byte units) for the init kernel
     size_t key_units;
     int32_t *status;   // device status word: 0 ok, ISTI_ERR_TIMEOUT after a bounded wait gave up
@@ -269,6 +276,7 @@ __device__ __forceinline__ void splat_pixel(const FrameParams &p, int view, uint
     const float4 cs_to = project(v.vp_to, ws_to);
     const float fmx = xsub(cs_to.x, cs_from.x), fmy = xsub(cs_to.y, cs_from.y), fmz = xsub(cs_to.z, cs_from.z);
     v.full_ff[idx] = make_float4(fmx, fmy, fmz, vis);
+    v.vis[idx] = visible ? 1u : 0u;
     const float4 d_ws = make_float4(xsub(ws_to.x, ws_from.x), xsub(ws_to.y, ws_from.y), xsub(ws_to.z, ws_from.z),
                                     xsub(ws_to.w, ws_from.w));
 
@@ -283,13 +291,17 @@ __device__ __forceinline__ void splat_pixel(const FrameParams &p, int view, uint
             break;
         const float wg = v.forward ? p.f[k].alpha : xsub(1.0f, p.f[k].alpha);
         unsigned long long *keys = v.splat + k * p.key_stride;
-        float4 *cam = v.cam_ff + k * p.cam_stride;
+        float2 *cam = v.cam_xy + k * p.cam_stride;
+        float *cdep = v.cam_depth + k * p.depth_stride;
         if (!p.linear)
         {
             const float4 scaled = make_float4(xadd(ws_from.x, xmul(wg, d_ws.x)), xadd(ws_from.y, xmul(wg, d_ws.y)),
                                               xadd(ws_from.z, xmul(wg, d_ws.z)), xadd(ws_from.w, xmul(wg, d_ws.w)));
             const float4 pc = project(p.cam_vp[k], scaled);
-            cam[idx] = make_float4(xsub(pc.x, cs_from.x), xsub(pc.y, cs_from.y), xsub(pc.z, cs_from.z), vis);
+            cam[idx] = make_float2(xsub(pc.x, cs_from.x), xsub(pc.y, cs_from.y));
+            // the reprojection's depth at this source pixel: its z plus the flow's dz, rounded
+            // as the reference rounds them (the stored dz, then the sum)
+            cdep[idx] = z_to_depth(xadd(z_from, xsub(pc.z, cs_from.z)));
             const float depth_cam = z_to_depth(pc.z);
             const int2 pix = cs2pixel(pc.x, pc.y, v.w, v.h);
             if (in_range(pix, v.w, v.h) && !(depth_cam < 0.0f))
@@ -297,7 +309,8 @@ __device__ __forceinline__ void splat_pixel(const FrameParams &p, int view, uint
         }
         else
         {
-            cam[idx] = make_float4(xmul(fmx, wg), xmul(fmy, wg), xmul(fmz, wg), vis);
+            cam[idx] = make_float2(xmul(fmx, wg), xmul(fmy, wg));
+            cdep[idx] = z_to_depth(xadd(z_from, xmul(fmz, wg)));
             atomicMin(keys + idx, encode_key(z_to_depth(z_from), x, y));
         }
     }
@@ -699,11 +712,13 @@ __device__ __forceinline__ unsigned long long window_key(const unsigned long lon
 // threads: the body of reproj_kernel, also run as a work unit of batch_kernel.  `maps`: the
 // views' key-tile tensor maps; `bar`: the block's TMA completion barrier, initialised once per
 // thread block; `round`: TMA rounds that barrier has completed so far (its phase carries over
-// from unit to unit); `block_id`: the index the test hook `withhold_block` refers to.  Every
-// thread returns together (early exits are block-uniform or come after the last barrier).
+// from unit to unit); `aborted`: a shared word, 0 when the block starts, that a thread whose
+// wait for the key tiles gave up sets to 1; `block_id`: the index the test hook
+// `withhold_block` refers to.  Every thread returns together (early exits are block-uniform
+// or come after the last barrier).
 template <int SW, int SI, bool MAV, int REGS>
 __device__ __forceinline__ void reproj_block(const FrameParams &p, const CUtensorMap *maps, uint32_t bx, uint32_t by, uint32_t block_id,
-                                             unsigned char *smem, unsigned long long &bar, int &round)
+                                             unsigned char *smem, unsigned long long &bar, int &round, volatile uint32_t &aborted)
 {
     using T = Tile<SW>;
     const int nv = p.n_views, nf = p.n_frames, np = p.row_pairs, nu = nf * np;
@@ -718,7 +733,6 @@ __device__ __forceinline__ void reproj_block(const FrameParams &p, const CUtenso
     const bool xok = x < p.out_w;
     const bool leader = lane == 0 && vw == 0;
     const int round0 = round;
-    bool failed = false; // this thread's wait for the key tiles gave up (status word set)
     {
         const DevView &v = p.v[vw];
         const uint32_t ix = v.sx == 1 ? x : x / v.sx, tx0 = v.sx == 1 ? x0 : x0 / v.sx;
@@ -745,13 +759,16 @@ __device__ __forceinline__ void reproj_block(const FrameParams &p, const CUtenso
         for (int k = 0; k < nf; k++, round++)
         {
             const int u = k * np + rp;
-            // every warp is done with the previous unit's tiles; a block in which any thread's wait
-            // gave up leaves here, every thread together, having written nothing
-            if (round > round0 && __syncthreads_or(failed ? 1 : 0))
-                return;
+            if (round > round0)
+                __syncthreads(); // every warp is done with the previous unit's tiles
+            bool arrived = true;
             if (p.use_tma)
             {
-                if (leader)
+                // Once a wait of this block has given up (marked before the barrier above), the
+                // leader issues no more rounds: its arrival on a barrier whose phase did not
+                // complete would overrun the barrier's count.  It waits exactly when it issued.
+                const bool skip = aborted != 0u;
+                if (leader && !skip)
                 {
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     mbar_expect_tx(&bar, (uint32_t)(nv * T::BYTES));
@@ -763,9 +780,12 @@ __device__ __forceinline__ void reproj_block(const FrameParams &p, const CUtenso
                             tma_load_3d(tiles + (size_t)w * T::ELEMS, &maps[w], tile_x0(wx0, SW), (int)wy0 - SW, k, &bar);
                         }
                 }
-                // a thread whose copies did not arrive reads none of the tiles; the block leaves at
-                // its next barrier (the next unit's, or the one before phase 2)
-                failed = !mbar_wait_bounded(&bar, (uint32_t)(round & 1), p.status, p.wait_limit);
+                // a thread whose copies did not arrive reads none of the tiles and marks the block,
+                // which then leaves after the barrier that ends phase 1, writing nothing (the
+                // mark is written before that barrier and read after it, by every thread)
+                arrived = !skip && mbar_wait_bounded(&bar, (uint32_t)(round & 1), p.status, p.wait_limit);
+                if (!arrived)
+                    aborted = 1u;
             }
             else
             {
@@ -784,10 +804,11 @@ __device__ __forceinline__ void reproj_block(const FrameParams &p, const CUtenso
                 }
                 __syncwarp();
             }
-            if (!failed)
+            if (arrived)
             {
                 const unsigned long long *tg = tiles + (size_t)vw * T::ELEMS;
-                const float4 *cam = v.cam_ff + k * p.cam_stride;
+                const float2 *cam = v.cam_xy + k * p.cam_stride;
+                const float *cdep = v.cam_depth + k * p.depth_stride;
                 const bool search_ok = !fwd || p.f[k].alpha < 1.0f;
                 bool s[ROWS];
                 uint32_t ax[ROWS], ay[ROWS];
@@ -811,17 +832,17 @@ __device__ __forceinline__ void reproj_block(const FrameParams &p, const CUtenso
                     // splatted source pixel, in range): fetch its line into L1 during the search
                     // (3x3 window, 6 views: 0.537 -> 0.533 ms; no gain for the 7x7 window)
                     if (SW == 1 && s[r])
-                        asm volatile("prefetch.global.L1 [%0];" ::"l"(v.z + (ay[r] * vwid + ax[r])));
+                        asm volatile("prefetch.global.L1 [%0];" ::"l"(cdep + (ay[r] * vwid + ax[r])));
                 }
                 // iterativeSearch<SI>, src/renderer.cu:177-202, both rows interleaved.  The start is a
                 // splatted source pixel and every accepted step is in range: no border handling needed.
 #pragma unroll
                 for (int i = 0; i < SI; i++)
                 {
-                    float4 m[ROWS];
+                    float2 m[ROWS];
 #pragma unroll
                     for (int r = 0; r < ROWS; r++)
-                        m[r] = s[r] ? __ldg(cam + (ay[r] * vwid + ax[r])) : make_float4(0.f, 0.f, 0.f, 0.f);
+                        m[r] = s[r] ? __ldg(cam + (ay[r] * vwid + ax[r])) : make_float2(0.f, 0.f);
 #pragma unroll
                     for (int r = 0; r < ROWS; r++)
                     {
@@ -834,18 +855,21 @@ __device__ __forceinline__ void reproj_block(const FrameParams &p, const CUtenso
                     }
                 }
                 // final flow, depth and computeReprojError, src/renderer.cu:338-341, 204-215
-                float4 m[ROWS];
-                float zz[ROWS], fx[ROWS], fy[ROWS];
+                float2 m[ROWS];
+                float dz[ROWS], fx[ROWS], fy[ROWS];
+                bool vs[ROWS];
 #pragma unroll
                 for (int r = 0; r < ROWS; r++)
                 {
-                    m[r] = make_float4(0.f, 0.f, 0.f, 0.f);
-                    zz[r] = fx[r] = fy[r] = 0.f;
+                    m[r] = make_float2(0.f, 0.f);
+                    dz[r] = fx[r] = fy[r] = 0.f;
+                    vs[r] = false;
                     if (s[r])
                     {
                         const uint32_t si = ay[r] * vwid + ax[r];
                         m[r] = __ldg(cam + si);
-                        zz[r] = __ldg(v.z + si);
+                        dz[r] = __ldg(cdep + si);
+                        vs[r] = __ldg(v.vis + si) != 0;
                         fx[r] = __ldg(v.lut + ax[r]);
                         fy[r] = __ldg(v.lut + vwid + ay[r]);
                     }
@@ -858,14 +882,14 @@ __device__ __forceinline__ void reproj_block(const FrameParams &p, const CUtenso
                     d.depth = d_init[r];
                     if (s[r])
                     {
-                        d.depth = z_to_depth(xadd(zz[r], m[r].z));
+                        d.depth = dz[r];
                         // the scale res / min(res) (src/renderer.cu:213): the host's IEEE quotient, or
                         // under the reference's GPU semantics its device division
                         const float esx = FAST_MATH ? xdiv((float)vwid, (float)min(vwid, vhei)) : v.err_sx;
                         const float esy = FAST_MATH ? xdiv((float)vhei, (float)min(vwid, vhei)) : v.err_sy;
                         const float ex = xmul(xsub(xadd(fx[r], m[r].x), pcx), esx);
                         const float ey = xmul(xsub(xadd(fy[r], m[r].y), pcy[r]), esy);
-                        d.error_vis = pack_error_vis<SQUARED_ERRORS<REGS>>(xadd(xmul(ex, ex), xmul(ey, ey)), m[r].w > 0.0f);
+                        d.error_vis = pack_error_vis<SQUARED_ERRORS<REGS>>(xadd(xmul(ex, ex), xmul(ey, ey)), vs[r]);
                     }
                     d.src = (ax[r] << 16) | ay[r];
                     res[((u * ROWS + r) * nv + vw) * 32 + lane] = d;
@@ -874,7 +898,8 @@ __device__ __forceinline__ void reproj_block(const FrameParams &p, const CUtenso
         }
         }
     }
-    if (__syncthreads_or(failed ? 1 : 0))
+    __syncthreads();
+    if (aborted)
         return;
 
     // phase 2: (unit, row) tasks over the warps
@@ -936,14 +961,16 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
     unsigned long long &bar = *reinterpret_cast<unsigned long long *>(
         smem + reproj_tile_region<SW>(p.n_views, p.n_frames * p.row_pairs) +
         (size_t)p.n_frames * p.row_pairs * ROWS * p.n_views * 32 * sizeof(DirRes)); // TMA completion barrier
-    if (p.use_tma)
+    volatile uint32_t &aborted = *reinterpret_cast<volatile uint32_t *>(&bar + 1);
+    if (threadIdx.x == 0 && threadIdx.y == 0)
     {
-        if (threadIdx.x == 0 && threadIdx.y == 0)
+        if (p.use_tma)
             mbar_init(&bar, 1);
-        __syncthreads();
+        aborted = 0u;
     }
+    __syncthreads();
     int round = 0;
-    reproj_block<SW, SI, MAV, REGS>(p, km.m, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x, smem, bar, round);
+    reproj_block<SW, SI, MAV, REGS>(p, km.m, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x, smem, bar, round, aborted);
 }
 
 // ---- timewarp (mode 4), src/renderer.cu:467-522, 615-629 ----
@@ -1121,6 +1148,6 @@ __global__ void rgb8_to_rgba8_kernel(uint32_t *__restrict__ dst, const uint8_t *
 template <int SW>
 constexpr size_t reproj_smem(int n_views, int n_units)
 {
-    return reproj_tile_region<SW>(n_views, n_units) + (size_t)n_units * ROWS * n_views * 32 * sizeof(DirRes) + 16; // + mbarrier
+    return reproj_tile_region<SW>(n_views, n_units) + (size_t)n_units * ROWS * n_views * 32 * sizeof(DirRes) + 16; // + mbarrier, abort word
 }
 } // namespace isti

@@ -499,10 +499,10 @@ __global__ void __launch_bounds__(256) label_kernel(const __grid_constant__ Fram
             if (!(__uint_as_float((uint32_t)(lo >> 32)) > 0.0f))
                 continue;
             uint32_t sx = min(((uint32_t)lo) >> 16, dv.w - 1u), sy = min((uint32_t)lo & 0xFFFFu, dv.h - 1u);
-            const float4 *cam = dv.cam_ff + k * p.cam_stride;
+            const float2 *cam = dv.cam_xy + k * p.cam_stride;
             for (int i = 0; i < 3; i++)
             {
-                const float4 m = __ldg(cam + (sy * dv.w + sx));
+                const float2 m = __ldg(cam + (sy * dv.w + sx));
                 const int2 t = cs2pixel(xsub(qxc, m.x), xsub(qyc, m.y), dv.w, dv.h);
                 if (in_range(t, dv.w, dv.h))
                 {
@@ -510,7 +510,7 @@ __global__ void __launch_bounds__(256) label_kernel(const __grid_constant__ Fram
                     sy = (uint32_t)t.y;
                 }
             }
-            const float4 m = __ldg(cam + (sy * dv.w + sx));
+            const float2 m = __ldg(cam + (sy * dv.w + sx));
             const float ex = xmul(xsub(xadd(__ldg(dv.lut + sx), m.x), qxc), dv.err_sx);
             const float ey = xmul(xsub(xadd(__ldg(dv.lut + dv.w + sy), m.y), qyc), dv.err_sy);
             if (err_below<true>(err_pack<true>(xadd(xmul(ex, ex), xmul(ey, ey))), ERR_EPS_1_FULL_RES<true>))

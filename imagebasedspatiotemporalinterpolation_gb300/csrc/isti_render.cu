@@ -160,10 +160,12 @@ isti_status validate(int n_frames, void *const *outs, const isti_render_info *in
     return ISTI_OK;
 }
 
+// [keys: frame, view][client flow (x, y): frame, view][client-flow depth: frame, view]
+// [keyframe flow: view][visibility: view][pixel->clip tables: view][status word]
 struct Layout
 {
-    size_t key_frame_bytes, cam_frame_bytes; // one frame, every view
-    size_t key_bytes, cam_bytes, ff_bytes, lut_bytes, total;
+    size_t key_frame_bytes, cam_frame_bytes, depth_frame_bytes; // one frame, every view
+    size_t key_bytes, cam_bytes, depth_bytes, ff_bytes, vis_bytes, lut_bytes, total;
 };
 
 constexpr size_t STATUS_BYTES = 256;
@@ -175,13 +177,16 @@ Layout layout_of(const isti_view *const *views, int n_views, int n_frames)
     {
         const size_t px = (size_t)views[k]->width * views[k]->height;
         l.key_frame_bytes += align_up(px * 8, 256);
-        l.cam_frame_bytes += align_up(px * 16, 256);
+        l.cam_frame_bytes += align_up(px * 8, 256);
+        l.depth_frame_bytes += align_up(px * 4, 256);
+        l.ff_bytes += align_up(px * 16, 256);
+        l.vis_bytes += align_up(px, 256);
         l.lut_bytes += align_up((size_t)(views[k]->width + views[k]->height) * 4, 256);
     }
-    l.ff_bytes = l.cam_frame_bytes;
     l.key_bytes = l.key_frame_bytes * n_frames;
     l.cam_bytes = l.cam_frame_bytes * n_frames;
-    l.total = l.key_bytes + l.cam_bytes + l.ff_bytes + l.lut_bytes + STATUS_BYTES;
+    l.depth_bytes = l.depth_frame_bytes * n_frames;
+    l.total = l.key_bytes + l.cam_bytes + l.depth_bytes + l.ff_bytes + l.vis_bytes + l.lut_bytes + STATUS_BYTES;
     return l;
 }
 
@@ -207,7 +212,8 @@ void fill_params(isti::FrameParams &p, int n_frames, void *const *outs, const is
     p.withhold_block = -1;
     p.withhold_x = p.withhold_y = -1;
     const isti_render_info &info = infos[0];
-    size_t off_key = 0, off_cam = l.key_bytes, off_full = l.key_bytes + l.cam_bytes, off_lut = l.key_bytes + l.cam_bytes + l.ff_bytes;
+    size_t off_key = 0, off_cam = l.key_bytes, off_dep = off_cam + l.cam_bytes, off_full = off_dep + l.depth_bytes;
+    size_t off_vis = off_full + l.ff_bytes, off_lut = off_vis + l.vis_bytes;
     for (int k = 0; k < n_views; k++)
     {
         const bool fw = (k % 2) == 0;
@@ -238,12 +244,16 @@ void fill_params(isti::FrameParams &p, int n_frames, void *const *outs, const is
         std::memcpy(d.vp_self, v.viewproj, sizeof d.vp_self);
         const size_t px = (size_t)v.width * v.height;
         d.splat = reinterpret_cast<unsigned long long *>(base + off_key);
-        d.cam_ff = reinterpret_cast<float4 *>(base + off_cam);
+        d.cam_xy = l.cam_bytes ? reinterpret_cast<float2 *>(base + off_cam) : nullptr;
+        d.cam_depth = l.depth_bytes ? reinterpret_cast<float *>(base + off_dep) : nullptr;
+        d.vis = l.vis_bytes ? reinterpret_cast<uint8_t *>(base + off_vis) : nullptr;
         d.full_ff = reinterpret_cast<float4 *>(base + off_full);
         d.lut = reinterpret_cast<float *>(base + off_lut);
         off_key += align_up(px * 8, 256);
-        off_cam += align_up(px * 16, 256);
+        off_cam += align_up(px * 8, 256);
+        off_dep += align_up(px * 4, 256);
         off_full += align_up(px * 16, 256);
+        off_vis += align_up(px, 256);
         off_lut += align_up((size_t)(v.width + v.height) * 4, 256);
     }
     for (int k = 0; k < n_frames; k++)
@@ -257,7 +267,8 @@ void fill_params(isti::FrameParams &p, int n_frames, void *const *outs, const is
         p.f[k].no_shadows = infos[k].no_shadows ? 1 : 0;
     }
     p.key_stride = l.key_frame_bytes / sizeof(unsigned long long);
-    p.cam_stride = l.cam_frame_bytes / sizeof(float4);
+    p.cam_stride = l.cam_frame_bytes / sizeof(float2);
+    p.depth_stride = l.depth_frame_bytes / sizeof(float);
     p.keys = reinterpret_cast<ulonglong2 *>(base);
     p.key_units = l.key_bytes / sizeof(ulonglong2);
     p.status = reinterpret_cast<int32_t *>(base + l.total - STATUS_BYTES);
@@ -628,7 +639,7 @@ isti_status isti_renderer_tuning(const isti_renderer *r, int32_t index, isti_tun
     return ISTI_OK;
 }
 
-isti_status isti_renderer_view_buffers(const isti_renderer *r, int32_t view, const uint64_t **splat, const float **cam_ff,
+isti_status isti_renderer_view_buffers(const isti_renderer *r, int32_t view, const uint64_t **splat, const float **cam_xy,
                                        const float **full_ff, uint32_t *width, uint32_t *height)
 {
     if (!r || !r->has_frame)
@@ -641,14 +652,31 @@ isti_status isti_renderer_view_buffers(const isti_renderer *r, int32_t view, con
     const bool materialised = r->last.tw_mean == nullptr; // timewarp keeps no splat intermediates
     if (splat)
         *splat = materialised ? reinterpret_cast<const uint64_t *>(d.splat + k * r->last.key_stride) : nullptr;
-    if (cam_ff)
-        *cam_ff = materialised ? reinterpret_cast<const float *>(d.cam_ff + k * r->last.cam_stride) : nullptr;
+    if (cam_xy)
+        *cam_xy = materialised && d.cam_xy ? reinterpret_cast<const float *>(d.cam_xy + k * r->last.cam_stride) : nullptr;
     if (full_ff)
         *full_ff = materialised ? reinterpret_cast<const float *>(d.full_ff) : nullptr;
     if (width)
         *width = d.w;
     if (height)
         *height = d.h;
+    return ISTI_OK;
+}
+
+isti_status isti_renderer_view_depth(const isti_renderer *r, int32_t view, const float **cam_depth, const uint8_t **visible)
+{
+    if (!r || !r->has_frame)
+        return fail(ISTI_ERR_INVALID_ARG, "no frame rendered yet");
+    const int nv = r->last.n_views;
+    if (view < 0 || view >= nv * r->last.n_frames)
+        return fail(ISTI_ERR_INVALID_ARG, "view index out of range");
+    const int k = view / nv;
+    const isti::DevView &d = r->last.v[view % nv];
+    const bool materialised = r->last.tw_mean == nullptr;
+    if (cam_depth)
+        *cam_depth = materialised && d.cam_depth ? d.cam_depth + k * r->last.depth_stride : nullptr;
+    if (visible)
+        *visible = materialised ? d.vis : nullptr;
     return ISTI_OK;
 }
 
@@ -1053,9 +1081,8 @@ isti_status learned_setup(isti_renderer *r, isti_flownet *net, int32_t n_frames,
     }
     char *base = static_cast<char *>(r->learned_arena);
     isti::LearnedParams &p = r->learned;
-    fill_params(p.fp, n_frames, out_rgba, infos, frame, views, n_views, l, base, chain);
-    for (int v = 0; v < 2; v++)
-        p.fp.v[v].cam_ff = nullptr; // the client-camera flow is computed on the fly
+    fill_params(p.fp, n_frames, out_rgba, infos, frame, views, n_views, l, base, chain); // no client-flow buffers:
+                                                                                            // computed on the fly
     char *extra = base + l.total;
     for (int v = 0; v < 2; v++)
     {

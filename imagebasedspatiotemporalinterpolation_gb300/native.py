@@ -90,6 +90,7 @@ SIGNATURES = {
     "isti_render": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(IstiRenderInfo), C.POINTER(IstiFrameData), C.c_void_p]),
     "isti_renderer_view_buffers": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
                                              C.POINTER(C.c_void_p), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "isti_renderer_view_depth": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
     "isti_renderer_device_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "isti_renderer_enable_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "isti_renderer_timing": (C.c_int, [C.c_void_p, C.POINTER(IstiTiming)]),

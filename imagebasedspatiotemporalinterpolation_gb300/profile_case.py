@@ -1,10 +1,12 @@
 """Small, fixed workloads for kernel profiles (one launch of each hot kernel).
 
     python -m imagebasedspatiotemporalinterpolation_gb300.profile_case [--case all|plain|learned|pairs]
+                                                                     [--arith reference_gpu|ieee]
 
 plain   one batched call (isti_render_batch, chained) at 1920x1080: main camera plus aux
         cameras at +-0.3 m (6 source views), soft shadows, t = 0.25 / 0.5 / 0.75; one launch
-        each of init_kernel, splat_kernel and reproj_kernel.
+        each of init_kernel, splat_kernel and reproj_kernel, in the arithmetic --arith names
+        (default: the reference's GPU arithmetic, as the benchmark line).
 learned one learned-initialiser call (isti_render_learned, trained weights, 1 iteration) at
         1920x1080, main camera only, 3 frames: the network's conv kernels, keyframe_kernel,
         learned_kernel and the fallback kernels.
@@ -21,12 +23,13 @@ import argparse
 import sys
 
 
-def _plain(torch, seq_cls, frame_cls, renderer_cls):
+def _plain(torch, seq_cls, frame_cls, renderer_cls, arith):
     seq = seq_cls(1920, 1080, 2, seed=2024, aux_offsets=(-0.3, 0.3), shadows=True)
     frame = frame_cls.from_host(seq.frame(0))
     clients = [seq.client(0, b) for b in (1, 2, 3)]
     outs = [torch.zeros((1080, 1920, 4), dtype=torch.uint8, device="cuda") for _ in clients]
     r = renderer_cls()
+    r.set_arithmetic(arith)
     for _ in range(2):
         r.render_batch(outs, clients, frame, chain=True)
     torch.cuda.synchronize()
@@ -35,7 +38,7 @@ def _plain(torch, seq_cls, frame_cls, renderer_cls):
     return status
 
 
-def _learned(torch, seq_cls, frame_cls, renderer_cls):
+def _learned(torch, seq_cls, frame_cls, renderer_cls, arith):
     from . import train_flownet as T
     net = T.load()
     seq = seq_cls(1920, 1080, 2, seed=T.EVAL_SEED_BASE + 7, n_spheres=120, max_speed=1.0, max_rot_deg=5.0, max_step_m=0.1)
@@ -52,7 +55,7 @@ def _learned(torch, seq_cls, frame_cls, renderer_cls):
     return status
 
 
-def _pairs(torch, seq_cls, frame_cls, renderer_cls):
+def _pairs(torch, seq_cls, frame_cls, renderer_cls, arith):
     seq = seq_cls(1920, 1080, 5, seed=77)
     jobs = []
     for p in range(4):
@@ -72,8 +75,13 @@ def _pairs(torch, seq_cls, frame_cls, renderer_cls):
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", choices=["all", "plain", "learned", "pairs"], default="all")
+    ap.add_argument("--arith", choices=["reference_gpu", "ieee"], default="reference_gpu",
+                    help="arithmetic of the plain case (the learned and pairs cases are IEEE)")
     args = ap.parse_args(argv)
     import torch
+
+    from . import native
+    arith = native.ARITH_REFERENCE_GPU if args.arith == "reference_gpu" else native.ARITH_IEEE
 
     from .renderer import DeviceFrame, Renderer
     from .scene import Sequence
@@ -82,7 +90,7 @@ def main(argv=None) -> int:
     names = list(cases) if args.case == "all" else [args.case]
     bad = 0
     for name in names:
-        status = cases[name](torch, Sequence, DeviceFrame, Renderer)
+        status = cases[name](torch, Sequence, DeviceFrame, Renderer, arith)
         print(f"{name}: device status {status}", flush=True)
         bad |= status
     return 1 if bad else 0

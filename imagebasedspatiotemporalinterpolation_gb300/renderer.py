@@ -281,17 +281,29 @@ class Renderer:
         return out
 
     def view_buffers(self, view: int):
-        """(splat keys as int64 bit patterns (H, W), cam_ff f32 (H, W, 4), full_ff f32 (H, W, 4)) of the
-        last render, as copies."""
+        """(splat keys as int64 bit patterns (H, W), client flow (x, y) f32 (H, W, 2), full_ff f32
+        (H, W, 4)) of the last render, as copies."""
         torch = _torch()
         sp, cf, ff = C.c_void_p(), C.c_void_p(), C.c_void_p()
         w, h = C.c_uint32(), C.c_uint32()
         check(self._lib.isti_renderer_view_buffers(self._h, view, C.byref(sp), C.byref(cf), C.byref(ff), C.byref(w), C.byref(h)))
         H, W = h.value, w.value
         out = []
-        for ptr, shape, ts in ((sp, (H, W), "<i8"), (cf, (H, W, 4), "<f4"), (ff, (H, W, 4), "<f4")):
+        for ptr, shape, ts in ((sp, (H, W), "<i8"), (cf, (H, W, 2), "<f4"), (ff, (H, W, 4), "<f4")):
             out.append(None if not ptr.value else torch.as_tensor(_CudaArray(ptr.value, shape, ts), device="cuda").clone())
         return tuple(out)
+
+    def view_depth(self, view: int):
+        """(client-flow depth z_to_depth(z + dz) f32 (H, W), visible_in_main uint8 (H, W)) of the
+        last render, as copies (isti_renderer_view_depth)."""
+        torch = _torch()
+        dp, vs = C.c_void_p(), C.c_void_p()
+        w, h = C.c_uint32(), C.c_uint32()
+        check(self._lib.isti_renderer_view_buffers(self._h, view, None, None, None, C.byref(w), C.byref(h)))
+        check(self._lib.isti_renderer_view_depth(self._h, view, C.byref(dp), C.byref(vs)))
+        H, W = h.value, w.value
+        return tuple(None if not ptr.value else torch.as_tensor(_CudaArray(ptr.value, (H, W), ts), device="cuda").clone()
+                     for ptr, ts in ((dp, "<f4"), (vs, "|u1")))
 
 
 def render_noalloc(render_buffer, info, frame_data: DeviceFrame, stream=None) -> None:

@@ -26,9 +26,10 @@ Continuous batching: whenever a slot is free, the eye with the oldest waiting re
 of that eye's waiting requests on the same pair are rendered by one chained
 isti_render_batch call on the slot's stream, the first output starting as a copy of
 the eye's previous output.  When several eyes of that client are ready on the same pair
-(a stereo request), their next frames share one unchained call instead, each output
-starting as a copy of its own eye's previous output: one splat of the keyframe pair for
-both eyes.  Batches of different clients overlap on the device (one stream per slot).  A new keyframe pair is uploaded into the client's older pair slot
+(a stereo request) and the picked eye has only one request waiting on it, their next
+frames share one unchained call instead, each output starting as a copy of its own
+eye's previous output: one splat of the keyframe pair for both eyes.  (With a backlog
+the chained batch of the picked eye is larger than the stereo call, so it goes first.)  Batches of different clients overlap on the device (one stream per slot).  A new keyframe pair is uploaded into the client's older pair slot
 once no waiting or running request uses that slot's pair; the upload waits for the
 last batch that read the slot, and batches on the new pair wait for the upload (CUDA
 events, no host blocking).
@@ -43,6 +44,7 @@ unchanged on a fake backend in the CPU tests.
 from __future__ import annotations
 
 import collections
+import itertools
 import time
 from dataclasses import dataclass, field
 
@@ -401,7 +403,10 @@ class Server:
                 break
             _, c, ei, pslot = pick
             ready = self._ready_eyes(c, pslot)[:self.max_batch] if self.multi_eye else [ei]
-            if len(ready) > 1:
+            # an eye with a backlog on this pair (the device is behind) takes a chained batch of
+            # its own frames instead: fewer, larger calls while the load lasts
+            backlog = sum(1 for r in itertools.islice(c.eyes[ei].waiting, 2) if r.pair_seq == pslot.seq) > 1
+            if len(ready) > 1 and not backlog:
                 # the next frame of every ready eye in one unchained call: each output
                 # starts as a copy of its own eye's previous output
                 takes, chain = [(x, 1) for x in ready], False
@@ -512,8 +517,8 @@ class CudaBackend:
     @staticmethod
     def slot_bytes(pixels: int, views: int, frames: int) -> int:
         """Renderer arena of one slot: per view splat keys (8 B/px) and client-camera flow
-        (16 B/px) per frame, keyframe flow (16 B/px)."""
-        return pixels * views * (24 * frames + 16)
+        (x, y and depth, 12 B/px) per frame, keyframe flow (16 B/px) and visibility (1 B/px)."""
+        return pixels * views * (20 * frames + 17)
 
     @staticmethod
     def pair_bytes(template) -> int:

@@ -178,12 +178,21 @@ isti_status isti_render_pairs(isti_renderer *r, int32_t n_pairs, const isti_pair
 /* Device pointers to the intermediates of the last render call for view
  * `view` (0 fwd, 1 bwd, 2+2i aux i curr, 3+2i aux i next; after a batch,
  * frame k's views follow at k * (2 + 2 * num_aux)): 64-bit splat keys
- * (depth bits << 32 | x << 16 | y), f32x4 source->client flow and f32x4
- * source->other-keyframe flow (shared by the frames of a batch), each
- * width*height elements.  A field that is not materialised is returned as
+ * (depth bits << 32 | x << 16 | y), the f32x2 (x, y) of the source->client
+ * flow and the f32x4 source->other-keyframe flow (shared by the frames of a
+ * batch), each width*height elements.  The reference keeps the client flow
+ * as f32x4 (x, y, dz, visible); its other two parts are read by
+ * isti_renderer_view_depth.  A field that is not materialised is returned as
  * NULL.  Valid until the next render or destroy. */
-isti_status isti_renderer_view_buffers(const isti_renderer *r, int32_t view, const uint64_t **splat, const float **cam_ff,
+isti_status isti_renderer_view_buffers(const isti_renderer *r, int32_t view, const uint64_t **splat, const float **cam_xy,
                                        const float **full_ff, uint32_t *width, uint32_t *height);
+
+/* The rest of the client flow of the same view: per source pixel the depth the
+ * reprojection derives from it, z_to_depth(z + dz) (src/renderer.cu:339, the
+ * reference's rounding: dz first, then the sum), f32, and visible_in_main as
+ * one byte (0 / 1, the reference flow's w; shared by the frames of a batch),
+ * each width*height elements.  NULL when not materialised. */
+isti_status isti_renderer_view_depth(const isti_renderer *r, int32_t view, const float **cam_depth, const uint8_t **visible);
 
 /* Per-stage device time (no counterpart in the reference, which has no
  * timers): when enabled, each render records CUDA events around the key
@@ -266,10 +275,11 @@ isti_status isti_renderer_tuning(const isti_renderer *r, int32_t index, isti_tun
  * array inside this library (ISTI_NOALLOC_SCRATCH_BYTES, held by every GPU
  * that loads the library until the process exits).
  *
- *  - Limit: the sum over source views of width*height*40 bytes (each buffer
- *    rounded up to 256 bytes) must fit in ISTI_NOALLOC_SCRATCH_BYTES minus the
- *    256 bytes of its status word, e.g. 640x360 with up to two aux cameras;
- *    larger frames are rejected with ISTI_ERR_INVALID_ARG.
+ *  - Limit: the sum over source views of width*height*37 bytes and
+ *    (width+height)*4 bytes (each buffer rounded up to 256 bytes) must fit in
+ *    ISTI_NOALLOC_SCRATCH_BYTES minus the 256 bytes of its status word, e.g.
+ *    640x360 with up to two aux cameras; larger frames are rejected with
+ *    ISTI_ERR_INVALID_ARG.
  *  - A call made outside a stream capture looks up the array's device address
  *    (with the device current) and remembers it; a captured call uses the
  *    remembered one.  So make the first call on a device, and the first call

@@ -12,6 +12,7 @@ import oracle
 from imagebasedspatiotemporalinterpolation_gb300 import native
 from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame, Renderer
 from imagebasedspatiotemporalinterpolation_gb300.scene import Sequence
+from tests.flowcheck import assert_client_flow_equal
 from tests.golden import fixtures
 
 pytestmark = pytest.mark.gpu
@@ -33,27 +34,38 @@ def render_gpu(frame, client, prev, motion_format="f16x3", renderer=None):
     r.render(out, client, dev)
     torch.cuda.synchronize()
     assert r.device_status() == 0
-    bufs = [r.view_buffers(k) for k in range(len(dev.views()))]
+    nv = len(dev.views())
+    bufs = [r.view_buffers(k) for k in range(nv)]
+    deps = [r.view_depth(k) for k in range(nv)]
     npy = lambda t, view=None: None if t is None else (t.cpu().numpy().view(view) if view else t.cpu().numpy())
-    res = (out.cpu().numpy(), [npy(b[0], np.uint64) for b in bufs], [npy(b[1]) for b in bufs], [npy(b[2]) for b in bufs])
+    cams = [None if b[1] is None else client_flow(b[1], d[0], d[1]) for b, d in zip(bufs, deps)]
+    res = (out.cpu().numpy(), [npy(b[0], np.uint64) for b in bufs], cams, [npy(b[2]) for b in bufs],
+           [v.z.cpu().numpy() for v in dev.views()])
     if renderer is None:
         r.close()
     return res
 
 
+def client_flow(xy, depth, vis):
+    """The renderer's client-flow parts as numpy: (x, y) (H, W, 2), depth (H, W), visible (H, W)."""
+    return xy.cpu().numpy(), depth.cpu().numpy(), vis.cpu().numpy()
+
+
 def assert_bit_exact(got, exp_out, exp_splat, exp_cam=None, exp_full=None):
-    out, splats, cams, fulls = got
+    out, splats, cams, fulls, zs = got
     diff = np.abs(out.astype(np.int32) - exp_out.astype(np.int32))
     assert diff.max() <= TOL_PER_CHANNEL and psnr(out, exp_out) >= TOL_PSNR_DB
     assert np.array_equal(out, exp_out), f"{int((out != exp_out).any(-1).sum())} output pixels differ"
     for k, (a, b) in enumerate(zip(splats, exp_splat)):
         assert np.array_equal(a, b), f"view {k}: {int((a != b).sum())} splat keys differ"
-    for name, got_l, exp_l in (("cam_ff", cams, exp_cam), ("full_ff", fulls, exp_full)):
-        if exp_l is None:
-            continue
-        for k, (a, b) in enumerate(zip(got_l, exp_l)):
+    if exp_cam is not None:
+        for k, (a, b) in enumerate(zip(cams, exp_cam)):
             if b is not None:
-                assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), f"view {k}: {name} differs"
+                assert_client_flow_equal(k, a, b, zs[k])
+    if exp_full is not None:
+        for k, (a, b) in enumerate(zip(fulls, exp_full)):
+            if b is not None:
+                assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), f"view {k}: full_ff differs"
 
 
 @pytest.mark.parametrize("motion_format", ["f16x3", "f32x4"])

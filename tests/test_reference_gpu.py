@@ -23,6 +23,7 @@ import oracle
 from imagebasedspatiotemporalinterpolation_gb300 import native
 from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame, Renderer
 from imagebasedspatiotemporalinterpolation_gb300.scene import Sequence
+from tests.flowcheck import assert_client_flow_equal, expected_client_flow
 
 pytestmark = pytest.mark.gpu
 
@@ -54,9 +55,12 @@ def render(frame, client, prev, arith):
     r.render(out, client, dev)
     torch.cuda.synchronize()
     assert r.device_status() == native.ISTI_OK
-    bufs = [r.view_buffers(k) for k in range(len(dev.views()))]
-    res = (out.cpu().numpy(), [b[0].cpu().numpy().view(np.uint64) for b in bufs], [b[1].cpu().numpy() for b in bufs],
-           [b[2].cpu().numpy() for b in bufs])
+    nv = len(dev.views())
+    bufs = [r.view_buffers(k) for k in range(nv)]
+    deps = [r.view_depth(k) for k in range(nv)]
+    res = (out.cpu().numpy(), [b[0].cpu().numpy().view(np.uint64) for b in bufs],
+           [(b[1].cpu().numpy(), d[0].cpu().numpy(), d[1].cpu().numpy()) for b, d in zip(bufs, deps)],
+           [b[2].cpu().numpy() for b in bufs], [v.z.cpu().numpy() for v in dev.views()])
     r.close()
     return res
 
@@ -98,7 +102,7 @@ def test_reference_gpu_semantics_bit_exact(cuda, ref_gpu, case, b, mode):
     prev = np.full((client.height, client.width, 4), 40, np.uint8)
     exp = ref_gpu(frame, client, prev)
     got = render(frame, client, prev, native.ARITH_REFERENCE_GPU)
-    out, splats, cams, fulls = got
+    out, splats, cams, fulls, zs = got
     diff = np.abs(out.astype(np.int32) - exp[0].astype(np.int32))
     assert diff.max() <= TOL_PER_CHANNEL and psnr(out, exp[0]) >= TOL_PSNR_DB
     assert np.array_equal(out, exp[0]), f"{int((out != exp[0]).any(-1).sum())} output pixels differ"
@@ -106,9 +110,10 @@ def test_reference_gpu_semantics_bit_exact(cuda, ref_gpu, case, b, mode):
         idx = int(((a & 0xFFFFFFFF) != (e & 0xFFFFFFFF)).sum())
         assert idx == 0, f"view {k}: {idx} winning source indices differ"
         assert np.array_equal(a, e), f"view {k}: {int((a != e).sum())} splat keys differ"
-    for name, got_l, exp_l in (("cam_ff", cams, exp[2]), ("full_ff", fulls, exp[3])):
-        for k, (a, e) in enumerate(zip(got_l, exp_l)):
-            assert np.array_equal(a.view(np.uint32), e.view(np.uint32)), f"view {k}: {name} differs"
+    for k, (a, e) in enumerate(zip(cams, exp[2])):
+        assert_client_flow_equal(k, a, e, zs[k])
+    for k, (a, e) in enumerate(zip(fulls, exp[3])):
+        assert np.array_equal(a.view(np.uint32), e.view(np.uint32)), f"view {k}: full_ff differs"
 
 
 @pytest.mark.parametrize("case,b", [("c1", 2), ("c2", 2)])
@@ -119,14 +124,17 @@ def test_ieee_mode_against_reference_gpu_build(cuda, ref_gpu, case, b):
     frame, client = seq.frame(0), seq.client(0, b)
     prev = np.full((client.height, client.width, 4), 40, np.uint8)
     exp = ref_gpu(frame, client, prev)
-    out, splats, cams, _ = render(frame, client, prev, native.ARITH_IEEE)
+    out, splats, cams, _, zs = render(frame, client, prev, native.ARITH_IEEE)
     counts = []
     for a, e in zip(splats, exp[1]):
         mism = int(((a & 0xFFFFFFFF) != (e & 0xFFFFFFFF)).sum())
         counts.append(mism)
         assert mism <= IEEE_MAX_INDEX_MISMATCH * a.size
-    for a, e in zip(cams, exp[2]):
-        fin = np.isfinite(a[..., :3]) & np.isfinite(e[..., :3])
-        assert np.abs(a[..., :3] - e[..., :3])[fin].max() < 1e-4
+    for (xy, depth, _), e, z in zip(cams, exp[2], zs):
+        exy, edepth, _ = expected_client_flow(e, z)
+        fin = np.isfinite(xy) & np.isfinite(exy)
+        assert np.abs(xy - exy)[fin].max() < 1e-4
+        fin = np.isfinite(depth) & np.isfinite(edepth)
+        assert np.abs(depth - edepth)[fin].max() < 1e-4
     print(f"{case}: IEEE-mode winning-index mismatches per view {counts}, "
           f"{int((out != exp[0]).any(-1).sum())} output pixels differ, PSNR {psnr(out, exp[0]):.1f} dB")

@@ -70,7 +70,7 @@ class FakeBackend:
 
     @staticmethod
     def slot_bytes(pixels, views, frames):
-        return pixels * views * (24 * frames + 16)
+        return pixels * views * (20 * frames + 17)
 
     @staticmethod
     def pair_bytes(template):
@@ -434,3 +434,25 @@ def test_sessions_defer_admission_and_every_accepted_request_completes():
     assert st["refused_not_admitted"] > 0
     assert st["peak_reserved_bytes"] <= server.budget
     assert st["requests"] == st["offered_requests"] - st["refused_requests"]
+
+
+def test_backlogged_eye_takes_a_chained_batch_before_the_stereo_call():
+    """One request per eye: both eyes share one unchained (stereo) call.  An eye with a
+    backlog on the pair takes a chained batch of its own frames first."""
+    for backlog, want in ((1, (2, False)), (3, (3, True))):
+        rng = random.Random(2)
+        be = FakeBackend(rng, max_advance=0)
+        server = Server(be, hbm_budget=10**12, n_slots=1, max_batch=4, slot_pixels=64 * 36, clock=Clock())
+        assert server.open_client(0, 64, 36, 2, Pair(1000))
+        server.push_pair(0, HostPair(5))
+        for i in range(backlog):
+            server.submit(0, 0, (i, (0, 0), 5))
+        server.submit(0, 1, (9, (0, 1), 5))
+        server.step()
+        be.advance(10)              # the upload
+        server.step()
+        assert be.launch_log, "nothing launched"
+        size, _, _, chain, _ = be.launch_log[0]
+        assert (size, chain) == want
+        be.max_advance = 3
+        server.drain(timeout_s=5.0)
