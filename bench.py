@@ -785,6 +785,7 @@ def run_graph_batch(args, dev, rank):
             r.render_batch(o, infos, frame, chain=False, stream=stream)
     stream.synchronize()
     tuned = [{"size": f"{t['width']}x{t['height']}", "regs": t["regs"], "row_pairs": t["row_pairs"],
+              "key_tiles": "plain loads" if t["plain_tiles"] else "TMA",
               "reproj_ms": round(t["best_ms"], 4), "rule_reproj_ms": round(t["rule_ms"], 4)} for t in r.tuning()]
     graph = torch.cuda.CUDAGraph()
     with torch.cuda.stream(stream):
@@ -857,10 +858,25 @@ def run_graph_batch(args, dev, rank):
             raise RuntimeError("persistent launch: frames differ from the per-pair launches")
         if rp.device_status() != 0:
             raise RuntimeError("persistent launch: a bounded wait gave up")
+        # work-unit sizes (isti_renderer_set_pair_units), uncaptured calls; the output must not change
+        sizes = []
+        for rows, kib in ((16, 64), (8, 64), (32, 256), (64, 1024)):
+            rp.set_pair_units(rows, kib)
+            with torch.cuda.stream(stream):
+                for _ in range(2):
+                    rp.render_pairs(pjobs, stream=stream)
+                u0, u1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                u0.record(stream)
+                for _ in range(5):
+                    rp.render_pairs(pjobs, stream=stream)
+                u1.record(stream)
+            stream.synchronize()
+            ok = all(torch.equal(a, b) for po, o in zip(pouts, outs) for a, b in zip(po, o)) and rp.device_status() == 0
+            sizes.append({"splat_rows": rows, "init_unit_kib": kib, "ms_per_batch": round(u0.elapsed_time(u1) / 5, 4), "equal": ok})
         rp.close()
         persistent = {"value": round(mpix / (pms / 1e3), 2), "unit": "Mpix/s", "ms_per_batch": round(pms, 4),
                       "p50_batch_ms": round(pb[len(pb) // 2], 4), "p99_batch_ms": round(pb[min(len(pb) - 1, int(0.99 * len(pb)))], 4),
-                      "launches_per_batch": 1, "equal_to_per_pair_launches": True}
+                      "launches_per_batch": 1, "equal_to_per_pair_launches": True, "unit_sizes_uncaptured": sizes}
     except Exception as ex:  # reported, not fatal: the per-pair graph is the reference line
         persistent = {"error": str(ex)[:300]}
     return {"value": round(mpix / (ms / 1e3), 2), "unit": "Mpix/s", "mpix_per_batch": round(mpix, 2),

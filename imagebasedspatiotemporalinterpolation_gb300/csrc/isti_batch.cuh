@@ -2,8 +2,9 @@
 // counterpart in the reference, which renders frame by frame, src/main.cu:152-190).
 //
 // The work of every pair -- key initialisation, splatting, reprojection (isti_kernels.cuh) --
-// is cut into units: init units (64 KiB of keys each, plus the pixel->clip tables), splat
-// units (32 x 16 source pixels of one view, every frame) and reprojection units (one
+// is cut into units: init units (256 KiB of keys each by default, plus the pixel->clip
+// tables), splat units (32 x 32 source pixels of one view by default, every frame) and
+// reprojection units (one
 // reprojection block, reproj_block).  One cooperative launch keeps every CTA resident; each
 // CTA takes tickets from one atomic queue until it runs dry.  The queue is
 // software-pipelined over the pairs,
@@ -21,8 +22,11 @@
 
 namespace isti
 {
-constexpr uint32_t BATCH_INIT_UNIT_KEYS = 4096; // 16-byte key units per init unit (64 KiB)
-constexpr int BATCH_SPLAT_ROWS = 16;            // source rows per splat unit (32 columns)
+// Unit sizes when the caller sets none (isti_renderer_set_pair_units).  Measured on the
+// 96-frame mixed batch (16 pairs x 3 t x 2 eyes, uncaptured calls): 8 rows / 64 KiB 16.68 ms,
+// 16 / 64 KiB 15.65, 32 / 256 KiB 15.15, 64 / 1024 KiB 15.73.
+constexpr uint32_t BATCH_INIT_UNIT_KEYS = 16384; // 16-byte key units per init unit (256 KiB)
+constexpr uint32_t BATCH_SPLAT_ROWS = 32;        // source rows per splat unit (32 columns)
 
 struct BatchPair
 {
@@ -30,7 +34,7 @@ struct BatchPair
     const CUtensorMap *maps;   // device copy of its key-tile tensor maps (n_views of them)
     uint32_t init_units, splat_units, reproj_units;
     uint32_t reproj_gx;        // reprojection blocks per block row
-    uint32_t splat_gx, splat_gy; // splat units per view: columns of 32, rows of BATCH_SPLAT_ROWS
+    uint32_t splat_gx, splat_gy; // splat units per view: columns of 32, rows of BatchParams::splat_rows
 };
 
 struct BatchSeg
@@ -50,6 +54,7 @@ struct BatchParams
     uint32_t spin_limit;
     uint32_t region_bytes;     // reprojection shared memory of the largest pair; the barrier follows
     uint32_t param_bytes;      // params_prefix(n_views): the staged part of a pair's FrameParams
+    uint32_t splat_rows;       // source rows per splat unit
 };
 
 // Shared memory of a batch_kernel block: [the current pair's FrameParams prefix, padded to
@@ -179,8 +184,8 @@ __global__ void __maxnreg__(REGS) batch_kernel(const __grid_constant__ BatchPara
                 const int view = (int)(u / per_view);
                 const uint32_t r = u % per_view;
                 const uint32_t x = (r % bpair.splat_gx) * 32 + threadIdx.x;
-                const uint32_t y0 = (r / bpair.splat_gx) * BATCH_SPLAT_ROWS;
-                for (uint32_t yy = threadIdx.y; yy < BATCH_SPLAT_ROWS; yy += blockDim.y)
+                const uint32_t y0 = (r / bpair.splat_gx) * bp.splat_rows;
+                for (uint32_t yy = threadIdx.y; yy < bp.splat_rows; yy += blockDim.y)
                     splat_pixel(p, view, x, y0 + yy);
             }
             else

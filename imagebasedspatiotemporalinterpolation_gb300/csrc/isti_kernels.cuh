@@ -156,21 +156,28 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, uint32_t 
     return ok != 0;
 }
 
+// The part of mbar_wait_bounded after its first limit ran out, out of line so that the
+// common path keeps no registers for it: the status word is set and the wait is retried
+// once more with the same limit (the copies may still be landing).
+__device__ __noinline__ bool mbar_wait_late(unsigned long long *bar, uint32_t parity, int32_t *status, uint32_t lim)
+{
+    atomicExch(status, (int32_t)ISTI_ERR_TIMEOUT);
+    for (uint32_t i = 0; i < lim; i++)
+        if (mbar_try_wait(bar, parity))
+            return true;
+    return false;
+}
+
 // Waits for phase `parity` of the barrier with an iteration limit (0: the default of 2^22
-// polls, seconds at most).  On timeout the device status word is set and the wait is
-// retried once more with the same limit (the copies may still be landing).  Returns false
-// when both waits gave up: the tiles are then not to be read.
+// polls, seconds at most).  Returns false when the wait and its retry (mbar_wait_late) gave
+// up: the tiles are then not to be read.
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, uint32_t parity, int32_t *status, uint32_t limit)
 {
     const uint32_t lim = limit ? limit : (1u << 22);
     for (uint32_t i = 0; i < lim; i++)
         if (mbar_try_wait(bar, parity))
             return true;
-    atomicExch(status, (int32_t)ISTI_ERR_TIMEOUT);
-    for (uint32_t i = 0; i < lim; i++)
-        if (mbar_try_wait(bar, parity))
-            return true;
-    return false;
+    return mbar_wait_late(bar, parity, status, lim);
 }
 
 // 3-D tiled bulk copy global -> shared, completion counted on `bar`.  x * 8 bytes must be a
@@ -714,9 +721,9 @@ __device__ __forceinline__ unsigned long long window_key(const unsigned long lon
 // thread block; `round`: TMA rounds that barrier has completed so far (its phase carries over
 // from unit to unit); `aborted`: a shared word, 0 when the block starts, that a thread whose
 // wait for the key tiles gave up sets to 1; `block_id`: the index the test hook
-// `withhold_block` refers to.  Every thread returns together (early exits are block-uniform
-// or come after the last barrier).
-template <int SW, int SI, bool MAV, int REGS>
+// `withhold_block` refers to, compiled in only where HOOK is set.  Every thread returns
+// together (early exits are block-uniform or come after the last barrier).
+template <int SW, int SI, bool MAV, int REGS, bool HOOK = false>
 __device__ __forceinline__ void reproj_block(const FrameParams &p, const CUtensorMap *maps, uint32_t bx, uint32_t by, uint32_t block_id,
                                              unsigned char *smem, unsigned long long &bar, int &round, volatile uint32_t &aborted)
 {
@@ -766,13 +773,13 @@ __device__ __forceinline__ void reproj_block(const FrameParams &p, const CUtenso
             {
                 // Once a wait of this block has given up (marked before the barrier above), the
                 // leader issues no more rounds: its arrival on a barrier whose phase did not
-                // complete would overrun the barrier's count.  It waits exactly when it issued.
-                const bool skip = aborted != 0u;
-                if (leader && !skip)
+                // complete would overrun the barrier's count.  The other waits then run out too
+                // (bounded), and the block writes nothing.
+                if (leader && aborted == 0u)
                 {
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     mbar_expect_tx(&bar, (uint32_t)(nv * T::BYTES));
-                    if (p.withhold_block != (int32_t)block_id)
+                    if (!HOOK || p.withhold_block != (int32_t)block_id)
                         for (int w = 0; w < nv; w++)
                         {
                             const DevView &vv = p.v[w];
@@ -783,7 +790,7 @@ __device__ __forceinline__ void reproj_block(const FrameParams &p, const CUtenso
                 // a thread whose copies did not arrive reads none of the tiles and marks the block,
                 // which then leaves after the barrier that ends phase 1, writing nothing (the
                 // mark is written before that barrier and read after it, by every thread)
-                arrived = !skip && mbar_wait_bounded(&bar, (uint32_t)(round & 1), p.status, p.wait_limit);
+                arrived = mbar_wait_bounded(&bar, (uint32_t)(round & 1), p.status, p.wait_limit);
                 if (!arrived)
                     aborted = 1u;
             }
@@ -952,7 +959,9 @@ __device__ __forceinline__ void reproj_block(const FrameParams &p, const CUtenso
 // bidirectionalReprojection_kernel<SW, SI, MAIN_ALWAYS_VALID>, src/renderer.cu:400-465
 // block = (32, n_views): 32 output columns x (2 * row_pairs) output rows, one warp per source
 // view (reproj_block).
-template <int SW, int SI, bool MAV, int REGS>
+// HOOK: built with the failure-detection test hook (FrameParams::withhold_block); the
+// launch uses that instance only when the hook is armed.
+template <int SW, int SI, bool MAV, int REGS, bool HOOK = false>
 __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FrameParams p, const __grid_constant__ KeyMaps km)
 {
     // dynamic shared memory only (no static __shared__ in front of it): the key tiles start at
@@ -970,7 +979,7 @@ __global__ void __maxnreg__(REGS) reproj_kernel(const __grid_constant__ FramePar
     }
     __syncthreads();
     int round = 0;
-    reproj_block<SW, SI, MAV, REGS>(p, km.m, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x, smem, bar, round, aborted);
+    reproj_block<SW, SI, MAV, REGS, HOOK>(p, km.m, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x, smem, bar, round, aborted);
 }
 
 // ---- timewarp (mode 4), src/renderer.cu:467-522, 615-629 ----

@@ -82,6 +82,7 @@ struct ReprojChoice
 {
     int regs = 0;
     int row_pairs = 0;
+    int plain_tiles = 0; // 1: key tiles by plain loads even where a TMA copy is possible
 };
 
 // The fixed rule: register cap by window size and view count (isti_kernels.cuh), row pairs
@@ -96,7 +97,7 @@ int rule_regs(int sw, int n_views)
 int rule_row_pairs(int n_views, int n_frames) { return std::max(1, std::min(3, n_views / (isti::ROWS * n_frames))); }
 
 template <int SW, int SI, bool MAV, int REGS>
-cudaError_t launch_reproj_regs(isti::FrameParams &p, cudaStream_t stream, int row_pairs)
+cudaError_t launch_reproj_regs(isti::FrameParams &p, cudaStream_t stream, int row_pairs, bool plain_tiles)
 {
     // One unit's key tiles per TMA round: the least shared memory per block, so the most
     // resident blocks and the largest L1 (1080p, 6 views, 3 frames, 8 blocks per SM: one
@@ -109,31 +110,33 @@ cudaError_t launch_reproj_regs(isti::FrameParams &p, cudaStream_t stream, int ro
         return e;
     p.row_pairs = row_pairs > 0 ? std::min(row_pairs, 3) : rule_row_pairs(p.n_views, p.n_frames);
     static thread_local isti::KeyMaps km; // 2 KiB, passed by value as a kernel parameter
-    p.use_tma = make_key_maps<SW>(p, km) ? 1 : 0;
+    p.use_tma = (!plain_tiles && make_key_maps<SW>(p, km)) ? 1 : 0;
     const size_t smem = isti::reproj_smem<SW>(p.n_views, p.n_frames * p.row_pairs);
-    // raise the kernel's dynamic shared-memory limit once to the largest size requested, so
-    // that calls inside a CUDA graph capture make no attribute calls after a first uncaptured
-    // call of the same shape
-    static std::mutex attr_mutex;
-    static int attr_set[64] = {}; // per device
-    if (smem > 48 * 1024)
-    {
-        std::lock_guard<std::mutex> lock(attr_mutex);
-        int &cur = attr_set[dev & 63];
-        if ((int)smem > cur)
-        {
-            e = cudaFuncSetAttribute(isti::reproj_kernel<SW, SI, MAV, REGS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess)
-                return e;
-            cur = (int)smem;
-        }
-    }
     const uint32_t block_rows = (uint32_t)(isti::ROWS * p.row_pairs);
     const dim3 gr((p.out_w + 31) / 32, (p.out_h + block_rows - 1) / block_rows);
     p.withhold_block = -1;
     if (p.withhold_x >= 0 && p.withhold_y >= 0 && (uint32_t)p.withhold_x < p.out_w && (uint32_t)p.withhold_y < p.out_h)
         p.withhold_block = (int32_t)(((uint32_t)p.withhold_y / block_rows) * gr.x + (uint32_t)p.withhold_x / 32u);
-    isti::reproj_kernel<SW, SI, MAV, REGS><<<gr, dim3(32, p.n_views), smem, stream>>>(p, km);
+    const bool hook = p.withhold_block >= 0 && p.use_tma;
+    auto kernel = hook ? isti::reproj_kernel<SW, SI, MAV, REGS, true> : isti::reproj_kernel<SW, SI, MAV, REGS, false>;
+    // raise the kernel's dynamic shared-memory limit once to the largest size requested, so
+    // that calls inside a CUDA graph capture make no attribute calls after a first uncaptured
+    // call of the same shape
+    static std::mutex attr_mutex;
+    static int attr_set[2][64] = {}; // per kernel instance and device
+    if (smem > 48 * 1024)
+    {
+        std::lock_guard<std::mutex> lock(attr_mutex);
+        int &cur = attr_set[hook ? 1 : 0][dev & 63];
+        if ((int)smem > cur)
+        {
+            e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess)
+                return e;
+            cur = (int)smem;
+        }
+    }
+    kernel<<<gr, dim3(32, p.n_views), smem, stream>>>(p, km);
     return cudaGetLastError();
 }
 
@@ -144,11 +147,11 @@ cudaError_t launch_reproj(isti::FrameParams &p, cudaStream_t stream, ReprojChoic
     if constexpr (SW == 1)
     {
         if (regs == isti::REPROJ_REGS_MANY_VIEWS)
-            return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS_MANY_VIEWS>(p, stream, c.row_pairs);
-        return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS>(p, stream, c.row_pairs);
+            return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS_MANY_VIEWS>(p, stream, c.row_pairs, c.plain_tiles != 0);
+        return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS>(p, stream, c.row_pairs, c.plain_tiles != 0);
     }
     else
-        return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS_WIDE_WINDOW>(p, stream, c.row_pairs);
+        return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS_WIDE_WINDOW>(p, stream, c.row_pairs, c.plain_tiles != 0);
 }
 
 // window size of the reprojection of a render mode (src/renderer.cu:676-693)

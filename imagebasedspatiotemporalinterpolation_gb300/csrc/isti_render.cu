@@ -63,9 +63,11 @@ struct isti_renderer
     // pinned staging of the parameter block and the event of its last copy
     void *multi_arena = nullptr;
     size_t multi_bytes = 0;
-    void *multi_host = nullptr;
-    size_t multi_host_bytes = 0;
+    int32_t pair_splat_rows = 0, pair_init_kib = 0; // isti_render_pairs unit sizes (0: the defaults)
+    void *multi_host[2] = {nullptr, nullptr}; // parameter staging: uncaptured calls, captured calls
+    size_t multi_host_bytes[2] = {0, 0};
     cudaEvent_t multi_copied = nullptr;
+    bool multi_recorded = false; // multi_copied was last recorded outside a stream capture
 };
 
 namespace
@@ -305,7 +307,7 @@ isti_tuning *find_tuning(isti_renderer *r, int mode, const isti::FrameParams &p)
 cudaError_t launch_reproj_arith(isti_renderer *r, isti::FrameParams &p, int mode, cudaStream_t stream, isti::ReprojChoice c)
 {
     if (r->arith == ISTI_ARITH_REFERENCE_GPU)
-        return isti_fm_launch_reproj_mode(&p, mode, stream, c.regs, c.row_pairs);
+        return isti_fm_launch_reproj_mode(&p, mode, stream, c.regs, c.row_pairs, c.plain_tiles);
     return isti::launch_reproj_mode(p, mode, stream, c);
 }
 
@@ -314,10 +316,11 @@ isti_status tune_reproj(isti_renderer *r, int mode, cudaStream_t stream)
     constexpr int REPEAT = 3;
     isti::FrameParams &p = r->last;
     std::vector<isti::ReprojChoice> cands;
-    for (int regs : isti::mode_regs(mode))
-        for (int np = 1; np <= 3; np++)
-            cands.push_back({regs, np});
-    const isti::ReprojChoice rule{isti::rule_regs(isti::mode_window(mode), p.n_views), isti::rule_row_pairs(p.n_views, p.n_frames)};
+    for (int plain = 0; plain <= 1; plain++) // key tiles by TMA (where the views allow it), or by plain loads
+        for (int regs : isti::mode_regs(mode))
+            for (int np = 1; np <= 3; np++)
+                cands.push_back({regs, np, plain});
+    const isti::ReprojChoice rule{isti::rule_regs(isti::mode_window(mode), p.n_views), isti::rule_row_pairs(p.n_views, p.n_frames), 0};
     std::vector<cudaEvent_t> ev(2 * cands.size(), nullptr);
     cudaError_t e = cudaSuccess;
     for (cudaEvent_t &x : ev)
@@ -348,7 +351,7 @@ isti_status tune_reproj(isti_renderer *r, int mode, cudaStream_t stream)
             best_ms = ms;
             best = i;
         }
-        if (cands[i].regs == rule.regs && cands[i].row_pairs == rule.row_pairs)
+        if (cands[i].regs == rule.regs && cands[i].row_pairs == rule.row_pairs && cands[i].plain_tiles == rule.plain_tiles)
             rule_ms = ms;
     }
     for (cudaEvent_t x : ev)
@@ -365,6 +368,7 @@ isti_status tune_reproj(isti_renderer *r, int mode, cudaStream_t stream)
     t.height = p.out_h;
     t.regs = cands[best].regs;
     t.row_pairs = cands[best].row_pairs;
+    t.plain_tiles = cands[best].plain_tiles;
     t.best_ms = best_ms;
     t.rule_ms = rule_ms;
     r->tuned.push_back(t);
@@ -434,11 +438,11 @@ isti_status render_batch(isti_renderer *r, int n_frames, void *const *outs, cons
     isti::ReprojChoice choice{};
     const isti_tuning *tuned = timewarp ? nullptr : find_tuning(r, infos[0].mode, r->last);
     if (tuned)
-        choice = {tuned->regs, tuned->row_pairs};
+        choice = {tuned->regs, tuned->row_pairs, tuned->plain_tiles};
     cudaEvent_t ev1 = ev ? ev[1] : nullptr, ev2 = ev ? ev[2] : nullptr;
     if (r->arith == ISTI_ARITH_REFERENCE_GPU)
         e = timewarp ? isti_fm_launch_timewarp(&r->last, base, stream, ev1, ev2)
-                     : isti_fm_launch_batch(&r->last, infos[0].mode, stream, ev1, ev2, choice.regs, choice.row_pairs);
+                     : isti_fm_launch_batch(&r->last, infos[0].mode, stream, ev1, ev2, choice.regs, choice.row_pairs, choice.plain_tiles);
     else
         e = timewarp ? isti::launch_timewarp(r->last, base, stream, ev1, ev2)
                      : isti::launch_batch(r->last, infos[0].mode, stream, ev1, ev2, choice);
@@ -510,8 +514,9 @@ isti_status isti_renderer_destroy(isti_renderer *r)
         cudaFree(r->learned_arena);
     if (r->multi_arena)
         cudaFree(r->multi_arena);
-    if (r->multi_host)
-        cudaFreeHost(r->multi_host);
+    for (void *h : r->multi_host)
+        if (h)
+            cudaFreeHost(h);
     if (r->multi_copied)
         cudaEventDestroy(r->multi_copied);
     if (r->arena)
@@ -752,6 +757,17 @@ bool pair_maps(const isti::FrameParams &p, isti::KeyMaps &km)
 }
 } // namespace
 
+extern "C" isti_status isti_renderer_set_pair_units(isti_renderer *r, int32_t splat_rows, int32_t init_unit_kib)
+{
+    if (!r)
+        return fail(ISTI_ERR_INVALID_ARG, "null renderer");
+    if (splat_rows < 0 || splat_rows > 256 || init_unit_kib < 0 || init_unit_kib > 4096 || (init_unit_kib && init_unit_kib < 16))
+        return fail(ISTI_ERR_INVALID_ARG, "splat rows must be 0..256 and the init unit 0 or 16..4096 KiB");
+    r->pair_splat_rows = splat_rows;
+    r->pair_init_kib = init_unit_kib;
+    return ISTI_OK;
+}
+
 extern "C" isti_status isti_render_pairs(isti_renderer *r, int32_t n_pairs, const isti_pair_frames *pairs, void *stream_ptr)
 {
     if (!r || !pairs)
@@ -802,6 +818,11 @@ extern "C" isti_status isti_render_pairs(isti_renderer *r, int32_t n_pairs, cons
     const size_t cnt_bytes = align_up(sizeof(uint32_t) * (2 + 2 * n_pairs), 256);
     const size_t block_bytes = fp_bytes + map_bytes + pair_bytes + seg_bytes + cnt_bytes;
     const size_t total = data_bytes + block_bytes;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if ((e = cudaStreamIsCapturing(stream, &cs)) != cudaSuccess)
+        return cuda_fail(e, "cudaStreamIsCapturing");
+    if (total > r->multi_bytes && cs != cudaStreamCaptureStatusNone)
+        return fail(ISTI_ERR_INVALID_ARG, "isti_render_pairs: make one call of this size outside a stream capture first");
     if (total > r->multi_bytes)
     {
         if (r->multi_arena)
@@ -813,26 +834,33 @@ extern "C" isti_status isti_render_pairs(isti_renderer *r, int32_t n_pairs, cons
             return e == cudaErrorMemoryAllocation ? fail(ISTI_ERR_OOM, "cudaMalloc of the multi-pair arena failed") : cuda_fail(e, "cudaMalloc");
         r->multi_bytes = total;
     }
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    if ((e = cudaStreamIsCapturing(stream, &cs)) != cudaSuccess)
-        return cuda_fail(e, "cudaStreamIsCapturing");
     if (!r->multi_copied && (e = cudaEventCreateWithFlags(&r->multi_copied, cudaEventDisableTiming)) != cudaSuccess)
         return cuda_fail(e, "cudaEventCreate");
-    if (cs == cudaStreamCaptureStatusNone && r->multi_host && (e = cudaEventSynchronize(r->multi_copied)) != cudaSuccess)
-        return cuda_fail(e, "waiting for the previous parameter copy");
-    if (block_bytes > r->multi_host_bytes)
+    // Two pinned staging buffers: uncaptured calls reuse theirs once the previous uncaptured
+    // call's copy is done; a captured call's copy reads its buffer whenever the graph runs, so
+    // captured calls have their own, sized by the uncaptured calls (no allocation in a capture)
+    // and overwritten only by the next captured call.
+    if (cs == cudaStreamCaptureStatusNone)
     {
-        if (r->multi_host)
-            cudaFreeHost(r->multi_host);
-        r->multi_host = nullptr;
-        r->multi_host_bytes = 0;
-        if ((e = cudaHostAlloc(&r->multi_host, block_bytes, cudaHostAllocDefault)) != cudaSuccess)
-            return cuda_fail(e, "cudaHostAlloc of the parameter staging");
-        r->multi_host_bytes = block_bytes;
+        if (r->multi_recorded && (e = cudaEventSynchronize(r->multi_copied)) != cudaSuccess)
+            return cuda_fail(e, "waiting for the previous parameter copy");
+        for (int i = 0; i < 2; i++)
+            if (block_bytes > r->multi_host_bytes[i])
+            {
+                if (r->multi_host[i])
+                    cudaFreeHost(r->multi_host[i]);
+                r->multi_host[i] = nullptr;
+                r->multi_host_bytes[i] = 0;
+                if ((e = cudaHostAlloc(&r->multi_host[i], block_bytes, cudaHostAllocDefault)) != cudaSuccess)
+                    return cuda_fail(e, "cudaHostAlloc of the parameter staging");
+                r->multi_host_bytes[i] = block_bytes;
+            }
     }
+    else if (block_bytes > r->multi_host_bytes[1])
+        return fail(ISTI_ERR_INVALID_ARG, "isti_render_pairs: make one call of this size outside a stream capture first");
     char *dbase = static_cast<char *>(r->multi_arena);
     char *dblock = dbase + data_bytes;
-    char *h = static_cast<char *>(r->multi_host);
+    char *h = static_cast<char *>(r->multi_host[cs == cudaStreamCaptureStatusNone ? 0 : 1]);
     std::memset(h, 0, block_bytes);
     auto *hfp = reinterpret_cast<isti::FrameParams *>(h);
     auto *hmaps = reinterpret_cast<CUtensorMap *>(h + fp_bytes);
@@ -842,6 +870,8 @@ extern "C" isti_status isti_render_pairs(isti_renderer *r, int32_t n_pairs, cons
     const auto *dmaps = reinterpret_cast<const CUtensorMap *>(dblock + fp_bytes);
     auto *dcnt = reinterpret_cast<uint32_t *>(dblock + fp_bytes + map_bytes + pair_bytes + seg_bytes);
     int32_t *dstatus = reinterpret_cast<int32_t *>(dcnt + 1 + 2 * n_pairs);
+    const uint32_t splat_rows = r->pair_splat_rows ? (uint32_t)r->pair_splat_rows : isti::BATCH_SPLAT_ROWS;
+    const uint32_t init_keys = r->pair_init_kib ? (uint32_t)r->pair_init_kib * 64u : isti::BATCH_INIT_UNIT_KEYS; // 16-byte units
     const int sw = isti::mode_window(mode);
     const int regs = isti::rule_regs(sw, nv);
     const unsigned nthreads = 32u * (unsigned)nv;
@@ -871,9 +901,9 @@ extern "C" isti_status isti_render_pairs(isti_renderer *r, int32_t n_pairs, cons
         bpair.fp = dfp + i;
         bpair.maps = dmaps + (size_t)i * isti::MAX_VIEWS;
         const size_t lut_need = (std::max(max_w, max_h) + nthreads - 1) / nthreads;
-        bpair.init_units = (uint32_t)std::max<size_t>((p.key_units + isti::BATCH_INIT_UNIT_KEYS - 1) / isti::BATCH_INIT_UNIT_KEYS, lut_need);
+        bpair.init_units = (uint32_t)std::max<size_t>((p.key_units + init_keys - 1) / init_keys, lut_need);
         bpair.splat_gx = (max_w + 31) / 32;
-        bpair.splat_gy = (max_h + isti::BATCH_SPLAT_ROWS - 1) / isti::BATCH_SPLAT_ROWS;
+        bpair.splat_gy = (max_h + splat_rows - 1) / splat_rows;
         bpair.splat_units = (uint32_t)nv * bpair.splat_gx * bpair.splat_gy;
         bpair.reproj_gx = (p.out_w + 31) / 32;
         const uint32_t block_rows = (uint32_t)(isti::ROWS * p.row_pairs);
@@ -906,11 +936,16 @@ extern "C" isti_status isti_render_pairs(isti_renderer *r, int32_t n_pairs, cons
     bp.spin_limit = 1u << 24; // with 128 ns sleeps: about two seconds
     bp.region_bytes = (uint32_t)region;
     bp.param_bytes = (uint32_t)isti::params_prefix(nv);
+    bp.splat_rows = splat_rows;
     const size_t smem = isti::batch_param_space(bp.param_bytes) + region + isti::BATCH_CTRL_BYTES;
     // counters to zero (in the staged block), then the block to the device, then the launch
     e = cudaMemcpyAsync(dblock, h, block_bytes, cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess)
-        e = cudaEventRecord(r->multi_copied, stream);
+    {
+        r->multi_recorded = cs == cudaStreamCaptureStatusNone;
+        if (r->multi_recorded)
+            e = cudaEventRecord(r->multi_copied, stream);
+    }
     if (e == cudaSuccess)
         e = launch_pairs_mode(mode, regs, bp, smem, (unsigned)nv, stream);
     if (e != cudaSuccess)

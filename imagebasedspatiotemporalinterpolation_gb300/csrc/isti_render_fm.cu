@@ -19,15 +19,16 @@
 size_t isti_fm_params_size() { return sizeof(isti_fm::FrameParams); }
 
 cudaError_t isti_fm_launch_batch(void *params, int mode, cudaStream_t stream, cudaEvent_t after_init, cudaEvent_t after_splat, int regs,
-                                 int row_pairs)
+                                 int row_pairs, int plain_tiles)
 {
     return isti_fm::launch_batch(*static_cast<isti_fm::FrameParams *>(params), mode, stream, after_init, after_splat,
-                                 isti_fm::ReprojChoice{regs, row_pairs});
+                                 isti_fm::ReprojChoice{regs, row_pairs, plain_tiles});
 }
 
-cudaError_t isti_fm_launch_reproj_mode(void *params, int mode, cudaStream_t stream, int regs, int row_pairs)
+cudaError_t isti_fm_launch_reproj_mode(void *params, int mode, cudaStream_t stream, int regs, int row_pairs, int plain_tiles)
 {
-    return isti_fm::launch_reproj_mode(*static_cast<isti_fm::FrameParams *>(params), mode, stream, isti_fm::ReprojChoice{regs, row_pairs});
+    return isti_fm::launch_reproj_mode(*static_cast<isti_fm::FrameParams *>(params), mode, stream,
+                                       isti_fm::ReprojChoice{regs, row_pairs, plain_tiles});
 }
 
 cudaError_t isti_fm_launch_timewarp(void *params, char *base, cudaStream_t stream, cudaEvent_t after_mean, cudaEvent_t after_nothing)

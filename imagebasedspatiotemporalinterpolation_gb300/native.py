@@ -70,7 +70,7 @@ class IstiTiming(C.Structure):
 class IstiTuning(C.Structure):
     _fields_ = [("mode", C.c_int32), ("n_views", C.c_int32), ("n_frames", C.c_int32), ("shadows", C.c_int32),
                 ("width", C.c_uint32), ("height", C.c_uint32), ("regs", C.c_int32), ("row_pairs", C.c_int32),
-                ("best_ms", C.c_float), ("rule_ms", C.c_float)]
+                ("best_ms", C.c_float), ("rule_ms", C.c_float), ("plain_tiles", C.c_int32)]
 
 
 class IstiPairFrames(C.Structure):
@@ -92,6 +92,7 @@ SIGNATURES = {
                                              C.POINTER(C.c_void_p), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     "isti_renderer_view_depth": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
     "isti_renderer_device_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "isti_renderer_set_pair_units": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "isti_renderer_enable_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "isti_renderer_timing": (C.c_int, [C.c_void_p, C.POINTER(IstiTiming)]),
     "isti_renderer_set_autotune": (C.c_int, [C.c_void_p, C.c_int32]),

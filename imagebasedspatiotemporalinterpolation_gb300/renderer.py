@@ -214,6 +214,10 @@ class Renderer:
         self._keep_pairs = (arr, keep)  # the structs must outlive the call
         check(self._lib.isti_render_pairs(self._h, len(jobs), arr, C.c_void_p(s)))
 
+    def set_pair_units(self, splat_rows: int = 0, init_unit_kib: int = 0) -> None:
+        """isti_renderer_set_pair_units: render_pairs' splat-unit rows and init-unit KiB (0: default)."""
+        check(self._lib.isti_renderer_set_pair_units(self._h, int(splat_rows), int(init_unit_kib)))
+
     def render_learned(self, render_buffers, infos, frame_data: DeviceFrame, net=None, iterations: int = 1, chain: bool = False,
                        stream=None) -> None:
         """isti_render_learned: the frames of one keyframe pair (main camera only) with the

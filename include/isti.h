@@ -160,10 +160,13 @@ isti_status isti_render_batch(isti_renderer *r, int32_t n_frames, void *const *o
  * pair are units of one cooperative kernel that takes them from a device work queue, the
  * next pair's initialisation and splatting ahead of the previous pair's reprojection.  All
  * pairs share the render mode (not timewarp) and the number of source views.
- * 1 <= n_pairs <= ISTI_MAX_PAIRS.  The kernel parameters travel through a pinned staging
- * buffer of the renderer: a call captured into a CUDA graph reads that buffer when the graph
- * runs, so make no other isti_render_pairs call on that renderer while the graph is in use.
- * isti_renderer_device_status reports the call's status word. */
+ * 1 <= n_pairs <= ISTI_MAX_PAIRS.  The kernel parameters travel through pinned staging
+ * buffers of the renderer, one for uncaptured and one for captured calls: a call captured
+ * into a CUDA graph reads its buffer when the graph runs, so capture no other
+ * isti_render_pairs call on that renderer while the graph is in use, and make one call of
+ * the same size outside any capture first (a capture allocates nothing; a larger one is
+ * refused with ISTI_ERR_INVALID_ARG).  isti_renderer_device_status reports the call's
+ * status word. */
 #define ISTI_MAX_PAIRS 64
 typedef struct isti_pair_frames
 {
@@ -174,6 +177,11 @@ typedef struct isti_pair_frames
     int32_t chain_outputs;
 } isti_pair_frames;
 isti_status isti_render_pairs(isti_renderer *r, int32_t n_pairs, const isti_pair_frames *pairs, void *stream);
+
+/* Work-unit sizes of isti_render_pairs on this renderer: source rows per splat unit
+ * (32 columns of one view, every frame; 1..256) and KiB of splat keys per init unit
+ * (16..4096); 0 keeps a default (32 rows, 256 KiB).  The output does not depend on them. */
+isti_status isti_renderer_set_pair_units(isti_renderer *r, int32_t splat_rows, int32_t init_unit_kib);
 
 /* Device pointers to the intermediates of the last render call for view
  * `view` (0 fwd, 1 bwd, 2+2i aux i curr, 3+2i aux i next; after a batch,
@@ -243,8 +251,8 @@ isti_status isti_renderer_timing(isti_renderer *r, isti_timing *out);
 /* Autotuning of the reprojection launch (no counterpart in the reference, which has one
  * launch shape).  With autotuning on, the first uncaptured render of each shape class
  * (mode, source views, frames per call, render size, shadows present) also times every
- * candidate launch of its reprojection -- register cap x output row pairs per block --
- * on the call's stream, waits for them (one host synchronisation per class), and the
+ * candidate launch of its reprojection -- register cap x output row pairs per block x
+ * key tiles staged by TMA copies or by plain loads -- on the call's stream, waits for them (one host synchronisation per class), and the
  * class's later renders, captured ones included, use the fastest.  Every candidate
  * computes the same result and the reprojection rewrites its outputs identically when
  * repeated, so the output does not depend on the choice.  Off (the default): a fixed
@@ -257,6 +265,7 @@ typedef struct isti_tuning
     uint32_t width, height;
     int32_t regs, row_pairs;                  /* the chosen launch: register cap, output row pairs per block */
     float best_ms, rule_ms;                   /* reprojection time of the choice and of the fixed rule */
+    int32_t plain_tiles;                      /* 1: key tiles by plain loads instead of TMA copies */
 } isti_tuning;
 
 /* Number of tuned shape classes, and the index-th of them (0-based, in tuning order). */

@@ -59,8 +59,9 @@ def test_sixteen_pairs_one_launch_equal_per_frame_calls(cuda):
     ref.close()
 
 
+@pytest.mark.parametrize("units", [(0, 0), (1, 16), (7, 48), (64, 1024)], ids=lambda u: f"rows{u[0]}-kib{u[1]}")
 @pytest.mark.parametrize("mode", [0, 1])
-def test_mixed_pairs_chained_equal_render_batch(cuda, mode):
+def test_mixed_pairs_chained_equal_render_batch(cuda, mode, units):
     import torch
     seqs = [scene.Sequence(320, 180, 3, seed=4200, aux_offsets=(-0.3, 0.3), shadows=True, max_speed=2.0),
             scene.Sequence(400, 240, 3, seed=4201, aux_offsets=(-0.3, 0.3), shadows=True, max_speed=2.0)]
@@ -77,11 +78,54 @@ def test_mixed_pairs_chained_equal_render_batch(cuda, mode):
         jobs.append(([prev.clone() for _ in clients], clients, frame))
         wants.append(want)
     r = Renderer()
+    r.set_pair_units(*units)
     r.render_pairs(jobs, chain=True)
     torch.cuda.synchronize()
     assert r.device_status() == native.ISTI_OK
     for i, ((outs, _, _), want) in enumerate(zip(jobs, wants)):
         for k, (a, b) in enumerate(zip(outs, want)):
             assert torch.equal(a, b), f"pair {i} frame {k}: {int((a != b).any(-1).sum())} pixels differ"
+    r.close()
+    ref.close()
+
+
+def test_graph_capture_and_uncaptured_calls_alternate(cuda):
+    """A captured isti_render_pairs call replays with its own parameters after uncaptured calls
+    of the same renderer with other parameters (separate staging buffers)."""
+    import torch
+    seq = scene.Sequence(320, 180, 4, seed=4300)
+    jobs_a, jobs_b = [], []
+    for k, jobs in ((0, jobs_a), (1, jobs_b)):
+        clients = [seq.client(k, b) for b in (1, 2, 3)]
+        jobs.append(([torch.zeros((180, 320, 4), dtype=torch.uint8, device="cuda") for _ in clients], clients,
+                     DeviceFrame.from_host(seq.frame(k))))
+    ref = Renderer()
+    want = {}
+    for name, jobs in (("a", jobs_a), ("b", jobs_b)):
+        outs, clients, frame = jobs[0]
+        w = [torch.zeros_like(o) for o in outs]
+        ref.render_batch(w, clients, frame, chain=False)
+        want[name] = w
+    r = Renderer()
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        r.render_pairs(jobs_a, stream=stream)          # sizes the arena and both staging buffers
+    stream.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        with torch.cuda.graph(graph, stream=stream):
+            r.render_pairs(jobs_a, stream=stream)
+    for _ in range(2):
+        for o in jobs_a[0][0] + jobs_b[0][0]:
+            o.zero_()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            r.render_pairs(jobs_b, stream=stream)      # uncaptured, other parameters
+            graph.replay()                             # must still render pair a
+        stream.synchronize()
+        assert r.device_status() == native.ISTI_OK
+        for got, exp in ((jobs_a[0][0], want["a"]), (jobs_b[0][0], want["b"])):
+            for a, b in zip(got, exp):
+                assert torch.equal(a, b)
     r.close()
     ref.close()
