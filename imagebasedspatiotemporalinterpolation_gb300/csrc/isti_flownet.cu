@@ -14,6 +14,7 @@
 //   s1 = up2(conv1x1 64->32 (d2)) + e1     d1 = relu(conv3x3 32->32)(s1)
 //   flow = conv1x1 32->4 (d1)              [H,W,4] f32
 // 10 tensor-core layers + the head: 339,268 parameters.
+#include "isti_tc.cuh"
 #include "isti_unet.h"
 #include "isti_unet_ops.h"
 #include "host/isti_error.hpp"
@@ -84,6 +85,8 @@ __device__ __forceinline__ uint4 pack8(const float (&f)[8])
 // y[n, h/2, w/2] = mean of the 2x2 block of x[n, h, w]
 __global__ void pool_kernel(const bf16 *x, int n, int h, int w, int c, bf16 *y)
 {
+    isti_tc::griddep_launch_dependents();
+    isti_tc::griddep_wait();
     const int cg = c / 8, ho = h / 2, wo = w / 2;
     const size_t total = (size_t)n * ho * wo * cg;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
@@ -114,6 +117,8 @@ __global__ void pool_kernel(const bf16 *x, int n, int h, int w, int c, bf16 *y)
 // s[n, h, w] = a[n, h/2, w/2] (nearest upsampling) + b[n, h, w]
 __global__ void upadd_kernel(const bf16 *a, const bf16 *b, int n, int h, int w, int c, bf16 *s)
 {
+    isti_tc::griddep_launch_dependents();
+    isti_tc::griddep_wait();
     const int cg = c / 8;
     const size_t total = (size_t)n * h * w * cg;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
@@ -227,6 +232,8 @@ __global__ void head_kernel(const bf16 *d1, size_t npix, const float *hw, const 
         sw[i] = hw[i];
     if (threadIdx.x < HEAD_COUT)
         sw[HEAD_COUT * HEAD_CIN + threadIdx.x] = hb[threadIdx.x];
+    isti_tc::griddep_launch_dependents();
+    isti_tc::griddep_wait(); // the weights above are no previous kernel's output; d1 is
     __syncthreads();
     for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += (size_t)gridDim.x * blockDim.x)
     {
@@ -236,7 +243,7 @@ __global__ void head_kernel(const bf16 *d1, size_t npix, const float *hw, const 
         for (int q = 0; q < HEAD_CIN / 8; q++)
         {
             float t[8];
-            unpack8(__ldg(src + q), t);
+            unpack8(src[q], t); // plain load: written by the previous kernel, which may still run at launch
 #pragma unroll
             for (int k = 0; k < 8; k++)
                 f[8 * q + k] = t[k];
@@ -488,11 +495,11 @@ isti_status repack(isti_flownet *net, cudaStream_t s)
     return ISTI_OK;
 }
 
-isti_status conv(isti_flownet *net, int l, const bf16 *x, int n, int h, int w, const bf16 *mask, bf16 *out, cudaStream_t s)
+isti_status conv(isti_flownet *net, int l, const bf16 *x, int n, int h, int w, const bf16 *mask, bf16 *out, cudaStream_t s, bool pdl = false)
 {
     const LayerDef &d = LAYERS[l];
     return isti_unet::conv_launch(d.taps, x, n, h, w, d.cin, net->packs + net->pk_off[l], net->params + net->b_off[l], mask, d.relu, out, d.cout,
-                                  net->status, s);
+                                  net->status, s, pdl);
 }
 
 // data gradient of layer l: g_in = conv(g_out, W^T flipped), masked by (mask > 0) when given
@@ -525,29 +532,44 @@ isti_status wgrad(isti_flownet *net, int l, const bf16 *g_out, const bf16 *x, in
             return st_;                                                                                                                         \
     } while (0)
 
-isti_status forward(isti_flownet *net, const bf16 *x0, int n, int h, int w, Buffers &b, float *flow, __half *flow16, cudaStream_t s)
+// pdl: every launch after the first is a programmatic dependent of the one before (each
+// kernel sets up while its predecessor finishes; inference only)
+isti_status forward(isti_flownet *net, const bf16 *x0, int n, int h, int w, Buffers &b, float *flow, __half *flow16, cudaStream_t s,
+                    bool pdl = false)
 {
+    using isti_unet::launch_kernel;
     const int h2 = h / 2, w2 = w / 2, h4 = h / 4, w4 = w / 4, h8 = h / 8, w8 = w / 8;
-    ISTI_TRY(conv(net, 0, x0, n, h, w, nullptr, b.e1, s));
-    pool_kernel<<<grid_for((size_t)n * h2 * w2 * 4), 256, 0, s>>>(b.e1, n, h, w, 32, b.q1);
-    ISTI_TRY(conv(net, 1, b.q1, n, h2, w2, nullptr, b.e2, s));
-    pool_kernel<<<grid_for((size_t)n * h4 * w4 * 8), 256, 0, s>>>(b.e2, n, h2, w2, 64, b.q2);
-    ISTI_TRY(conv(net, 2, b.q2, n, h4, w4, nullptr, b.e3, s));
-    pool_kernel<<<grid_for((size_t)n * h8 * w8 * 12), 256, 0, s>>>(b.e3, n, h4, w4, 96, b.q3);
-    ISTI_TRY(conv(net, 3, b.q3, n, h8, w8, nullptr, b.e4, s));
-    ISTI_TRY(conv(net, 4, b.e4, n, h8, w8, nullptr, b.p3, s));
-    upadd_kernel<<<grid_for((size_t)n * h4 * w4 * 12), 256, 0, s>>>(b.p3, b.e3, n, h4, w4, 96, b.s3);
-    ISTI_TRY(conv(net, 5, b.s3, n, h4, w4, nullptr, b.d3, s));
-    ISTI_TRY(conv(net, 6, b.d3, n, h4, w4, nullptr, b.p2, s));
-    upadd_kernel<<<grid_for((size_t)n * h2 * w2 * 8), 256, 0, s>>>(b.p2, b.e2, n, h2, w2, 64, b.s2);
-    ISTI_TRY(conv(net, 7, b.s2, n, h2, w2, nullptr, b.d2, s));
-    ISTI_TRY(conv(net, 8, b.d2, n, h2, w2, nullptr, b.p1, s));
-    upadd_kernel<<<grid_for((size_t)n * h * w * 4), 256, 0, s>>>(b.p1, b.e1, n, h, w, 32, b.s1);
-    ISTI_TRY(conv(net, 9, b.s1, n, h, w, nullptr, b.d1, s));
+    const dim3 blk(256);
+    cudaError_t e = cudaSuccess;
+    auto ok = [&](cudaError_t x) {
+        if (e == cudaSuccess)
+            e = x;
+        return e == cudaSuccess;
+    };
+    ISTI_TRY(conv(net, 0, x0, n, h, w, nullptr, b.e1, s, pdl));
+    ok(launch_kernel(pool_kernel, dim3(grid_for((size_t)n * h2 * w2 * 4)), blk, 0, s, pdl, (const bf16 *)b.e1, n, h, w, 32, b.q1));
+    ISTI_TRY(conv(net, 1, b.q1, n, h2, w2, nullptr, b.e2, s, pdl));
+    ok(launch_kernel(pool_kernel, dim3(grid_for((size_t)n * h4 * w4 * 8)), blk, 0, s, pdl, (const bf16 *)b.e2, n, h2, w2, 64, b.q2));
+    ISTI_TRY(conv(net, 2, b.q2, n, h4, w4, nullptr, b.e3, s, pdl));
+    ok(launch_kernel(pool_kernel, dim3(grid_for((size_t)n * h8 * w8 * 12)), blk, 0, s, pdl, (const bf16 *)b.e3, n, h4, w4, 96, b.q3));
+    ISTI_TRY(conv(net, 3, b.q3, n, h8, w8, nullptr, b.e4, s, pdl));
+    ISTI_TRY(conv(net, 4, b.e4, n, h8, w8, nullptr, b.p3, s, pdl));
+    ok(launch_kernel(upadd_kernel, dim3(grid_for((size_t)n * h4 * w4 * 12)), blk, 0, s, pdl, (const bf16 *)b.p3, (const bf16 *)b.e3, n, h4, w4,
+                     96, b.s3));
+    ISTI_TRY(conv(net, 5, b.s3, n, h4, w4, nullptr, b.d3, s, pdl));
+    ISTI_TRY(conv(net, 6, b.d3, n, h4, w4, nullptr, b.p2, s, pdl));
+    ok(launch_kernel(upadd_kernel, dim3(grid_for((size_t)n * h2 * w2 * 8)), blk, 0, s, pdl, (const bf16 *)b.p2, (const bf16 *)b.e2, n, h2, w2,
+                     64, b.s2));
+    ISTI_TRY(conv(net, 7, b.s2, n, h2, w2, nullptr, b.d2, s, pdl));
+    ISTI_TRY(conv(net, 8, b.d2, n, h2, w2, nullptr, b.p1, s, pdl));
+    ok(launch_kernel(upadd_kernel, dim3(grid_for((size_t)n * h * w * 4)), blk, 0, s, pdl, (const bf16 *)b.p1, (const bf16 *)b.e1, n, h, w, 32,
+                     b.s1));
+    ISTI_TRY(conv(net, 9, b.s1, n, h, w, nullptr, b.d1, s, pdl));
     if (flow || flow16)
-        head_kernel<<<grid_for((size_t)n * h * w), 256, 0, s>>>(b.d1, (size_t)n * h * w, net->params + net->w_off[N_CONV],
-                                                                  net->params + net->b_off[N_CONV], flow, flow16);
-    const cudaError_t e = cudaGetLastError();
+        ok(launch_kernel(head_kernel, dim3(grid_for((size_t)n * h * w)), blk, 0, s, pdl, (const bf16 *)b.d1, (size_t)n * h * w,
+                         (const float *)(net->params + net->w_off[N_CONV]), (const float *)(net->params + net->b_off[N_CONV]), flow, flow16));
+    if (e == cudaSuccess)
+        e = cudaGetLastError();
     return e == cudaSuccess ? ISTI_OK : cuda_fail(e, "flownet forward");
 }
 
@@ -742,7 +764,8 @@ isti_status isti_flownet_forward(isti_flownet *net, const void *x, int32_t n, in
     ISTI_TRY(check_shape(x, n, h, w));
     Buffers b{};
     ISTI_TRY(ensure_arena(net, n, h, w, b));
-    return forward(net, static_cast<const bf16 *>(x), n, h, w, b, flow, static_cast<__half *>(flow_f16), static_cast<cudaStream_t>(stream));
+    return forward(net, static_cast<const bf16 *>(x), n, h, w, b, flow, static_cast<__half *>(flow_f16), static_cast<cudaStream_t>(stream),
+                   true);
 }
 
 isti_status isti_flownet_backward(isti_flownet *net, const void *x, const float *label, int32_t n, int32_t h, int32_t w, void *stream)

@@ -32,6 +32,17 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
 
 __device__ __forceinline__ void fence_barrier_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
+// Programmatic dependent launch (PTX griddepcontrol).  A kernel launched with
+// cudaLaunchAttributeProgrammaticStreamSerialization may start while the previous kernel of
+// its stream is still running, once every block of that kernel has called
+// griddep_launch_dependents() (or exited).  griddep_wait() returns when the previous kernel
+// has completed and its writes are visible; for a launch without the attribute it returns at
+// once.  A kernel touches nothing the previous one writes or reads before its wait.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+// after griddep_wait, before TMA reads of what the previous kernel wrote (generic -> async proxy)
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
 {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");

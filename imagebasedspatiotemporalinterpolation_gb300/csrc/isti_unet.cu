@@ -162,7 +162,7 @@ namespace isti_unet
 {
 // Launch of conv_kernel<taps> (shared with the network code in isti_flownet.cu).
 isti_status conv_launch(int taps, const void *x, int n, int h, int w, int cin, const void *wpack, const float *bias, const void *mask, int relu,
-                        void *out, int cout, int32_t *status, cudaStream_t stream)
+                        void *out, int cout, int32_t *status, cudaStream_t stream, bool pdl)
 {
     if ((taps != 9 && taps != 1) || n < 1 || h < 1 || w < 1 || cin % 16 || cout % 16 || cout < 16 || cout > 256 || !x || !wpack || !out)
         return isti::set_error(ISTI_ERR_INVALID_ARG, "isti_unet_conv: bad shape or NULL buffer");
@@ -208,9 +208,7 @@ isti_status conv_launch(int taps, const void *x, int n, int h, int w, int cin, c
             const int grid = std::min(units, sm_count() * per_sm);
             cudaError_t e = smem_limit(row_conv_kernel<0>, smem);
             if (e == cudaSuccess)
-                row_conv_kernel<0><<<(unsigned)grid, PCONV_THREADS, smem, stream>>>(p, xmap);
-            if (e == cudaSuccess)
-                e = cudaGetLastError();
+                e = launch_kernel(row_conv_kernel<0>, dim3((unsigned)grid), dim3(PCONV_THREADS), smem, stream, pdl, p, xmap);
             return e == cudaSuccess ? ISTI_OK : cuda_fail(e, "isti_unet_conv launch");
         }
     }
@@ -231,13 +229,13 @@ isti_status conv_launch(int taps, const void *x, int n, int h, int w, int cin, c
     {
         e = smem_limit(conv_kernel<9>, smem);
         if (e == cudaSuccess)
-            conv_kernel<9><<<(unsigned)grid, PCONV_THREADS, smem, stream>>>(p, xmap);
+            e = launch_kernel(conv_kernel<9>, dim3((unsigned)grid), dim3(PCONV_THREADS), smem, stream, pdl, p, xmap);
     }
     else
     {
         e = smem_limit(conv_kernel<1>, smem);
         if (e == cudaSuccess)
-            conv_kernel<1><<<(unsigned)grid, PCONV_THREADS, smem, stream>>>(p, xmap);
+            e = launch_kernel(conv_kernel<1>, dim3((unsigned)grid), dim3(PCONV_THREADS), smem, stream, pdl, p, xmap);
     }
     if (e == cudaSuccess)
         e = cudaGetLastError();

@@ -122,9 +122,13 @@ __global__ void __launch_bounds__(PCONV_THREADS, 1) conv_kernel(const __grid_con
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
     const int chunks = p.cin / p.ck, iters = TAPS * chunks;
+    if (threadIdx.x == 0)
+        griddep_launch_dependents(); // the next layer may set up while this one runs
 
     if (warp == 0 && lane == 0)
     {
+        griddep_wait(); // the previous layer's output is complete (every load below is later)
+        fence_proxy_async_global();
         uint32_t g = 0;
         bool stop = false;
         for (int t = blockIdx.x; t < p.n_tiles && !stop; t += gridDim.x)
@@ -331,11 +335,15 @@ __global__ void __launch_bounds__(PCONV_THREADS, 1) row_conv_kernel(const __grid
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
+    if (threadIdx.x == 0)
+        griddep_launch_dependents(); // the next layer may set up while this one runs
     if (warp == 0 && lane == 0)
     {
         mbar_expect_tx(wbar, w_bytes);
-        for (uint32_t o = 0; o < w_bytes; o += 32768u) // pieces of at most 32 KiB
+        for (uint32_t o = 0; o < w_bytes; o += 32768u) // pieces of at most 32 KiB (weights: no previous kernel writes them)
             bulk_load(wsm + o, reinterpret_cast<const uint8_t *>(p.wpack) + o, min(32768u, w_bytes - o), wbar);
+        griddep_wait(); // the previous layer's output is complete (every activation load below is later)
+        fence_proxy_async_global();
         uint32_t g = 0;
         bool stop = false;
         for (int u = blockIdx.x; u < n_units && !stop; u += gridDim.x)

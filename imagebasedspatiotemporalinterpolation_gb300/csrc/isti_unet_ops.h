@@ -8,11 +8,32 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <utility>
 
 namespace isti_unet
 {
+// pdl: launch as a programmatic dependent of the previous kernel in `stream` (it prepares
+// while that kernel finishes; see griddep_wait in isti_tc.cuh)
 isti_status conv_launch(int taps, const void *x, int n, int h, int w, int cin, const void *wpack, const float *bias, const void *mask, int relu,
-                        void *out, int cout, int32_t *status, cudaStream_t stream);
+                        void *out, int cout, int32_t *status, cudaStream_t stream, bool pdl = false);
+
+// <<<grid, block, smem, stream>>> with, when `pdl`, the programmatic-dependent-launch
+// attribute; the kernel must call griddep_wait before it touches the previous kernel's data
+template <typename... K, typename... A>
+cudaError_t launch_kernel(void (*kernel)(K...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream, bool pdl, A &&...args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = pdl ? attr : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
 isti_status wgrad_launch(int taps, const void *dy, const void *x, int n, int h, int w, int cin, int cout, float *dw, int accumulate, void *scratch,
                          size_t scratch_bytes, int32_t *status, cudaStream_t stream);
 isti_status pack_launch(int taps, const float *w, int cin, int cout, int transpose, void *wpack, cudaStream_t stream);
