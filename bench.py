@@ -75,7 +75,7 @@ def parse():
                     help="real time of the serving loop under pressure (more clients than the budget admits)")
     ap.add_argument("--no-pressure", action="store_true", help="skip the serving loop under pressure")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-initialiser comparison")
-    ap.add_argument("--no-config1", action="store_true", help="skip the 640x360 configuration")
+    ap.add_argument("--no-small-frame", action="store_true", help="skip the 640x360 single-frame timing")
     ap.add_argument("--no-reference-gpu", action="store_true", help="skip timing the reference's own GPU build")
     ap.add_argument("--no-arith-compare", action="store_true",
                     help="skip timing the same steps under IEEE arithmetic (the line itself uses the reference's GPU arithmetic)")
@@ -387,9 +387,9 @@ def main_ours(args):
         if not args.no_pressure:
             serving["pressure"] = run_serving(args, dev, rank, pressure=True)
 
-    # ---- learned initialiser vs plain at 1080p, configuration 1, the reference's own GPU build
+    # ---- learned initialiser vs plain at 1080p, one 640x360 frame per call, the reference's own GPU build
     learned = None if args.no_learned else run_learned(args, dev, rank)
-    config1 = None if args.no_config1 else run_config1(args, dev, rank)
+    small_frame = None if args.no_small_frame else run_small_frame(args, dev, rank)
     reference_gpu = None
     if rank == 0 and not args.no_reference_gpu:
         reference_gpu = run_reference_gpu(args, dev, seq, per_frame["p50_frame_ms"] if per_frame else None)
@@ -477,7 +477,7 @@ def main_ours(args):
             "per_frame_api": per_frame,
             "arith_ieee": arith,
             "learned_vs_plain": learned,
-            "config1": config1,
+            "frame_640x360": small_frame,
             "reference_gpu": reference_gpu,
             "graph_batch_mixed": graph_batch,
             "serving": serving,
@@ -508,19 +508,19 @@ def run_reference_gpu(args, dev, seq, ours_frame_ms):
     if not oracle.reference_gpu_available():
         return {"unavailable": "reference sources not staged (oracle/build_ref.py needs the reference tree)"}
     out = {}
-    for name, (sq, ts) in {"config2_1080p_6views_shadows": (seq, TS)}.items():
+    for name, (sq, ts) in {"frame_1080p_6views_shadows": (seq, TS)}.items():
         frame = sq.frame(0)
         ms = oracle.time_reference_gpu(frame, [sq.client(0, b) for b in ts], warmup=max(3, args.warmup), repeats=10)
         p50 = float(np.median(ms))
         out[name] = {"ms_per_frame_p50": round(p50, 4), "ms_per_frame_p99": round(float(np.percentile(ms, 99)), 4),
                      "mpix_s": round(sq.width * sq.height / 1e6 / (p50 / 1e3), 2), "frames_timed": int(ms.size)}
-    out["config2_1080p_6views_shadows"]["ours_per_frame_call_ms_p50"] = ours_frame_ms
+    out["frame_1080p_6views_shadows"]["ours_per_frame_call_ms_p50"] = ours_frame_ms
     out["build"] = "src/renderer.cu unmodified, nvcc -arch sm_103a -use_fast_math --expt-relaxed-constexpr (CMakeLists.txt:36)"
     return out
 
 
-def run_config1(args, dev, rank):
-    """Benchmark configuration 1: one interpolated frame at t = 0.5 between two 640x360
+def run_small_frame(args, dev, rank):
+    """One interpolated frame at t = 0.5 between two 640x360
     keyframes, main camera only, mode 0, no shadows.  Device-resident keyframes, one
     isti_render call per step on 5 resident pairs in turn; the reference GPU build and the
     CPU port (the C oracle, all threads) timed on the same frames."""
@@ -571,7 +571,7 @@ def run_config1(args, dev, rank):
 
 
 def run_learned(args, dev, rank):
-    """Learned initialiser vs the plain method (benchmark configuration 4's evaluation):
+    """Learned initialiser vs the plain method (held-out scenes of its training distribution):
     1920x1080 held-out seeds of the training distribution (U[16, 256] spheres, |v| <= 1
     m/s, camera rotation <= 5 degrees per keyframe interval), main camera only, t in
     {0.25, 0.5, 0.75}.  Per step one call renders the 3 frames of a keyframe pair: the plain

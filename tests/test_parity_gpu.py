@@ -2,7 +2,7 @@
 
 Bar: bit-exact.  The output image, every 64-bit splat key and every flow-field
 float must equal the reference renderer's (golden fixtures) and the C oracle's
-(live, seeded scenes at the benchmark sizes).  The benchmark spec's tolerance (colour
+(live, seeded scenes at the benchmark sizes).  The parity tolerance (colour
 within 1/255 per channel, >= 60 dB PSNR) is implied and asserted as well.
 """
 import numpy as np
@@ -17,7 +17,7 @@ from tests.golden import fixtures
 
 pytestmark = pytest.mark.gpu
 
-TOL_PER_CHANNEL = 1      # 1/255 per channel (spec bound; the kernels are bit-exact)
+TOL_PER_CHANNEL = 1      # 1/255 per channel (the parity bound; the kernels are bit-exact)
 TOL_PSNR_DB = 60.0
 
 
@@ -100,7 +100,7 @@ def test_timewarp_matches_oracle_1080p(cuda, aux):
 @pytest.mark.parametrize("mode", [0, 1, 2, 3])
 @pytest.mark.parametrize("b", [1, 2, 3])
 def test_oracle_parity_640x360_main_only(cuda, mode, b):
-    """Plain method at 640x360, main camera only, shadows off (config 1 inputs)."""
+    """Plain method at 640x360, main camera only, shadows off."""
     seq = Sequence(640, 360, 2, seed=101)
     frame, client = seq.frame(0), seq.client(0, b, mode=mode)
     prev = np.zeros((360, 640, 4), np.uint8)
@@ -110,7 +110,7 @@ def test_oracle_parity_640x360_main_only(cuda, mode, b):
 
 @pytest.mark.parametrize("b", [1, 2, 3])
 def test_oracle_parity_1080p_aux_shadows(cuda, b):
-    """1920x1080, left/right aux cameras at +-0.3 m (6 source views), soft shadows (config 2 inputs)."""
+    """1920x1080, left/right aux cameras at +-0.3 m (6 source views), soft shadows."""
     seq = Sequence(1920, 1080, 2, seed=202, aux_offsets=(-0.3, 0.3), shadows=True)
     frame, client = seq.frame(0), seq.client(0, b)
     prev = np.zeros((1080, 1920, 4), np.uint8)

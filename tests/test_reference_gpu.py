@@ -8,7 +8,7 @@ cameras), and the test compares:
 
 * ISTI_ARITH_REFERENCE_GPU (the kernels under the reference's GPU arithmetic):
   every 64-bit splat key (so every winning source index), every flow-field
-  float and every output pixel bit-exact -- beyond the spec bar of
+  float and every output pixel bit-exact -- beyond the parity bar of
   bit-exact indices, colour within 1/255 per channel and >= 60 dB;
 * ISTI_ARITH_IEEE (correctly rounded, the CPU oracle's arithmetic): the
   rounding differences move a few winning indices; their counts are reported
@@ -66,10 +66,10 @@ def render(frame, client, prev, arith):
 
 
 CASES = {
-    # benchmark configuration 1: 640x360, main camera only, mode 0, no shadows
-    "c1": dict(size=(640, 360), aux=(), shadows=False, seed=101),
-    # benchmark configuration 2: 1920x1080, aux cameras at +-0.3 m, soft shadows
-    "c2": dict(size=(1920, 1080), aux=(-0.3, 0.3), shadows=True, seed=202),
+    # 640x360, main camera only, mode 0, no shadows
+    "s640": dict(size=(640, 360), aux=(), shadows=False, seed=101),
+    # 1920x1080, aux cameras at +-0.3 m, soft shadows
+    "f1080": dict(size=(1920, 1080), aux=(-0.3, 0.3), shadows=True, seed=202),
     # every render mode with aux cameras and shadows at a small size
     "modes": dict(size=(400, 240), aux=(-0.3, 0.3), shadows=True, seed=303),
 }
@@ -78,8 +78,8 @@ CASES = {
 def _cases():
     out = []
     for b in (1, 2, 3):
-        out.append(("c1", b, 0))
-        out.append(("c2", b, 0))
+        out.append(("s640", b, 0))
+        out.append(("f1080", b, 0))
     for mode in (1, 2, 3):
         out.append(("modes", 2, mode))
     return out
@@ -116,7 +116,7 @@ def test_reference_gpu_semantics_bit_exact(cuda, ref_gpu, case, b, mode):
         assert np.array_equal(a.view(np.uint32), e.view(np.uint32)), f"view {k}: full_ff differs"
 
 
-@pytest.mark.parametrize("case,b", [("c1", 2), ("c2", 2)])
+@pytest.mark.parametrize("case,b", [("s640", 2), ("f1080", 2)])
 def test_ieee_mode_against_reference_gpu_build(cuda, ref_gpu, case, b):
     """The correctly rounded mode differs from the fast-math build only by rounding:
     bounded winning-index mismatches, flows within a few ulp of the NDC range."""
