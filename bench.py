@@ -527,16 +527,19 @@ def run_small_frame(args, dev, rank):
     import numpy as np
     import torch
 
-    from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame, Renderer
+    from imagebasedspatiotemporalinterpolation_gb300 import native
+    from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame, Renderer, render_info
     from imagebasedspatiotemporalinterpolation_gb300.scene import Sequence
     import oracle
 
     w, h, pairs = 640, 360, 5
     seq = Sequence(w, h, pairs + 1, seed=args.seed + 11 + rank)
     frames = [DeviceFrame.from_host(seq.frame(p), dev) for p in range(pairs)]
-    clients = [seq.client(p, 2) for p in range(pairs)]
+    host_clients = [seq.client(p, 2) for p in range(pairs)]
+    clients = [render_info(c) for c in host_clients]  # marshalled once, like the main line's
     out = torch.zeros((h, w, 4), dtype=torch.uint8, device=dev)
     r = Renderer()
+    r.set_arithmetic(native.ARITH_REFERENCE_GPU)  # as the reference GPU build timed beside it
     for s in range(max(3, args.warmup)):
         r.render(out, clients[s % pairs], frames[s % pairs])
     n = max(60, args.steps * 3)
@@ -548,17 +551,43 @@ def run_small_frame(args, dev, rank):
         b.record()
     torch.cuda.synchronize()
     ms = sorted(a.elapsed_time(b) for a, b in ev)
+    r.timing()
+    r.enable_timing(True)           # a second pass for the per-kernel split (its events cost host time)
+    for s in range(n):
+        r.render(out, clients[s % pairs], frames[s % pairs])
+    torch.cuda.synchronize()
+    r.enable_timing(False)
+    tim = r.timing()
+    # the same calls replayed from one CUDA graph: the device time without the host's per-call work
+    stream = torch.cuda.Stream(dev)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        with torch.cuda.graph(graph, stream=stream):
+            for s in range(pairs):
+                r.render(out, clients[s], frames[s], stream)
+        graph.replay()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        for _ in range(n // pairs):
+            graph.replay()
+        g1.record(stream)
+    torch.cuda.synchronize()
+    graph_ms = g0.elapsed_time(g1) / ((n // pairs) * pairs)
     r.close()
     res = {"workload": "640x360, main camera only, t = 0.5, mode 0, no shadows (one isti_render call per frame)",
+           "arithmetic": "reference GPU (fast-math)",
            "mpix_s": round(n * w * h / 1e6 / (sum(ms) / 1e3), 2), "p50_frame_ms": round(ms[len(ms) // 2], 4),
-           "p99_frame_ms": round(ms[min(len(ms) - 1, int(0.99 * len(ms)))], 4)}
+           "p99_frame_ms": round(ms[min(len(ms) - 1, int(0.99 * len(ms)))], 4),
+           "kernels_ms_per_frame": {"key_init": round(tim["init_ms"] / n, 4), "splat_kernel": round(tim["splat_ms"] / n, 4),
+                                    "reproj_kernel": round(tim["reproj_ms"] / n, 4)},
+           "graph_replayed_ms_per_frame": round(graph_ms, 4)}
     if rank == 0 and oracle.reference_gpu_available():
-        rg = oracle.time_reference_gpu(seq.frame(0), [clients[0]], warmup=5, repeats=30)
+        rg = oracle.time_reference_gpu(seq.frame(0), [host_clients[0]], warmup=5, repeats=30)
         res["reference_gpu_ms_per_frame_p50"] = round(float(np.median(rg)), 4)
     if rank == 0 and not args.no_cpu_baseline:
         oracle.build()
         fr = seq.frame(0)
-        call = oracle.prepared_call(fr, clients[0], np.zeros((h, w, 4), np.uint8))
+        call = oracle.prepared_call(fr, host_clients[0], np.zeros((h, w, 4), np.uint8))
         call()
         t0, k = time.perf_counter(), 0
         while time.perf_counter() - t0 < min(args.cpu_seconds, 5.0) or k == 0:

@@ -110,7 +110,34 @@ cudaError_t launch_reproj_regs(isti::FrameParams &p, cudaStream_t stream, int ro
         return e;
     p.row_pairs = row_pairs > 0 ? std::min(row_pairs, 3) : rule_row_pairs(p.n_views, p.n_frames);
     static thread_local isti::KeyMaps km; // 2 KiB, passed by value as a kernel parameter
-    p.use_tma = (!plain_tiles && make_key_maps<SW>(p, km)) ? 1 : 0;
+    // the maps depend only on the key buffers' addresses and shapes: encode them again only
+    // when those changed (a renderer reuses its arena from call to call)
+    struct MapsKey
+    {
+        const void *splat[isti::MAX_VIEWS];
+        uint32_t w[isti::MAX_VIEWS], h[isti::MAX_VIEWS];
+        size_t key_stride;
+        int n_views, n_frames;
+        bool operator==(const MapsKey &) const = default;
+    };
+    static thread_local MapsKey last{};
+    static thread_local int last_tma = -1; // -1: nothing cached
+    MapsKey key{};
+    for (int k = 0; k < p.n_views; k++)
+    {
+        key.splat[k] = p.v[k].splat;
+        key.w[k] = p.v[k].w;
+        key.h[k] = p.v[k].h;
+    }
+    key.key_stride = p.key_stride;
+    key.n_views = p.n_views;
+    key.n_frames = p.n_frames;
+    if (last_tma < 0 || !(key == last))
+    {
+        last_tma = make_key_maps<SW>(p, km) ? 1 : 0;
+        last = key;
+    }
+    p.use_tma = (!plain_tiles && last_tma == 1) ? 1 : 0;
     const size_t smem = isti::reproj_smem<SW>(p.n_views, p.n_frames * p.row_pairs);
     const uint32_t block_rows = (uint32_t)(isti::ROWS * p.row_pairs);
     const dim3 gr((p.out_w + 31) / 32, (p.out_h + block_rows - 1) / block_rows);
