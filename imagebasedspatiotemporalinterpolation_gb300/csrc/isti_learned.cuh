@@ -222,7 +222,9 @@ __device__ __forceinline__ void learned_step_approx(const LearnedParams &p, int 
 
 // One thread per output pixel handles every frame of the call (a pixel's sources for the
 // frames lie close together: the keyframe data stay in L1), both keyframes interleaved.
-__global__ void __launch_bounds__(LT_W *LT_H) learned_kernel(const __grid_constant__ LearnedParams p)
+// 6 blocks of 256 threads per SM (40 registers, no spills) instead of 5 at the natural 48:
+// the kernel waits on dependent gathers, so resident warps count
+__global__ void __launch_bounds__(LT_W *LT_H, 6) learned_kernel(const __grid_constant__ LearnedParams p)
 {
     const uint32_t x = blockIdx.x * LT_W + threadIdx.x, y = blockIdx.y * LT_H + threadIdx.y;
     const bool inb = x < p.fp.out_w && y < p.fp.out_h;
