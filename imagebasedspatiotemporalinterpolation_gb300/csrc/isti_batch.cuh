@@ -33,6 +33,7 @@ struct BatchPair
     const FrameParams *fp;     // device copy of the pair's kernel parameters
     const CUtensorMap *maps;   // device copy of its key-tile tensor maps (n_views of them)
     uint32_t init_units, splat_units, reproj_units;
+    uint32_t splat_need;       // splat units a reprojection unit waits for (splat_units; more under a test hook)
     uint32_t reproj_gx;        // reprojection blocks per block row
     uint32_t splat_gx, splat_gy; // splat units per view: columns of 32, rows of BatchParams::splat_rows
 };
@@ -148,7 +149,7 @@ __global__ void __maxnreg__(REGS) batch_kernel(const __grid_constant__ BatchPara
         {
             if (tid == 0)
             {
-                const uint32_t need = seg_phase == 1 ? bpair.init_units : bpair.splat_units;
+                const uint32_t need = seg_phase == 1 ? bpair.init_units : bpair.splat_need;
                 const uint32_t *cnt = bp.done + 2 * seg_pair + (seg_phase - 1);
                 uint32_t ok = 0;
                 for (uint32_t i = 0; i < bp.spin_limit; i++)

@@ -64,6 +64,8 @@ struct isti_renderer
     void *multi_arena = nullptr;
     size_t multi_bytes = 0;
     int32_t pair_splat_rows = 0, pair_init_kib = 0; // isti_render_pairs unit sizes (0: the defaults)
+    int32_t stall_pair = -1;                         // test hook (isti_renderer_test_stall_pair)
+    uint32_t stall_spin_limit = 0;
     void *multi_host[2] = {nullptr, nullptr}; // parameter staging: uncaptured calls, captured calls
     size_t multi_host_bytes[2] = {0, 0};
     cudaEvent_t multi_copied = nullptr;
@@ -585,6 +587,15 @@ isti_status isti_renderer_test_withhold_tile(isti_renderer *r, int32_t x, int32_
     return ISTI_OK;
 }
 
+isti_status isti_renderer_test_stall_pair(isti_renderer *r, int32_t pair, uint32_t spin_limit)
+{
+    if (!r)
+        return fail(ISTI_ERR_INVALID_ARG, "renderer is NULL");
+    r->stall_pair = pair;
+    r->stall_spin_limit = spin_limit;
+    return ISTI_OK;
+}
+
 isti_status isti_renderer_enable_timing(isti_renderer *r, int32_t on)
 {
     if (!r)
@@ -905,6 +916,7 @@ extern "C" isti_status isti_render_pairs(isti_renderer *r, int32_t n_pairs, cons
         bpair.splat_gx = (max_w + 31) / 32;
         bpair.splat_gy = (max_h + splat_rows - 1) / splat_rows;
         bpair.splat_units = (uint32_t)nv * bpair.splat_gx * bpair.splat_gy;
+        bpair.splat_need = bpair.splat_units + (i == r->stall_pair ? 1u : 0u); // the test hook: one unit more than there are
         bpair.reproj_gx = (p.out_w + 31) / 32;
         const uint32_t block_rows = (uint32_t)(isti::ROWS * p.row_pairs);
         bpair.reproj_units = bpair.reproj_gx * ((p.out_h + block_rows - 1) / block_rows);
@@ -933,7 +945,7 @@ extern "C" isti_status isti_render_pairs(isti_renderer *r, int32_t n_pairs, cons
     bp.ticket = dcnt;
     bp.done = dcnt + 1;
     bp.status = dstatus;
-    bp.spin_limit = 1u << 24; // with 128 ns sleeps: about two seconds
+    bp.spin_limit = r->stall_pair >= 0 && r->stall_spin_limit ? r->stall_spin_limit : 1u << 24; // with 128 ns sleeps: about two seconds
     bp.region_bytes = (uint32_t)region;
     bp.param_bytes = (uint32_t)isti::params_prefix(nv);
     bp.splat_rows = splat_rows;

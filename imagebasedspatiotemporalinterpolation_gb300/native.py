@@ -93,6 +93,7 @@ SIGNATURES = {
     "isti_renderer_view_depth": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
     "isti_renderer_device_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "isti_renderer_set_pair_units": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "isti_renderer_test_stall_pair": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint32]),
     "isti_renderer_enable_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "isti_renderer_timing": (C.c_int, [C.c_void_p, C.POINTER(IstiTiming)]),
     "isti_renderer_set_autotune": (C.c_int, [C.c_void_p, C.c_int32]),

@@ -214,6 +214,11 @@ class Renderer:
         self._keep_pairs = (arr, keep)  # the structs must outlive the call
         check(self._lib.isti_render_pairs(self._h, len(jobs), arr, C.c_void_p(s)))
 
+    def test_stall_pair(self, pair: int, spin_limit: int = 0) -> None:
+        """isti_renderer_test_stall_pair: the failure-detection test hook of render_pairs
+        (pair < 0: off)."""
+        check(self._lib.isti_renderer_test_stall_pair(self._h, int(pair), int(spin_limit)))
+
     def set_pair_units(self, splat_rows: int = 0, init_unit_kib: int = 0) -> None:
         """isti_renderer_set_pair_units: render_pairs' splat-unit rows and init-unit KiB (0: default)."""
         check(self._lib.isti_renderer_set_pair_units(self._h, int(splat_rows), int(init_unit_kib)))

@@ -244,6 +244,14 @@ isti_status isti_renderer_set_arithmetic(isti_renderer *r, int32_t arith);
  * their tiles by TMA have such a wait.  x < 0 switches the hook off. */
 isti_status isti_renderer_test_withhold_tile(isti_renderer *r, int32_t x, int32_t y, uint32_t wait_limit);
 
+/* Failure-detection test hook for isti_render_pairs (no counterpart in the reference).
+ * From the next isti_render_pairs call on, the reprojection units of pair `pair` wait for
+ * one splat unit more than the pair has, so that dependency wait runs out after
+ * `spin_limit` polls (0: the default limit, about two seconds): the unit sets
+ * ISTI_ERR_TIMEOUT in the device status word and is skipped, and every unit that starts
+ * after that only counts itself done.  pair < 0 switches the hook off. */
+isti_status isti_renderer_test_stall_pair(isti_renderer *r, int32_t pair, uint32_t spin_limit);
+
 isti_status isti_renderer_enable_timing(isti_renderer *r, int32_t on);
 /* Waits for the recorded events, returns the sums and resets them. */
 isti_status isti_renderer_timing(isti_renderer *r, isti_timing *out);

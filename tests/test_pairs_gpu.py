@@ -129,3 +129,38 @@ def test_graph_capture_and_uncaptured_calls_alternate(cuda):
                 assert torch.equal(a, b)
     r.close()
     ref.close()
+
+
+def test_stalled_dependency_wait_times_out_and_the_next_call_renders(cuda):
+    """Failure detection of the persistent launch: the reprojection units of one pair wait
+    for a splat unit that does not exist (test hook), their bounded waits run out, the call
+    reports ISTI_ERR_TIMEOUT instead of hanging, and the next call renders every pair bit for
+    bit."""
+    import torch
+    seq = scene.Sequence(320, 180, 4, seed=4400, aux_offsets=(-0.3, 0.3), shadows=True)
+    jobs, wants = [], []
+    ref = Renderer()
+    for k in range(3):
+        clients = [seq.client(k, b) for b in (1, 2, 3)]
+        frame = DeviceFrame.from_host(seq.frame(k))
+        want = [torch.zeros((180, 320, 4), dtype=torch.uint8, device="cuda") for _ in clients]
+        ref.render_batch(want, clients, frame, chain=False)
+        jobs.append(([torch.zeros_like(w) for w in want], clients, frame))
+        wants.append(want)
+    r = Renderer()
+    r.test_stall_pair(1, 4096)
+    r.render_pairs(jobs)
+    torch.cuda.synchronize()
+    assert r.device_status() == native.ISTI_ERR_TIMEOUT
+    r.test_stall_pair(-1)
+    for outs, _, _ in jobs:
+        for o in outs:
+            o.zero_()
+    r.render_pairs(jobs)
+    torch.cuda.synchronize()
+    assert r.device_status() == native.ISTI_OK
+    for (outs, _, _), want in zip(jobs, wants):
+        for a, b in zip(outs, want):
+            assert torch.equal(a, b)
+    r.close()
+    ref.close()
