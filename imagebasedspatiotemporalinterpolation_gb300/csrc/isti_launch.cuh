@@ -85,16 +85,78 @@ struct ReprojChoice
     int plain_tiles = 0; // 1: key tiles by plain loads even where a TMA copy is possible
 };
 
-// The fixed rule: register cap by window size and view count (isti_kernels.cuh), row pairs
-// so that every warp has a colour task in phase 2.
-int rule_regs(int sw, int n_views)
+// Per-SM limits of the current device that bound resident blocks (cached per device).
+struct SmLimits
+{
+    int regs = 65536, smem = 233472, threads = 2048, blocks = 32, reserved = 1024;
+};
+
+SmLimits sm_limits()
+{
+    static std::mutex mu;
+    static SmLimits cache[64];
+    static bool have[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+        return SmLimits{};
+    std::lock_guard<std::mutex> lock(mu);
+    if (!have[dev & 63])
+    {
+        SmLimits l;
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxRegistersPerMultiprocessor, dev) == cudaSuccess && v > 0)
+            l.regs = v;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess && v > 0)
+            l.smem = v;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxThreadsPerMultiProcessor, dev) == cudaSuccess && v > 0)
+            l.threads = v;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxBlocksPerMultiprocessor, dev) == cudaSuccess && v > 0)
+            l.blocks = v;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrReservedSharedMemoryPerBlock, dev) == cudaSuccess && v >= 0)
+            l.reserved = v;
+        cache[dev & 63] = l;
+        have[dev & 63] = true;
+    }
+    return cache[dev & 63];
+}
+
+// Resident reprojection blocks per SM at a register cap (registers are allocated per warp in
+// units of 256), for blocks of `warps` warps and `smem` bytes of dynamic shared memory.
+int resident_blocks(int regs, int warps, size_t smem)
+{
+    const SmLimits l = sm_limits();
+    const int per_warp = (regs * 32 + 255) / 256 * 256;
+    int b = std::min(l.blocks, l.threads / (32 * warps));
+    b = std::min(b, l.regs / (per_warp * warps));
+    return std::min(b, (int)((size_t)l.smem / (smem + (size_t)l.reserved)));
+}
+
+// The fixed rule's output row pairs per block: enough (frame, row) tasks for every warp in
+// phase 2 (a single frame of 6 views: 3 row pairs).
+int rule_row_pairs(int n_views, int n_frames) { return std::max(1, std::min(3, n_views / (isti::ROWS * n_frames))); }
+
+// The fixed rule's register cap: 56 for the 7x7 window, 48 with fewer than 4 views; with 4 or
+// more views 40 (more resident warps), unless 48 costs no resident blocks because the block's
+// shared memory limits them anyway -- many frames per call (1080p, 6 frames: 6 views 1.254 ->
+// 1.158 ms, 4 views 0.865 -> 0.785 ms).
+int rule_regs(int sw, int n_views, int n_frames, int row_pairs)
 {
     if (sw != 1)
         return isti::REPROJ_REGS_WIDE_WINDOW;
-    return n_views >= isti::REPROJ_MANY_VIEWS ? isti::REPROJ_REGS_MANY_VIEWS : isti::REPROJ_REGS;
+    if (n_views < isti::REPROJ_MANY_VIEWS)
+        return isti::REPROJ_REGS;
+    const size_t smem = isti::reproj_smem<1>(n_views, n_frames * row_pairs);
+    return resident_blocks(isti::REPROJ_REGS, n_views, smem) >= resident_blocks(isti::REPROJ_REGS_MANY_VIEWS, n_views, smem)
+               ? isti::REPROJ_REGS
+               : isti::REPROJ_REGS_MANY_VIEWS;
 }
 
-int rule_row_pairs(int n_views, int n_frames) { return std::max(1, std::min(3, n_views / (isti::ROWS * n_frames))); }
+// The rule's launch for a frame batch (register cap and row pairs; TMA key tiles).
+ReprojChoice rule_choice(int sw, const isti::FrameParams &p)
+{
+    const int rp = rule_row_pairs(p.n_views, p.n_frames);
+    return ReprojChoice{rule_regs(sw, p.n_views, p.n_frames, rp), rp, 0};
+}
 
 template <int SW, int SI, bool MAV, int REGS>
 cudaError_t launch_reproj_regs(isti::FrameParams &p, cudaStream_t stream, int row_pairs, bool plain_tiles)
@@ -109,6 +171,11 @@ cudaError_t launch_reproj_regs(isti::FrameParams &p, cudaStream_t stream, int ro
     if (e != cudaSuccess)
         return e;
     p.row_pairs = row_pairs > 0 ? std::min(row_pairs, 3) : rule_row_pairs(p.n_views, p.n_frames);
+    // Chained outputs of several frames: phase 3 gives each row of a block its own warp, so a
+    // block has at most as many rows as there are views.  A single frame's chained output is
+    // its unchained output (the persistent buffer is out[0] itself), so that launch runs unchained.
+    if (p.chain && p.n_frames > 1)
+        p.row_pairs = std::min(p.row_pairs, std::max(1, p.n_views / isti::ROWS));
     static thread_local isti::KeyMaps km; // 2 KiB, passed by value as a kernel parameter
     // the maps depend only on the key buffers' addresses and shapes: encode them again only
     // when those changed (a renderer reuses its arena from call to call)
@@ -163,22 +230,27 @@ cudaError_t launch_reproj_regs(isti::FrameParams &p, cudaStream_t stream, int ro
             cur = (int)smem;
         }
     }
+    const int32_t chain = p.chain;
+    if (p.n_frames == 1)
+        p.chain = 0;
     kernel<<<gr, dim3(32, p.n_views), smem, stream>>>(p, km);
+    p.chain = chain;
     return cudaGetLastError();
 }
 
 template <int SW, int SI, bool MAV>
 cudaError_t launch_reproj(isti::FrameParams &p, cudaStream_t stream, ReprojChoice c)
 {
-    const int regs = c.regs > 0 ? c.regs : rule_regs(SW, p.n_views);
+    const int rp = c.row_pairs > 0 ? std::min(c.row_pairs, 3) : rule_row_pairs(p.n_views, p.n_frames);
+    const int regs = c.regs > 0 ? c.regs : rule_regs(SW, p.n_views, p.n_frames, rp);
     if constexpr (SW == 1)
     {
         if (regs == isti::REPROJ_REGS_MANY_VIEWS)
-            return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS_MANY_VIEWS>(p, stream, c.row_pairs, c.plain_tiles != 0);
-        return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS>(p, stream, c.row_pairs, c.plain_tiles != 0);
+            return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS_MANY_VIEWS>(p, stream, rp, c.plain_tiles != 0);
+        return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS>(p, stream, rp, c.plain_tiles != 0);
     }
     else
-        return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS_WIDE_WINDOW>(p, stream, c.row_pairs, c.plain_tiles != 0);
+        return launch_reproj_regs<SW, SI, MAV, isti::REPROJ_REGS_WIDE_WINDOW>(p, stream, rp, c.plain_tiles != 0);
 }
 
 // window size of the reprojection of a render mode (src/renderer.cu:676-693)

@@ -48,6 +48,7 @@ struct isti_renderer
     // autotuning of the reprojection launch: one entry per tuned shape class
     bool autotune = false;
     std::vector<isti_tuning> tuned;
+    isti::ReprojChoice pinned{}; // isti_renderer_set_reproj_launch (zero fields: the rule's)
     // arithmetic of the kernels (isti_renderer_set_arithmetic)
     int32_t arith = ISTI_ARITH_IEEE;
     // learned render path: its own arena (keys for the fallback tiles, keyframe parts,
@@ -318,11 +319,13 @@ isti_status tune_reproj(isti_renderer *r, int mode, cudaStream_t stream)
     constexpr int REPEAT = 3;
     isti::FrameParams &p = r->last;
     std::vector<isti::ReprojChoice> cands;
+    // chained outputs of several frames allow at most one block row per view (the launch limits them)
+    const int max_pairs = p.chain && p.n_frames > 1 ? std::max(1, std::min(3, p.n_views / isti::ROWS)) : 3;
     for (int plain = 0; plain <= 1; plain++) // key tiles by TMA (where the views allow it), or by plain loads
         for (int regs : isti::mode_regs(mode))
-            for (int np = 1; np <= 3; np++)
+            for (int np = 1; np <= max_pairs; np++)
                 cands.push_back({regs, np, plain});
-    const isti::ReprojChoice rule{isti::rule_regs(isti::mode_window(mode), p.n_views), isti::rule_row_pairs(p.n_views, p.n_frames), 0};
+    const isti::ReprojChoice rule = isti::rule_choice(isti::mode_window(mode), p);
     std::vector<cudaEvent_t> ev(2 * cands.size(), nullptr);
     cudaError_t e = cudaSuccess;
     for (cudaEvent_t &x : ev)
@@ -438,8 +441,11 @@ isti_status render_batch(isti_renderer *r, int n_frames, void *const *outs, cons
         cudaEventRecord(ev[0], stream);
     }
     isti::ReprojChoice choice{};
-    const isti_tuning *tuned = timewarp ? nullptr : find_tuning(r, infos[0].mode, r->last);
-    if (tuned)
+    const bool pinned = r->pinned.regs || r->pinned.row_pairs || r->pinned.plain_tiles;
+    const isti_tuning *tuned = timewarp || pinned ? nullptr : find_tuning(r, infos[0].mode, r->last);
+    if (pinned)
+        choice = r->pinned;
+    else if (tuned)
         choice = {tuned->regs, tuned->row_pairs, tuned->plain_tiles};
     cudaEvent_t ev1 = ev ? ev[1] : nullptr, ev2 = ev ? ev[2] : nullptr;
     if (r->arith == ISTI_ARITH_REFERENCE_GPU)
@@ -453,7 +459,7 @@ isti_status render_batch(isti_renderer *r, int n_frames, void *const *outs, cons
     if (e != cudaSuccess)
         return cuda_fail(e, "kernel launch");
     r->has_frame = true;
-    if (r->autotune && !timewarp && !tuned)
+    if (r->autotune && !timewarp && !tuned && !pinned)
     {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         e = cudaStreamIsCapturing(stream, &cs);
@@ -634,6 +640,17 @@ isti_status isti_renderer_set_autotune(isti_renderer *r, int32_t on)
     if (!r)
         return fail(ISTI_ERR_INVALID_ARG, "renderer is NULL");
     r->autotune = on != 0;
+    return ISTI_OK;
+}
+
+isti_status isti_renderer_set_reproj_launch(isti_renderer *r, int32_t regs, int32_t row_pairs, int32_t plain_tiles)
+{
+    if (!r)
+        return fail(ISTI_ERR_INVALID_ARG, "null renderer");
+    if ((regs != 0 && regs != isti::REPROJ_REGS_MANY_VIEWS && regs != isti::REPROJ_REGS && regs != isti::REPROJ_REGS_WIDE_WINDOW) ||
+        row_pairs < 0 || row_pairs > 3 || (plain_tiles != 0 && plain_tiles != 1))
+        return fail(ISTI_ERR_INVALID_ARG, "register cap must be 0, 40, 48 or 56, row pairs 0..3 and plain_tiles 0 or 1");
+    r->pinned = isti::ReprojChoice{regs, row_pairs, plain_tiles};
     return ISTI_OK;
 }
 
@@ -884,7 +901,9 @@ extern "C" isti_status isti_render_pairs(isti_renderer *r, int32_t n_pairs, cons
     const uint32_t splat_rows = r->pair_splat_rows ? (uint32_t)r->pair_splat_rows : isti::BATCH_SPLAT_ROWS;
     const uint32_t init_keys = r->pair_init_kib ? (uint32_t)r->pair_init_kib * 64u : isti::BATCH_INIT_UNIT_KEYS; // 16-byte units
     const int sw = isti::mode_window(mode);
-    const int regs = isti::rule_regs(sw, nv);
+    // one register cap for every unit of the launch: by window size and view count (the
+    // per-batch rule's occupancy test depends on a batch's frames, which differ from pair to pair)
+    const int regs = sw != 1 ? isti::REPROJ_REGS_WIDE_WINDOW : (nv >= isti::REPROJ_MANY_VIEWS ? isti::REPROJ_REGS_MANY_VIEWS : isti::REPROJ_REGS);
     const unsigned nthreads = 32u * (unsigned)nv;
     size_t region = 0, off = 0;
     for (int i = 0; i < n_pairs; i++)

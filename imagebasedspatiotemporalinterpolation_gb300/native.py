@@ -97,6 +97,7 @@ SIGNATURES = {
     "isti_renderer_enable_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "isti_renderer_timing": (C.c_int, [C.c_void_p, C.POINTER(IstiTiming)]),
     "isti_renderer_set_autotune": (C.c_int, [C.c_void_p, C.c_int32]),
+    "isti_renderer_set_reproj_launch": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     "isti_renderer_tuning_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "isti_renderer_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(IstiTuning)]),
     "isti_render_noalloc": (C.c_int, [C.c_void_p, C.POINTER(IstiRenderInfo), C.POINTER(IstiFrameData), C.c_void_p]),

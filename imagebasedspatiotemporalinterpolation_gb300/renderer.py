@@ -278,6 +278,11 @@ class Renderer:
         the reprojection's candidate launches and later renders use the fastest."""
         check(self._lib.isti_renderer_set_autotune(self._h, int(on)))
 
+    def set_reproj_launch(self, regs: int = 0, row_pairs: int = 0, plain_tiles: int = 0) -> None:
+        """isti_renderer_set_reproj_launch: pin the reprojection launch of later renders
+        (register cap, output row pairs per block, key tiles by plain loads); 0: the rule's."""
+        check(self._lib.isti_renderer_set_reproj_launch(self._h, int(regs), int(row_pairs), int(plain_tiles)))
+
     def tuning(self) -> list:
         """The tuned shape classes and their chosen launches (isti_renderer_tuning)."""
         n = C.c_int32()

@@ -264,8 +264,19 @@ isti_status isti_renderer_timing(isti_renderer *r, isti_timing *out);
  * class's later renders, captured ones included, use the fastest.  Every candidate
  * computes the same result and the reprojection rewrites its outputs identically when
  * repeated, so the output does not depend on the choice.  Off (the default): a fixed
- * rule measured on GB300 at 1080p. */
+ * rule measured on GB300 (register cap by window size, view count and the resident blocks
+ * the call's shared memory allows; output row pairs by views and frames per call).
+ * Chained calls of several frames use at most one output row per source view in a block
+ * (row pairs <= views / 2), whatever is asked for. */
 isti_status isti_renderer_set_autotune(isti_renderer *r, int32_t on);
+
+/* Pins the reprojection launch of every later render (no counterpart in the reference):
+ * register cap (40 or 48 for the 3x3 window, 56 for the 7x7 window; 0: the rule's), output
+ * row pairs per block (1..3; 0: the rule's) and key tiles by plain loads (1) or TMA copies
+ * where the views allow them (0).  A cap the render mode is not built with takes the mode's
+ * own (48 for the 3x3 window, 56 for the 7x7).  A pinned launch takes precedence over a
+ * tuned one.  The output does not depend on it.  ISTI_ERR_INVALID_ARG for other values. */
+isti_status isti_renderer_set_reproj_launch(isti_renderer *r, int32_t regs, int32_t row_pairs, int32_t plain_tiles);
 
 typedef struct isti_tuning
 {

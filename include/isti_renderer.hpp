@@ -396,6 +396,15 @@ public:
             report(isti_renderer_set_autotune(_r, on ? 1 : 0), "Renderer::setAutotune");
     }
 
+    // isti_renderer_set_reproj_launch (no counterpart in the reference): pins the
+    // reprojection launch (register cap, row pairs per block, plain-load key tiles; 0: the
+    // rule's); the output does not depend on it.
+    void setReprojLaunch(int regs, int row_pairs, bool plain_tiles)
+    {
+        if (_r)
+            report(isti_renderer_set_reproj_launch(_r, regs, row_pairs, plain_tiles ? 1 : 0), "Renderer::setReprojLaunch");
+    }
+
 private:
     void report(isti_status s, const char *what, const char *msg = nullptr)
     {

@@ -77,6 +77,7 @@ def test_argument_validation_without_device(built):
     assert lib.isti_renderer_view_buffers(None, 0, None, None, None, None, None) == native.ISTI_ERR_INVALID_ARG
     assert lib.isti_renderer_set_pair_units(None, 16, 64) == native.ISTI_ERR_INVALID_ARG
     assert lib.isti_renderer_set_autotune(None, 1) == native.ISTI_ERR_INVALID_ARG
+    assert lib.isti_renderer_set_reproj_launch(None, 48, 1, 0) == native.ISTI_ERR_INVALID_ARG
     assert lib.isti_renderer_tuning_count(None, None) == native.ISTI_ERR_INVALID_ARG
     assert lib.isti_renderer_tuning(None, 0, None) == native.ISTI_ERR_INVALID_ARG
 

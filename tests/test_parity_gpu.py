@@ -413,3 +413,41 @@ def test_autotuned_unchained_batch_of_eight(cuda):
     assert len(tuned.tuning()) == 1 and tuned.tuning()[0]["n_frames"] == 8
     tuned.close()
     rule.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [(160, 90, (), False, 0, 2, True), (128, 72, (0.3,), True, 0, 3, True),
+                                  (96, 54, (), False, 0, 1, True), (160, 90, (-0.3, 0.3), True, 0, 1, False),
+                                  (96, 54, (0.3,), False, 1, 2, True)],
+                         ids=["2v-2f-chained", "4v-3f-chained-shadows", "2v-1f-chained", "6v-1f", "mode1-4v-2f-chained"])
+def test_every_pinned_reprojection_launch_equals_the_rule(cuda, case):
+    """Every reprojection launch a renderer can be pinned to (register cap x output row
+    pairs x key tiles by TMA or plain loads) renders the rule's frames bit for bit, chained
+    batches of several frames included (their blocks keep at most one row per view)."""
+    import torch
+    w, h, aux, sh, mode, nf, chain = case
+    seq = Sequence(w, h, 2, seed=6200 + w + nf, aux_offsets=aux, shadows=sh, max_speed=2.0)
+    dev = DeviceFrame.from_host(seq.frame(0))
+    clients = [seq.client(0, b % 4, mode=mode, alpha=(b + 1) / (nf + 1)) for b in range(nf)]
+    g = torch.Generator().manual_seed(w + 7 * nf)
+    prevs = [torch.randint(0, 256, (h, w, 4), dtype=torch.uint8, generator=g).cuda() for _ in clients]
+    rule = Renderer()
+    want = [p.clone() for p in prevs]
+    rule.render_batch(want, clients, dev, chain=chain)
+    pinned = Renderer()
+    with pytest.raises(native.IstiError):
+        pinned.set_reproj_launch(44, 1, 0)
+    with pytest.raises(native.IstiError):
+        pinned.set_reproj_launch(48, 4, 0)
+    for regs in ((56,) if mode == 1 else (40, 48)):
+        for rp in (1, 2, 3):
+            for plain in (0, 1):
+                pinned.set_reproj_launch(regs, rp, plain)
+                got = [p.clone() for p in prevs]
+                pinned.render_batch(got, clients, dev, chain=chain)
+                torch.cuda.synchronize()
+                for k in range(nf):
+                    assert torch.equal(got[k], want[k]), f"regs {regs}, row pairs {rp}, plain tiles {plain}: frame {k} differs"
+    assert pinned.device_status() == 0 and rule.device_status() == 0
+    pinned.close()
+    rule.close()
