@@ -317,7 +317,9 @@ __device__ __forceinline__ void splat_pixel(const FrameParams &p, int view, uint
         else
         {
             cam[idx] = make_float2(xmul(fmx, wg), xmul(fmy, wg));
-            cdep[idx] = z_to_depth(xadd(z_from, xmul(fmz, wg)));
+            // the reference stores the product (the flow's dz) before the search adds it to z:
+            // rounded on its own (never contracted into the addition), in either arithmetic
+            cdep[idx] = z_to_depth(xadd(z_from, __fmul_rn(fmz, wg)));
             atomicMin(keys + idx, encode_key(z_to_depth(z_from), x, y));
         }
     }

@@ -72,6 +72,10 @@ CASES = {
     "f1080": dict(size=(1920, 1080), aux=(-0.3, 0.3), shadows=True, seed=202),
     # every render mode with aux cameras and shadows at a small size
     "modes": dict(size=(400, 240), aux=(-0.3, 0.3), shadows=True, seed=303),
+    # aux cameras at half the main resolution (aux_idx = idx / (res / aux_res))
+    "half": dict(size=(640, 360), aux=(-0.3, 0.3), aux_size=(320, 180), shadows=True, seed=404),
+    # odd sizes: partial blocks and key tiles at the right and bottom edges
+    "odd": dict(size=(333, 197), aux=(0.3,), shadows=True, seed=505),
 }
 
 
@@ -82,6 +86,12 @@ def _cases():
         out.append(("f1080", b, 0))
     for mode in (1, 2, 3):
         out.append(("modes", 2, mode))
+    out.append(("half", 2, 0))
+    out.append(("half", 1, 1))
+    out.append(("odd", 3, 0))
+    # extrapolation past the later keyframe (the frame loop's latency option): t = 1.25
+    out.append(("s640", 5, 0))
+    out.append(("modes", 5, 0))
     return out
 
 
@@ -91,7 +101,7 @@ _seqs = {}
 def seq_for(name):
     if name not in _seqs:
         c = CASES[name]
-        _seqs[name] = Sequence(*c["size"], 2, seed=c["seed"], aux_offsets=c["aux"], shadows=c["shadows"])
+        _seqs[name] = Sequence(*c["size"], 2, seed=c["seed"], aux_offsets=c["aux"], aux_size=c.get("aux_size"), shadows=c["shadows"])
     return _seqs[name]
 
 
