@@ -309,49 +309,19 @@ __global__ void __launch_bounds__(LT_W *LT_H, 6) learned_kernel(const __grid_con
 }
 
 // ---- fallback: the plain method for the marked tiles ----
+//
+// The window initialisation of a marked tile's edge pixels reads keys one pixel outside the
+// tile, so the fallback keeps exact keys for the marked tiles and a ring of FB_RING pixels
+// around each: both are reset to the empty value and receive every source pixel that splats
+// into them.  Keys elsewhere are never read.
+constexpr int FB_RING = 1;
 
-__device__ __forceinline__ bool tile_marked(const LearnedParams &p, int k, uint32_t x, uint32_t y)
+// Whether a marked tile of frame k lies within m pixels (either axis) of pixel (x, y), which
+// may lie outside the image (the box is clipped to it).
+__device__ __forceinline__ bool marked_within(const LearnedParams &p, int k, int x, int y, int m)
 {
-    return __ldg(p.tile_flags + ((size_t)k * p.tiles_y + y / LT_H) * p.tiles_x + x / LT_W) != 0u;
-}
-
-// keys of every marked tile <- the empty value (both views).  A small grid walks the list of
-// marked tiles (blocks of LT_W x LT_H threads, one tile per iteration).
-__device__ __forceinline__ void tile_of(const LearnedParams &p, uint32_t flag_idx, int &k, uint32_t &x, uint32_t &y)
-{
-    const uint32_t per_frame = (uint32_t)(p.tiles_x * p.tiles_y);
-    k = (int)(flag_idx / per_frame);
-    const uint32_t t = flag_idx % per_frame;
-    x = (t % (uint32_t)p.tiles_x) * LT_W + threadIdx.x;
-    y = (t / (uint32_t)p.tiles_x) * LT_H + threadIdx.y;
-}
-
-__global__ void __launch_bounds__(LT_W *LT_H) fallback_init_kernel(const __grid_constant__ LearnedParams p)
-{
-    const int n = *p.fallback_count;
-    for (int i = blockIdx.x; i < n; i += gridDim.x)
-    {
-        int k;
-        uint32_t x, y;
-        tile_of(p, __ldg(p.tile_list + i), k, x, y);
-        if (x >= p.fp.out_w || y >= p.fp.out_h)
-            continue;
-        for (int v = 0; v < 2; v++)
-            p.fp.v[v].splat[k * p.fp.key_stride + y * p.fp.v[v].w + x] = SPLAT_EMPTY;
-    }
-}
-
-// Every source pixel whose client-camera target lies in a marked tile: atomicMin of its key
-// (computeFlowFields_sortedSplatting_kernel, src/renderer.cu:110-145).  One thread per source
-// pixel and view handles every frame (the keyframe part is read once).  An approximate
-// projection (contracted multiply-adds, fast division) first rejects targets farther than 2
-// pixels from every marked tile -- its error is orders of magnitude below that margin; a w
-// near zero or a non-finite value is never rejected -- and only candidates take the exact
-// projection of the plain path.
-__device__ __forceinline__ bool near_marked_tile(const LearnedParams &p, int k, float fx, float fy)
-{
-    const int x0 = max(0, (int)floorf(fx) - 2), x1 = min((int)p.fp.out_w - 1, (int)floorf(fx) + 2);
-    const int y0 = max(0, (int)floorf(fy) - 2), y1 = min((int)p.fp.out_h - 1, (int)floorf(fy) + 2);
+    const int x0 = max(0, x - m), x1 = min((int)p.fp.out_w - 1, x + m);
+    const int y0 = max(0, y - m), y1 = min((int)p.fp.out_h - 1, y + m);
     if (x0 > x1 || y0 > y1)
         return false;
     for (int ty = y0 / LT_H; ty <= y1 / LT_H; ty++)
@@ -361,6 +331,54 @@ __device__ __forceinline__ bool near_marked_tile(const LearnedParams &p, int k, 
     return false;
 }
 
+// The frame and first pixel of a marked tile from its flag index.
+__device__ __forceinline__ void tile_origin(const LearnedParams &p, uint32_t flag_idx, int &k, int &x0, int &y0)
+{
+    const uint32_t per_frame = (uint32_t)(p.tiles_x * p.tiles_y);
+    k = (int)(flag_idx / per_frame);
+    const uint32_t t = flag_idx % per_frame;
+    x0 = (int)(t % (uint32_t)p.tiles_x) * LT_W;
+    y0 = (int)(t / (uint32_t)p.tiles_x) * LT_H;
+}
+
+// This thread's pixel of a marked tile.
+__device__ __forceinline__ void tile_of(const LearnedParams &p, uint32_t flag_idx, int &k, uint32_t &x, uint32_t &y)
+{
+    int x0, y0;
+    tile_origin(p, flag_idx, k, x0, y0);
+    x = (uint32_t)x0 + threadIdx.x;
+    y = (uint32_t)y0 + threadIdx.y;
+}
+
+// keys of every marked tile and its ring <- the empty value (both views).  A small grid walks
+// the list of marked tiles (blocks of LT_W x LT_H threads, one tile per iteration); rings that
+// overlap a neighbour are reset twice to the same value.
+__global__ void __launch_bounds__(LT_W *LT_H) fallback_init_kernel(const __grid_constant__ LearnedParams p)
+{
+    constexpr int RW = LT_W + 2 * FB_RING, RH = LT_H + 2 * FB_RING;
+    const int n = *p.fallback_count;
+    for (int i = blockIdx.x; i < n; i += gridDim.x)
+    {
+        int k, x0, y0;
+        tile_origin(p, __ldg(p.tile_list + i), k, x0, y0);
+        for (int j = threadIdx.y * LT_W + threadIdx.x; j < RW * RH; j += LT_W * LT_H)
+        {
+            const int x = x0 - FB_RING + j % RW, y = y0 - FB_RING + j / RW;
+            if (x < 0 || y < 0 || x >= (int)p.fp.out_w || y >= (int)p.fp.out_h)
+                continue;
+            for (int v = 0; v < 2; v++)
+                p.fp.v[v].splat[k * p.fp.key_stride + (uint32_t)y * p.fp.v[v].w + (uint32_t)x] = SPLAT_EMPTY;
+        }
+    }
+}
+
+// Every source pixel whose client-camera target lies in a marked tile or its ring: atomicMin
+// of its key (computeFlowFields_sortedSplatting_kernel, src/renderer.cu:110-145).  One thread
+// per source pixel and view handles every frame (the keyframe part is read once).  An
+// approximate projection (contracted multiply-adds, fast division) first rejects targets
+// farther than 2 pixels beyond every tile's ring -- its error is orders of magnitude below
+// that margin; a w near zero or a non-finite value is never rejected -- and only candidates
+// take the exact projection of the plain path.
 __global__ void __launch_bounds__(256) fallback_splat_kernel(const __grid_constant__ LearnedParams p)
 {
     if (*p.fallback_count == 0)
@@ -385,14 +403,16 @@ __global__ void __launch_bounds__(256) fallback_splat_kernel(const __grid_consta
         if (isfinite(qx) && isfinite(qy) && fabsf(qw) > 1e-6f)
         {
             const float fx = (__fdividef(qx, qw) + 1.0f) * (float)dv.w * 0.5f, fy = (__fdividef(qy, qw) + 1.0f) * (float)dv.h * 0.5f;
-            candidate = isfinite(fx) && isfinite(fy) ? near_marked_tile(p, k, fx, fy) : true;
+            if (isfinite(fx) && isfinite(fy))
+                candidate = marked_within(p, k, (int)floorf(fminf(fmaxf(fx, -1e6f), 1e6f)), (int)floorf(fminf(fmaxf(fy, -1e6f), 1e6f)),
+                                          2 + FB_RING);
         }
         if (!candidate)
             continue;
         const float4 pc = learned_project(p, v, k, x, y);
         const float depth_cam = z_to_depth(pc.z);
         const int2 pix = cs2pixel(pc.x, pc.y, dv.w, dv.h);
-        if (!in_range(pix, dv.w, dv.h) || depth_cam < 0.0f || !tile_marked(p, k, (uint32_t)pix.x, (uint32_t)pix.y))
+        if (!in_range(pix, dv.w, dv.h) || depth_cam < 0.0f || !marked_within(p, k, pix.x, pix.y, FB_RING))
             continue;
         atomicMin(dv.splat + k * p.fp.key_stride + ((uint32_t)pix.y * dv.w + (uint32_t)pix.x), encode_key(depth_cam, x, y));
     }

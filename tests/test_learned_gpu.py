@@ -61,6 +61,35 @@ def test_all_tiles_plain_chained_equals_plain_path(cuda):
     r.close()
 
 
+def test_fallback_reads_only_keys_it_rebuilt(cuda):
+    """The fallback resets and splats the keys of the marked tiles and of a one-pixel ring
+    around each (the window of a tile's edge pixels reads one pixel outside it): with some
+    tiles marked, a call renders the same frames after another keyframe pair's call has
+    left its keys everywhere as on a fresh renderer."""
+    import torch
+    # seeds on which keys left outside the ring changed 8 and 4 pixels before the ring existed
+    for seed in (520, 521):
+        seq = Sequence(640, 360, 3, seed=seed, max_speed=1.0, max_rot_deg=3.0)
+        f0, c0 = _frames(seq, 0)
+        f1, c1 = _frames(seq, 1)
+        prev = torch.full((360, 640, 4), 9, dtype=torch.uint8, device="cuda")
+        used = Renderer()
+        scratch = [prev.clone() for _ in c0]
+        used.render_learned(scratch, c0, f0, None, iterations=-1)   # every tile: keys of pair 0 everywhere
+        got = [prev.clone() for _ in c1]
+        used.render_learned(got, c1, f1, None, iterations=1)
+        fb, tiles = used.learned_stats()
+        assert 0 < fb < tiles, "the case needs some tiles, not all, sent to the plain method"
+        fresh = Renderer()
+        want = [prev.clone() for _ in c1]
+        fresh.render_learned(want, c1, f1, None, iterations=1)
+        for k, (a, b) in enumerate(zip(got, want)):
+            assert torch.equal(a, b), f"seed {seed}, frame {k}: {int((a != b).any(-1).sum())} pixels depend on the earlier call"
+        assert used.device_status() == 0 and fresh.device_status() == 0
+        used.close()
+        fresh.close()
+
+
 def test_learned_without_network_mostly_matches_plain(cuda):
     import torch
     seq = Sequence(640, 360, 2, seed=516, max_speed=0.5, max_rot_deg=1.0)
