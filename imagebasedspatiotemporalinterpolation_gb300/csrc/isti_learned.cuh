@@ -52,7 +52,11 @@ struct LearnedParams
     int32_t *fallback_count;    // marked tiles (all frames)
     uint32_t *tile_list;        // the marked tiles' flag indices, fallback_count of them (any order)
     uint8_t *valid;             // [frame][h][w]: 1 where the frame wrote a pixel (chained outputs only)
+    uint32_t *cell_bits;        // [frame][cells_y][cell_words]: FB_CELL-pixel square cells near a marked tile (fallback splat)
+    int32_t cells_y, cell_words;
 };
+
+constexpr int FB_CELL = 8; // pixels per side of a fallback-splat rejection cell
 
 // client-camera position of source pixel (sx, sy) of view v for frame k: the splat kernel's
 // per-frame arithmetic (src/renderer.cu:110-116) on the stored keyframe part
@@ -350,18 +354,36 @@ __device__ __forceinline__ void tile_of(const LearnedParams &p, uint32_t flag_id
     y = (uint32_t)y0 + threadIdx.y;
 }
 
-// keys of every marked tile and its ring <- the empty value (both views).  A small grid walks
-// the list of marked tiles (blocks of LT_W x LT_H threads, one tile per iteration); rings that
-// overlap a neighbour are reset twice to the same value.
+// Margin of the fallback splat's approximate rejection: the ring plus 2 pixels for the
+// approximate projection's error (orders of magnitude below that).
+constexpr int FB_MARGIN = FB_RING + 2;
+
+// keys of every marked tile and its ring <- the empty value (both views), and the rejection
+// cells within FB_MARGIN pixels of the tile marked.  A small grid walks the list of marked
+// tiles (blocks of LT_W x LT_H threads, one tile per iteration); rings and cells shared with a
+// neighbour are written twice with the same value.
 __global__ void __launch_bounds__(LT_W *LT_H) fallback_init_kernel(const __grid_constant__ LearnedParams p)
 {
     constexpr int RW = LT_W + 2 * FB_RING, RH = LT_H + 2 * FB_RING;
     const int n = *p.fallback_count;
+    const int cells_x = ((int)p.fp.out_w + FB_CELL - 1) / FB_CELL;
     for (int i = blockIdx.x; i < n; i += gridDim.x)
     {
         int k, x0, y0;
         tile_origin(p, __ldg(p.tile_list + i), k, x0, y0);
-        for (int j = threadIdx.y * LT_W + threadIdx.x; j < RW * RH; j += LT_W * LT_H)
+        const int t = threadIdx.y * LT_W + threadIdx.x;
+        {
+            // cells overlapping [x0 - FB_MARGIN, x0 + LT_W + FB_MARGIN) x [y0 - FB_MARGIN, y0 + LT_H + FB_MARGIN)
+            const int cx0 = max(0, (x0 - FB_MARGIN) / FB_CELL), cx1 = min(cells_x - 1, (x0 + LT_W + FB_MARGIN - 1) / FB_CELL);
+            const int cy0 = max(0, (y0 - FB_MARGIN) / FB_CELL), cy1 = min(p.cells_y - 1, (y0 + LT_H + FB_MARGIN - 1) / FB_CELL);
+            const int ncx = cx1 - cx0 + 1;
+            if (t < ncx * (cy1 - cy0 + 1))
+            {
+                const int cx = cx0 + t % ncx, cy = cy0 + t / ncx;
+                atomicOr(p.cell_bits + ((size_t)k * p.cells_y + cy) * p.cell_words + cx / 32, 1u << (cx % 32));
+            }
+        }
+        for (int j = t; j < RW * RH; j += LT_W * LT_H)
         {
             const int x = x0 - FB_RING + j % RW, y = y0 - FB_RING + j / RW;
             if (x < 0 || y < 0 || x >= (int)p.fp.out_w || y >= (int)p.fp.out_h)
@@ -404,8 +426,19 @@ __global__ void __launch_bounds__(256) fallback_splat_kernel(const __grid_consta
         {
             const float fx = (__fdividef(qx, qw) + 1.0f) * (float)dv.w * 0.5f, fy = (__fdividef(qy, qw) + 1.0f) * (float)dv.h * 0.5f;
             if (isfinite(fx) && isfinite(fy))
-                candidate = marked_within(p, k, (int)floorf(fminf(fmaxf(fx, -1e6f), 1e6f)), (int)floorf(fminf(fmaxf(fy, -1e6f), 1e6f)),
-                                          2 + FB_RING);
+            {
+                // a marked tile within FB_MARGIN pixels of (ix, iy) (the box clipped to the image) is
+                // within FB_MARGIN of the nearest pixel of the image too, whose cell is then marked:
+                // the cell test keeps every candidate the box test would keep
+                const int ix = (int)floorf(fminf(fmaxf(fx, -1e6f), 1e6f)), iy = (int)floorf(fminf(fmaxf(fy, -1e6f), 1e6f));
+                if (ix < -FB_MARGIN || iy < -FB_MARGIN || ix >= (int)dv.w + FB_MARGIN || iy >= (int)dv.h + FB_MARGIN)
+                    candidate = false;
+                else
+                {
+                    const int cx = min(max(ix, 0), (int)dv.w - 1) / FB_CELL, cy = min(max(iy, 0), (int)dv.h - 1) / FB_CELL;
+                    candidate = (__ldg(p.cell_bits + ((size_t)k * p.cells_y + cy) * p.cell_words + cx / 32) >> (cx % 32)) & 1u;
+                }
+            }
         }
         if (!candidate)
             continue;

@@ -1013,6 +1013,8 @@ extern "C" isti_status isti_render_learned(isti_renderer *r, isti_flownet *net, 
     cudaError_t e = cudaMemsetAsync(p.fallback_count, 0, 4, stream);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(p.fp.status, 0, 4, stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(p.cell_bits, 0, (size_t)n_frames * p.cells_y * p.cell_words * 4, stream);
     if (e != cudaSuccess)
         return cuda_fail(e, "cudaMemsetAsync");
     const dim3 b2(32, 8);
@@ -1133,7 +1135,10 @@ isti_status learned_setup(isti_renderer *r, isti_flownet *net, int32_t n_frames,
     const size_t guess_bytes = align_up((size_t)n_frames * hq * wq * 4 * 2, 256);
     const size_t flag_bytes = 2 * align_up((size_t)n_frames * tiles_x * tiles_y * 4, 256); // flags, then the marked-tile list
     const size_t valid_bytes = align_up((size_t)n_frames * px, 256);
-    const size_t total = l.total + 4 * ws_bytes + in_bytes + guess_bytes + flag_bytes + 256 + valid_bytes;
+    const int cells_y = (int)((h + isti::FB_CELL - 1) / isti::FB_CELL);
+    const int cell_words = (int)(((w + isti::FB_CELL - 1) / isti::FB_CELL + 31) / 32);
+    const size_t cell_bytes = align_up((size_t)n_frames * cells_y * cell_words * 4, 256);
+    const size_t total = l.total + 4 * ws_bytes + in_bytes + guess_bytes + flag_bytes + 256 + valid_bytes + cell_bytes;
     if (total > r->learned_bytes)
     {
         if (r->learned_arena)
@@ -1162,6 +1167,9 @@ isti_status learned_setup(isti_renderer *r, isti_flownet *net, int32_t n_frames,
     p.tile_list = reinterpret_cast<uint32_t *>(extra + 4 * ws_bytes + in_bytes + guess_bytes + flag_bytes / 2);
     p.fallback_count = reinterpret_cast<int32_t *>(extra + 4 * ws_bytes + in_bytes + guess_bytes + flag_bytes);
     p.valid = reinterpret_cast<uint8_t *>(extra + 4 * ws_bytes + in_bytes + guess_bytes + flag_bytes + 256);
+    p.cell_bits = reinterpret_cast<uint32_t *>(extra + 4 * ws_bytes + in_bytes + guess_bytes + flag_bytes + 256 + valid_bytes);
+    p.cells_y = cells_y;
+    p.cell_words = cell_words;
     p.hq = hq;
     p.wq = wq;
     p.learned_iters = iterations;
