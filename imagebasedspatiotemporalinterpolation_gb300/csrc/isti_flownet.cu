@@ -255,7 +255,7 @@ __global__ void head_kernel(const bf16 *d1, size_t npix, const float *hw, const 
             float a = sw[HEAD_COUT * HEAD_CIN + j];
 #pragma unroll
             for (int k = 0; k < HEAD_CIN; k++)
-                a += sw[j * HEAD_CIN + k] * f[k];
+                a = fmaf(sw[j * HEAD_CIN + k], f[k], a); // fused multiply-adds in channel order, as the fused head
             o[j] = a;
         }
         if (flow)
@@ -313,7 +313,7 @@ __global__ void head_back_kernel(const bf16 *d1, size_t npix, const float *hw, c
             float a = sw[HEAD_COUT * HEAD_CIN + j];
 #pragma unroll
             for (int k = 0; k < HEAD_CIN; k++)
-                a += sw[j * HEAD_CIN + k] * f[k];
+                a = fmaf(sw[j * HEAD_CIN + k], f[k], a); // fused multiply-adds in channel order, as the fused head
             const float l = __ldg(label + p * 4 + j);
             go[j] = 0.0f;
             if (!isnan(l))
@@ -495,11 +495,12 @@ isti_status repack(isti_flownet *net, cudaStream_t s)
     return ISTI_OK;
 }
 
-isti_status conv(isti_flownet *net, int l, const bf16 *x, int n, int h, int w, const bf16 *mask, bf16 *out, cudaStream_t s, bool pdl = false)
+isti_status conv(isti_flownet *net, int l, const bf16 *x, int n, int h, int w, const bf16 *mask, bf16 *out, cudaStream_t s, bool pdl = false,
+                 const isti_unet::ConvHead *head = nullptr, bool *head_fused = nullptr)
 {
     const LayerDef &d = LAYERS[l];
     return isti_unet::conv_launch(d.taps, x, n, h, w, d.cin, net->packs + net->pk_off[l], net->params + net->b_off[l], mask, d.relu, out, d.cout,
-                                  net->status, s, pdl);
+                                  net->status, s, pdl, head, head_fused);
 }
 
 // data gradient of layer l: g_in = conv(g_out, W^T flipped), masked by (mask > 0) when given
@@ -564,8 +565,12 @@ isti_status forward(isti_flownet *net, const bf16 *x0, int n, int h, int w, Buff
     ISTI_TRY(conv(net, 8, b.d2, n, h2, w2, nullptr, b.p1, s, pdl));
     ok(launch_kernel(upadd_kernel, dim3(grid_for((size_t)n * h * w * 4)), blk, 0, s, pdl, (const bf16 *)b.p1, (const bf16 *)b.e1, n, h, w, 32,
                      b.s1));
-    ISTI_TRY(conv(net, 9, b.s1, n, h, w, nullptr, b.d1, s, pdl));
-    if (flow || flow16)
+    // inference: the 1x1 head in d1's epilogue where the row-tile kernel runs d1 (d1 itself is
+    // then not stored), else its own kernel
+    const isti_unet::ConvHead head{net->params + net->w_off[N_CONV], net->params + net->b_off[N_CONV], flow, flow16};
+    bool fused = false;
+    ISTI_TRY(conv(net, 9, b.s1, n, h, w, nullptr, b.d1, s, pdl, pdl && (flow || flow16) ? &head : nullptr, &fused));
+    if ((flow || flow16) && !fused)
         ok(launch_kernel(head_kernel, dim3(grid_for((size_t)n * h * w)), blk, 0, s, pdl, (const bf16 *)b.d1, (size_t)n * h * w,
                          (const float *)(net->params + net->w_off[N_CONV]), (const float *)(net->params + net->b_off[N_CONV]), flow, flow16));
     if (e == cudaSuccess)

@@ -162,8 +162,12 @@ namespace isti_unet
 {
 // Launch of conv_kernel<taps> (shared with the network code in isti_flownet.cu).
 isti_status conv_launch(int taps, const void *x, int n, int h, int w, int cin, const void *wpack, const float *bias, const void *mask, int relu,
-                        void *out, int cout, int32_t *status, cudaStream_t stream, bool pdl)
+                        void *out, int cout, int32_t *status, cudaStream_t stream, bool pdl, const ConvHead *head, bool *head_fused)
 {
+    if (head_fused)
+        *head_fused = false;
+    if (head && (!head->w || !head->b || (!head->flow && !head->flow16) || ((uintptr_t)head->flow & 15u) || ((uintptr_t)head->flow16 & 7u)))
+        return isti::set_error(ISTI_ERR_INVALID_ARG, "isti_unet_conv: fused head needs weights, bias and an aligned output");
     if ((taps != 9 && taps != 1) || n < 1 || h < 1 || w < 1 || cin % 16 || cout % 16 || cout < 16 || cout > 256 || !x || !wpack || !out)
         return isti::set_error(ISTI_ERR_INVALID_ARG, "isti_unet_conv: bad shape or NULL buffer");
     if (((uintptr_t)out & 15u) || ((uintptr_t)mask & 15u) || ((uintptr_t)wpack & 15u))
@@ -203,12 +207,21 @@ isti_status conv_launch(int taps, const void *x, int n, int h, int w, int cin, c
         p.stages = (int)std::min<size_t>(8, stages);
         if (p.stages >= 2)
         {
+            if (head)
+            {
+                p.head_w = head->w;
+                p.head_b = head->b;
+                p.head_flow = head->flow;
+                p.head_flow16 = static_cast<__half *>(head->flow16);
+            }
             const size_t smem = w_region + (size_t)p.stages * sb + (2 * p.stages + 6) * 8 + 16;
             const int units = n * h * ((w + ROW_M - 1) / ROW_M);
             const int grid = std::min(units, sm_count() * per_sm);
             cudaError_t e = smem_limit(row_conv_kernel<0>, smem);
             if (e == cudaSuccess)
                 e = launch_kernel(row_conv_kernel<0>, dim3((unsigned)grid), dim3(PCONV_THREADS), smem, stream, pdl, p, xmap);
+            if (e == cudaSuccess && head && head_fused)
+                *head_fused = true;
             return e == cudaSuccess ? ISTI_OK : cuda_fail(e, "isti_unet_conv launch");
         }
     }

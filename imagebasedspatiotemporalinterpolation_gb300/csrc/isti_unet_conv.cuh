@@ -32,6 +32,7 @@
 #include "isti_tc.cuh"
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <stdint.h>
 
 namespace isti_unet
@@ -63,7 +64,17 @@ struct ConvParams
     int relu;
     int stages;                 // depth of the shared-memory ring
     int chunked_map;            // 1: one 5-D box per stage (channel chunks outermost); 0: ck / 8 4-D boxes
+    // 1x1 output head fused into the epilogue (row_conv_kernel, inference): when head_w is
+    // set, each pixel's bf16 outputs feed HEAD outputs = head_b + head_w . out (f32, fused
+    // multiply-adds in channel order) written to head_flow (f32) and/or head_flow16 (f16),
+    // and `out` is not written
+    const float *head_w;        // [HEAD][cout]
+    const float *head_b;        // [HEAD]
+    float *head_flow;           // [pixel][HEAD], or null
+    __half *head_flow16;        // [pixel][HEAD], or null
 };
+
+constexpr int CONV_HEAD = 4; // outputs of a fused head
 
 __host__ __device__ constexpr uint32_t conv_stage_bytes(int ck, int cout) { return (uint32_t)ck * 256u + (uint32_t)ck * cout * 2u; }
 
@@ -421,6 +432,11 @@ __global__ void __launch_bounds__(PCONV_THREADS, 1) row_conv_kernel(const __grid
             const int px = seg * ROW_M + m;
             const bool inb = px < p.w;
             const size_t pix = ((size_t)bi * p.h + row) * p.w + (inb ? px : 0);
+            float hacc[CONV_HEAD];
+            if (p.head_w)
+#pragma unroll
+                for (int q = 0; q < CONV_HEAD; q++)
+                    hacc[q] = __ldg(p.head_b + q);
             for (int c0 = 0; c0 < p.cout; c0 += 16)
             {
                 uint32_t r[16];
@@ -455,9 +471,35 @@ __global__ void __launch_bounds__(PCONV_THREADS, 1) row_conv_kernel(const __grid
                     const __nv_bfloat162 h2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
                     o[j] = *reinterpret_cast<const uint32_t *>(&h2);
                 }
+                if (p.head_w)
+                {
+#pragma unroll
+                    for (int j = 0; j < 8; j++)
+                    {
+                        const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&o[j]));
+#pragma unroll
+                        for (int q = 0; q < CONV_HEAD; q++)
+                        {
+                            hacc[q] = fmaf(__ldg(p.head_w + q * p.cout + c0 + 2 * j), f.x, hacc[q]);
+                            hacc[q] = fmaf(__ldg(p.head_w + q * p.cout + c0 + 2 * j + 1), f.y, hacc[q]);
+                        }
+                    }
+                    continue;
+                }
                 uint4 *dst = reinterpret_cast<uint4 *>(p.out + pix * p.cout + c0);
                 dst[0] = make_uint4(o[0], o[1], o[2], o[3]);
                 dst[1] = make_uint4(o[4], o[5], o[6], o[7]);
+            }
+            if (p.head_w && inb)
+            {
+                if (p.head_flow)
+                    *reinterpret_cast<float4 *>(p.head_flow + pix * CONV_HEAD) = make_float4(hacc[0], hacc[1], hacc[2], hacc[3]);
+                if (p.head_flow16)
+                {
+                    const __half2 h0 = __floats2half2_rn(hacc[0], hacc[1]), h1 = __floats2half2_rn(hacc[2], hacc[3]);
+                    *reinterpret_cast<uint2 *>(p.head_flow16 + pix * CONV_HEAD) =
+                        make_uint2(*reinterpret_cast<const uint32_t *>(&h0), *reinterpret_cast<const uint32_t *>(&h1));
+                }
             }
             tc_fence_before();
             __syncwarp();

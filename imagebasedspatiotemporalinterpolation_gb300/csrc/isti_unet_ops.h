@@ -12,10 +12,22 @@
 
 namespace isti_unet
 {
+// A 1x1 head of 4 outputs (f32 weights [4][cout] and bias) to fuse into a convolution's
+// epilogue: its outputs go to flow (f32) and/or flow16 (f16), [pixel][4].
+struct ConvHead
+{
+    const float *w, *b;
+    float *flow;
+    void *flow16;
+};
+
 // pdl: launch as a programmatic dependent of the previous kernel in `stream` (it prepares
-// while that kernel finishes; see griddep_wait in isti_tc.cuh)
+// while that kernel finishes; see griddep_wait in isti_tc.cuh).  head: fuse that head into
+// the epilogue where the row-tile kernel runs the layer (then `out` is not written and
+// *head_fused is set); otherwise the layer runs as usual and *head_fused is cleared.
 isti_status conv_launch(int taps, const void *x, int n, int h, int w, int cin, const void *wpack, const float *bias, const void *mask, int relu,
-                        void *out, int cout, int32_t *status, cudaStream_t stream, bool pdl = false);
+                        void *out, int cout, int32_t *status, cudaStream_t stream, bool pdl = false, const ConvHead *head = nullptr,
+                        bool *head_fused = nullptr);
 
 // <<<grid, block, smem, stream>>> with, when `pdl`, the programmatic-dependent-launch
 // attribute; the kernel must call griddep_wait before it touches the previous kernel's data

@@ -70,3 +70,24 @@ def test_training_reduces_loss(cuda):
     assert net.device_status() == 0
     assert net.loss() < 0.5 * first, (first, net.loss())
     net.close()
+
+
+def test_forward_with_fused_head_matches_oracle(cuda):
+    """Rows of 128 pixels or more run the last 3x3 layer on the row-tile kernel, whose
+    epilogue also computes the 1x1 head (the layer's own output is then not stored): the
+    flow matches the oracle like the separate head's, and the f16 copy is the f32 flow
+    rounded."""
+    import torch
+    net = FlowNet(seed=4)
+    x, _ = _batch(12, n=1, h=16, w=160)
+    f32 = torch.empty((1, 16, 160, 4), dtype=torch.float32, device="cuda")
+    f16 = torch.empty((1, 16, 160, 4), dtype=torch.float16, device="cuda")
+    net.forward(x, flow=f32, flow16=f16)
+    torch.cuda.synchronize()
+    assert net.device_status() == 0
+    params = net.params().cpu().numpy().astype(np.float64)
+    acts = OF.forward(params, x.float().cpu().numpy().astype(np.float64), True)
+    got = f32.cpu().numpy()
+    assert np.abs(got - acts["flow"]).max() <= 1e-2 * np.abs(acts["flow"]).max()
+    assert torch.equal(f16, f32.half())
+    net.close()
