@@ -924,80 +924,86 @@ def run_e2e(args, seq, res, clients, r, dev, world):
     and shadows; plus the earlier keyframe's forward motion and shadows), the 3
     frames are rendered, the 3 frames come back.  Each keyframe's images sit in
     one pinned host slab and one device slab, ordered so that what a step needs
-    of it is one contiguous range: 2 large copies per step.  Every keyframe of
-    the cycle has its own device slab, so when the steps wrap around to the
-    first pair its earlier keyframe is still resident, as in an endless stream.
-    Three streams overlap the upload of step s + 1 and the read-back of step
-    s - 1 with the rendering of step s; the timed region spans all of them."""
+    of it is one contiguous range: 2 large copies per step.  Colour travels as
+    packed RGB, shadows as sparse entries (isti_unpack_shadows: the pixels whose
+    shadow-info field is non-zero, the only ones the renderer reads); both are
+    expanded on the device.  Every keyframe of the cycle has its own device slab,
+    so when the steps wrap around to the first pair its earlier keyframe is still
+    resident, as in an endless stream.  Three streams overlap the upload of step
+    s + 1 and the read-back of step s - 1 with the rendering of step s; the timed
+    region spans all of them."""
     import ctypes as C
 
     import numpy as np
     import torch
 
     from imagebasedspatiotemporalinterpolation_gb300 import native
-    from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame, DeviceView
+    from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame, DeviceView, pack_shadow_entries
 
     P = args.pairs
     n_cams = 1 + len(AUX)
-    # Slab layout of one keyframe: [arrival part | forward part], each grouped by image kind
-    # over the cameras.  arrival = colour, backward shadow A/B/Info, z, backward motion;
-    # forward = forward motion, forward shadows.  Colour and shadow images travel as packed
-    # RGB and are expanded to RGBA on the device after upload (isti_rgb8_to_rgba8, one launch
-    # per part): the renderer never reads the shadow images' alpha, and the colour images
-    # come from RGB sources (alpha 255, what an RGB PNG decodes to; asserted below).
+    # Slab layout of one keyframe: [arrival part | forward part], each grouped by kind over
+    # the cameras.  arrival = colour (packed RGB), z, backward motion, backward shadow entries;
+    # forward = forward motion, forward shadow entries.  The colour images come from RGB
+    # sources (alpha 255, what an RGB PNG decodes to; asserted below).  Shadow entries have a
+    # size of their own per keyframe and camera, so each keyframe has its own layout.
     zb, mot, rgb = H * W * 4, H * W * 6, H * W * 3   # each a multiple of 256 bytes
-    layout, off = {}, 0
-    for kind, n in (("color", rgb), ("sb", 3 * rgb), ("z", zb), ("mb", mot), ("mf", mot), ("sf", 3 * rgb)):
-        for c in range(n_cams):
-            layout[(kind, c)] = (off, n)
-            off += n
-    slab_bytes = off
-    A = layout[("mf", 0)][0]            # arrival part = [0, A), forward part = [A, slab_bytes)
-    sf_lo = layout[("sf", 0)][0]
-    n_arr_rgb, n_fwd_rgb = 4 * n_cams, 3 * n_cams   # RGB images per part, contiguous from 0 / sf_lo
-
-    def fields(slab, c):
-        """Tensor views of camera c's images inside one slab (host or device)."""
-        sl = lambda kind: slab[layout[(kind, c)][0]:layout[(kind, c)][0] + layout[(kind, c)][1]]
-        return dict(color=sl("color").view(H, W, 3), z=sl("z").view(torch.float32).view(H, W),
-                    mf=sl("mf").view(torch.float16).view(H, W, 3), mb=sl("mb").view(torch.float16).view(H, W, 3),
-                    sf=sl("sf").view(3, H, W, 3), sb=sl("sb").view(3, H, W, 3))
-
-    host = []
+    pad = lambda n: (n + 255) // 256 * 256
+    host, layouts, packs = [], [], []
     for k in range(P + 1):
-        slab = torch.empty(slab_bytes, dtype=torch.uint8).pin_memory()
-        for c in range(n_cams):
-            kf, f = seq.keyframe(k, c), fields(slab, c)
+        kfs = [seq.keyframe(k, c) for c in range(n_cams)]
+        for kf in kfs:
             if not (kf.color[..., 3] == 255).all():
                 raise RuntimeError("e2e uploads colour as RGB: the source colour must be opaque")
-            f["color"].copy_(torch.from_numpy(np.ascontiguousarray(kf.color[..., :3])))
-            f["z"].copy_(torch.from_numpy(np.ascontiguousarray(kf.z, np.float32)))
-            f["mf"].copy_(torch.from_numpy(np.ascontiguousarray(kf.motion_fwd, np.float16)))
-            f["mb"].copy_(torch.from_numpy(np.ascontiguousarray(kf.motion_bwd, np.float16)))
-            for i in range(3):
-                f["sf"][i].copy_(torch.from_numpy(np.ascontiguousarray(kf.shadow_fwd[i][..., :3])))
-                f["sb"][i].copy_(torch.from_numpy(np.ascontiguousarray(kf.shadow_bwd[i][..., :3])))
+        # the shadow images in (A, B, Info) order: the renderer's shadow_a, shadow_b, shadow_info
+        pk = {("sb", c): pack_shadow_entries(kfs[c].shadow_bwd[2], kfs[c].shadow_bwd[0], kfs[c].shadow_bwd[1]) for c in range(n_cams)}
+        pk.update({("sf", c): pack_shadow_entries(kfs[c].shadow_fwd[2], kfs[c].shadow_fwd[0], kfs[c].shadow_fwd[1]) for c in range(n_cams)})
+        layout, off = {}, 0
+        for kind in ("color", "z", "mb", "sb", "mf", "sf"):
+            for c in range(n_cams):
+                n = {"color": rgb, "z": zb, "mb": mot, "mf": mot}[kind] if kind not in ("sb", "sf") else pk[(kind, c)].nbytes
+                layout[(kind, c)] = (off, n)
+                off += pad(n)
+        layout["A"] = layout[("mf", 0)][0]   # arrival part = [0, A), forward part = [A, total)
+        layout["total"] = off
+        slab = torch.zeros(off, dtype=torch.uint8).pin_memory()
+        put = lambda key, arr: slab[layout[key][0]:layout[key][0] + layout[key][1]].copy_(
+            torch.from_numpy(np.ascontiguousarray(arr).reshape(-1).view(np.uint8)))
+        for c, kf in enumerate(kfs):
+            put(("color", c), kf.color[..., :3])
+            put(("z", c), np.asarray(kf.z, np.float32))
+            put(("mb", c), np.asarray(kf.motion_bwd, np.float16))
+            put(("mf", c), np.asarray(kf.motion_fwd, np.float16))
+            for kind in ("sb", "sf"):
+                if layout[(kind, c)][1]:
+                    put((kind, c), pk[(kind, c)])
         host.append(slab)
-    ring = [torch.empty(slab_bytes, dtype=torch.uint8, device=dev) for _ in range(P + 1)]
+        layouts.append(layout)
+        packs.append({key: len(v) for key, v in pk.items()})
+    ring = [torch.empty(layouts[k]["total"], dtype=torch.uint8, device=dev) for k in range(P + 1)]
     # RGBA images the renderer reads, per slot: arrival [colour per camera, then A, B, Info
-    # per camera] and forward [A, B, Info per camera], in the order of the RGB blocks
-    rgba_arr = [torch.empty((n_arr_rgb, H, W, 4), dtype=torch.uint8, device=dev) for _ in range(P + 1)]
-    rgba_fwd = [torch.empty((n_fwd_rgb, H, W, 4), dtype=torch.uint8, device=dev) for _ in range(P + 1)]
+    # per camera] and forward [A, B, Info per camera]
+    rgba_arr = [torch.empty((4 * n_cams, H, W, 4), dtype=torch.uint8, device=dev) for _ in range(P + 1)]
+    rgba_fwd = [torch.empty((3 * n_cams, H, W, 4), dtype=torch.uint8, device=dev) for _ in range(P + 1)]
+
+    def dev_field(slot, kind, c, dtype, shape):
+        lo, n = layouts[slot][(kind, c)]
+        return ring[slot][lo:lo + n].view(dtype).view(*shape)
+
     ring_fields = []
-    for s_, ra, rf in zip(ring, rgba_arr, rgba_fwd):
+    for slot in range(P + 1):
         per_cam = []
         for c in range(n_cams):
-            f = fields(s_, c)
-            f["color"] = ra[c]
-            f["sb"] = [ra[n_cams + 3 * c + i] for i in range(3)]
-            f["sf"] = [rf[3 * c + i] for i in range(3)]
-            per_cam.append(f)
+            per_cam.append(dict(color=rgba_arr[slot][c], z=dev_field(slot, "z", c, torch.float32, (H, W)),
+                                mb=dev_field(slot, "mb", c, torch.float16, (H, W, 3)), mf=dev_field(slot, "mf", c, torch.float16, (H, W, 3)),
+                                sb=[rgba_arr[slot][n_cams + 3 * c + i] for i in range(3)],
+                                sf=[rgba_fwd[slot][3 * c + i] for i in range(3)]))
         ring_fields.append(per_cam)
     lib = native.load()
     outs_dev = [[torch.zeros((H, W, 4), dtype=torch.uint8, device=dev) for _ in TS] for _ in range(2)]
     outs_host = [[torch.empty((H, W, 4), dtype=torch.uint8).pin_memory() for _ in TS] for _ in range(2)]
     up, comp, down = torch.cuda.Stream(dev), torch.cuda.Stream(dev), torch.cuda.Stream(dev)
-    xp = torch.cuda.Stream(dev, priority=-1)   # RGB -> RGBA expansion of the uploaded colour and shadow images
+    xp = torch.cuda.Stream(dev, priority=-1)   # expansion of the uploaded colour and shadow data
     ups = [up, xp]
     ev = lambda: torch.cuda.Event()
     up_done, comp_done, down_done = {}, {}, {}
@@ -1006,6 +1012,24 @@ def run_e2e(args, seq, res, clients, r, dev, world):
 
     last_use = {}  # (ring slot, "arr" | "fwd") -> last step that read that part
     last_frame = []  # [pair, DeviceFrame] of the latest step
+
+    def expand(slot, part, k):
+        """Device-side expansion of one uploaded part of keyframe k in its slot (stream xp)."""
+        st = C.c_void_p(xp.cuda_stream)
+        launches = 0
+        if part == "arr":
+            lo = layouts[slot][("color", 0)][0]
+            native.check(lib.isti_rgb8_to_rgba8(rgba_arr[slot].data_ptr(), ring[slot][lo:].data_ptr(), n_cams * H * W, st))
+            launches += 1
+        kind = "sb" if part == "arr" else "sf"
+        for c in range(n_cams):
+            a_, b_, info = ring_fields[slot][c][kind]
+            lo, _ = layouts[slot][(kind, c)]
+            n = packs[k][(kind, c)]
+            native.check(lib.isti_unpack_shadows(info.data_ptr(), a_.data_ptr(), b_.data_ptr(), H * W,
+                                                 C.c_void_p(ring[slot][lo:].data_ptr() if n else None), n, st))
+            launches += 1 + (1 if n else 0) + 3   # three clears and the scatter
+        return launches
 
     def step(s, count):
         p = s % P
@@ -1019,20 +1043,18 @@ def run_e2e(args, seq, res, clients, r, dev, world):
             if (slot, part) in last_use:
                 up.wait_event(comp_done[last_use[(slot, part)]])
         for slot, part, k in copies:
-            lo, hi = (0, A) if part == "arr" else (A, slab_bytes)
+            A, total = layouts[k]["A"], layouts[k]["total"]
+            lo, hi = (0, A) if part == "arr" else (A, total)
             with torch.cuda.stream(up):
                 ring[slot][lo:hi].copy_(host[k][lo:hi], non_blocking=True)
             # the expansion runs on its own high-priority stream, so the link keeps copying
             copied = ev()
             copied.record(up)
             xp.wait_event(copied)
-            n_img = n_arr_rgb if part == "arr" else n_fwd_rgb
-            src = ring[slot][0 if part == "arr" else sf_lo:][:n_img * rgb]
-            dst = rgba_arr[slot] if part == "arr" else rgba_fwd[slot]
-            native.check(lib.isti_rgb8_to_rgba8(dst.data_ptr(), src.data_ptr(), n_img * H * W, C.c_void_p(xp.cuda_stream)))
+            n_launch = expand(slot, part, k)
             if count:
                 counters["h2d"] += hi - lo
-                counters["launches"] += 1
+                counters["launches"] += n_launch
         resident[s0], resident[s1] = k0, k1
         up_done[s] = [ev()]
         up_done[s][0].record(xp)
@@ -1097,9 +1119,9 @@ def run_e2e(args, seq, res, clients, r, dev, world):
         raise RuntimeError("e2e: frames rendered from the streamed keyframes differ from the resident ones")
     return {"value": round(value, 2), "unit": "Mpix/s", "h2d_bytes_per_step": counters["h2d"] // args.steps,
             "d2h_bytes_per_step": counters["d2h"] // args.steps, "ms_per_step": round(ms / args.steps, 4),
-            "expand_launches_per_step": counters["launches"] / args.steps,
-            "pipeline": "one contiguous slab per keyframe, 2 uploads per step (colour and shadow images as RGB, "
-                        "expanded to RGBA on the device) / render / read-back overlapped"}
+            "expand_ops_per_step": counters["launches"] / args.steps,
+            "pipeline": "one contiguous slab per keyframe, 2 uploads per step (colour as RGB, shadows as sparse "
+                        "entries of the pixels the renderer reads, both expanded on the device) / render / read-back overlapped"}
 
 
 def main():

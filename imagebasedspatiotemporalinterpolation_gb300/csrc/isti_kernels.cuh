@@ -1155,6 +1155,24 @@ __global__ void rgb8_to_rgba8_kernel(uint32_t *__restrict__ dst, const uint8_t *
         dst[i] = (uint32_t)__ldg(src + 3 * i) | (uint32_t)__ldg(src + 3 * i + 1) << 8 | (uint32_t)__ldg(src + 3 * i + 2) << 16 | 0xff000000u;
 }
 
+// Sparse shadow entries -> the three RGBA8 shadow images (zeroed before): one thread per
+// entry {pixel index, info RGB, A RGB, B RGB, pad} (16 bytes).
+__global__ void unpack_shadows_kernel(uint32_t *__restrict__ info, uint32_t *__restrict__ a, uint32_t *__restrict__ b, size_t n_pixels,
+                                      const uint4 *__restrict__ entries, size_t n_entries)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n_entries; e += stride)
+    {
+        const uint4 v = __ldg(entries + e);
+        if (v.x >= n_pixels)
+            continue;
+        // bytes 4..15: info R G B, A R G B, B R G B, pad (little-endian words y, z, w)
+        info[v.x] = (v.y & 0xffffffu) | 0xff000000u;
+        a[v.x] = (v.y >> 24) | ((v.z & 0xffffu) << 8) | 0xff000000u;
+        b[v.x] = (v.z >> 16) | ((v.w & 0xffu) << 16) | 0xff000000u;
+    }
+}
+
 // Dynamic shared memory of one reprojection block of `n_units` units.
 template <int SW>
 constexpr size_t reproj_smem(int n_views, int n_units)

@@ -351,3 +351,43 @@ def rgb8_to_rgba8(dst, src, stream=None) -> None:
         raise ValueError("rgb8_to_rgba8 expects contiguous uint8 (..., 3) -> (..., 4) tensors of the same pixel count")
     s = (stream or torch.cuda.current_stream()).cuda_stream
     check(native.load().isti_rgb8_to_rgba8(_dptr(dst), _dptr(src), C.c_size_t(src.numel() // 3), C.c_void_p(s)))
+
+
+SHADOW_ENTRY_BYTES = 16  # ISTI_SHADOW_ENTRY_BYTES
+
+
+def pack_shadow_entries(info, a, b):
+    """Host side of isti_unpack_shadows: the sparse form of one view's shadow info, colour A
+    and colour B images ((H, W, 3 or 4) uint8 numpy arrays).  One 16-byte entry per pixel
+    whose info field (R, G, B) is non-zero -- the only pixels where the renderer reads any of
+    the three images: pixel index (uint32 little-endian), info RGB, A RGB, B RGB, 3 zero
+    bytes.  Returns an (n, 16) uint8 array."""
+    import numpy as np
+    info, a, b = (np.asarray(x) for x in (info, a, b))
+    if not (info.shape[:2] == a.shape[:2] == b.shape[:2]) or info.dtype != np.uint8 or a.dtype != np.uint8 or b.dtype != np.uint8:
+        raise ValueError("shadow images must be uint8 arrays of one size")
+    n_px = info.shape[0] * info.shape[1]
+    if n_px >= 1 << 32:
+        raise ValueError("too many pixels for 32-bit indices")
+    rgb = lambda x: x.reshape(n_px, x.shape[-1])[:, :3]
+    idx = np.flatnonzero(rgb(info).any(axis=1))
+    out = np.zeros((len(idx), SHADOW_ENTRY_BYTES), np.uint8)
+    out[:, 0:4] = idx.astype("<u4").view(np.uint8).reshape(-1, 4)
+    out[:, 4:7] = rgb(info)[idx]
+    out[:, 7:10] = rgb(a)[idx]
+    out[:, 10:13] = rgb(b)[idx]
+    return out
+
+
+def unpack_shadows(info, a, b, entries, n_entries=None, stream=None) -> None:
+    """isti_unpack_shadows: device RGBA8 tensors info, a, b ((H, W, 4) uint8, 16-byte aligned)
+    <- zero, then the listed pixels of `entries` (a device uint8 tensor of n x 16 bytes, as
+    pack_shadow_entries makes them)."""
+    torch = _torch()
+    for t in (info, a, b):
+        if t.dtype != torch.uint8 or t.shape[-1] != 4 or not t.is_contiguous() or t.shape != info.shape:
+            raise ValueError("unpack_shadows expects three contiguous uint8 (..., 4) tensors of one shape")
+    n = entries.numel() // SHADOW_ENTRY_BYTES if n_entries is None else int(n_entries)
+    s = (stream or torch.cuda.current_stream()).cuda_stream
+    check(native.load().isti_unpack_shadows(_dptr(info), _dptr(a), _dptr(b), C.c_size_t(info.numel() // 4),
+                                            C.c_void_p(_dptr(entries) if n else None), C.c_size_t(n), C.c_void_p(s)))

@@ -102,6 +102,20 @@ isti_status isti_normalize_proj(const float proj[16], float out[16]);
  * expand them on the device.  dst and src must not overlap. */
 isti_status isti_rgb8_to_rgba8(void *dst_rgba, const void *src_rgb, size_t n_pixels, void *stream);
 
+/* Sparse shadow images (no counterpart in the reference, whose loader reads dense PNGs).
+ * The renderer reads a view's shadow info, colour A and colour B images only at pixels whose
+ * shadow-info field (R, G, B) is non-zero, and reads no alpha byte of them (src/renderer.cu
+ * :217-295).  A caller bound by the host link can therefore send just those pixels: each
+ * entry is 16 bytes -- the pixel index (uint32, little-endian), info R G B, colour A R G B,
+ * colour B R G B, 3 bytes of padding (ISTI_SHADOW_ENTRY_BYTES).  isti_unpack_shadows writes
+ * the three RGBA8 images of n_pixels (device, 16-byte aligned, not overlapping the entries)
+ * on `stream`: zero everywhere, then each listed pixel's colours with alpha 255.  Entries
+ * whose index is not below n_pixels are skipped.  Rendering with the unpacked images gives
+ * the same frames as with the dense ones. */
+#define ISTI_SHADOW_ENTRY_BYTES 16
+isti_status isti_unpack_shadows(void *info_rgba, void *a_rgba, void *b_rgba, size_t n_pixels, const void *entries, size_t n_entries,
+                                void *stream);
+
 /* Host matrix helpers of the frame loop (src/main.cu:26-28,161,176), the glm
  * operations the reference applies: out = a * b, out = inverse(m), and
  * glm::interpolate(m1, m2, t). */
