@@ -1013,6 +1013,12 @@ def run_e2e(args, seq, res, clients, r, dev, world):
     last_use = {}  # (ring slot, "arr" | "fwd") -> last step that read that part
     last_frame = []  # [pair, DeviceFrame] of the latest step
 
+    # entries last unpacked into each slot's shadow images: the next unpack clears only their
+    # pixels (the images are zero elsewhere) instead of the whole images
+    prev_entries = {(slot, kind, c): torch.empty(max(16, packs[slot][(kind, c)] * 16), dtype=torch.uint8, device=dev)
+                    for slot in range(P + 1) for kind in ("sb", "sf") for c in range(n_cams)}
+    prev_n = {}
+
     def expand(slot, part, k):
         """Device-side expansion of one uploaded part of keyframe k in its slot (stream xp)."""
         st = C.c_void_p(xp.cuda_stream)
@@ -1026,9 +1032,19 @@ def run_e2e(args, seq, res, clients, r, dev, world):
             a_, b_, info = ring_fields[slot][c][kind]
             lo, _ = layouts[slot][(kind, c)]
             n = packs[k][(kind, c)]
+            key = (slot, kind, c)
+            if n * 16 > prev_entries[key].numel():
+                raise RuntimeError("e2e: a slot received more shadow entries than its buffer holds")
+            nc = prev_n.get(key)
             native.check(lib.isti_unpack_shadows(info.data_ptr(), a_.data_ptr(), b_.data_ptr(), H * W,
-                                                 C.c_void_p(ring[slot][lo:].data_ptr() if n else None), n, st))
-            launches += 1 + (1 if n else 0) + 3   # three clears and the scatter
+                                                 C.c_void_p(ring[slot][lo:].data_ptr() if n else None), n,
+                                                 C.c_void_p(prev_entries[key].data_ptr() if nc is not None else None), nc or 0, st))
+            launches += (3 if nc is None else (1 if nc else 0)) + (1 if n else 0)   # clears, scatter
+            if n:
+                with torch.cuda.stream(xp):
+                    prev_entries[key][:n * 16].copy_(ring[slot][lo:lo + n * 16], non_blocking=True)
+                launches += 1
+            prev_n[key] = n
         return launches
 
     def step(s, count):

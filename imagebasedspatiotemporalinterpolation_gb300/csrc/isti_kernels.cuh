@@ -1173,6 +1173,19 @@ __global__ void unpack_shadows_kernel(uint32_t *__restrict__ info, uint32_t *__r
     }
 }
 
+// The pixels of sparse shadow entries <- 0 in the three shadow images.
+__global__ void clear_shadows_kernel(uint32_t *__restrict__ info, uint32_t *__restrict__ a, uint32_t *__restrict__ b, size_t n_pixels,
+                                     const uint4 *__restrict__ entries, size_t n_entries)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n_entries; e += stride)
+    {
+        const uint32_t i = __ldg(&entries[e].x);
+        if (i < n_pixels)
+            info[i] = a[i] = b[i] = 0u;
+    }
+}
+
 // Dynamic shared memory of one reprojection block of `n_units` units.
 template <int SW>
 constexpr size_t reproj_smem(int n_views, int n_units)

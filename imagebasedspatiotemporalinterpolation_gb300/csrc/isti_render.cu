@@ -1324,29 +1324,40 @@ extern "C" isti_status isti_rgb8_to_rgba8(void *dst_rgba, const void *src_rgb, s
 
 // Sparse shadow entries -> RGBA8 shadow images, declared in include/isti_dataset.h.
 extern "C" isti_status isti_unpack_shadows(void *info_rgba, void *a_rgba, void *b_rgba, size_t n_pixels, const void *entries, size_t n_entries,
-                                           void *stream_ptr)
+                                           const void *clear_entries, size_t n_clear, void *stream_ptr)
 {
     if (n_pixels == 0)
         return ISTI_OK;
     if (!info_rgba || !a_rgba || !b_rgba || (n_entries && !entries))
         return fail(ISTI_ERR_INVALID_ARG, "isti_unpack_shadows: NULL buffer");
-    if ((((uintptr_t)info_rgba | (uintptr_t)a_rgba | (uintptr_t)b_rgba | (uintptr_t)entries) & 15u) != 0)
+    if ((((uintptr_t)info_rgba | (uintptr_t)a_rgba | (uintptr_t)b_rgba | (uintptr_t)entries | (uintptr_t)clear_entries) & 15u) != 0)
         return fail(ISTI_ERR_INVALID_ARG, "isti_unpack_shadows: buffers must be 16-byte aligned");
     const size_t img = 4 * n_pixels;
     const uintptr_t imgs[3] = {(uintptr_t)info_rgba, (uintptr_t)a_rgba, (uintptr_t)b_rgba};
-    const uintptr_t e0 = (uintptr_t)entries, e1 = e0 + n_entries * ISTI_SHADOW_ENTRY_BYTES;
+    const uintptr_t lists[2][2] = {{(uintptr_t)entries, (uintptr_t)entries + n_entries * ISTI_SHADOW_ENTRY_BYTES},
+                                   {(uintptr_t)clear_entries, (uintptr_t)clear_entries + (clear_entries ? n_clear : 0) * ISTI_SHADOW_ENTRY_BYTES}};
     for (int i = 0; i < 3; i++)
     {
         for (int j = i + 1; j < 3; j++)
             if (imgs[i] < imgs[j] + img && imgs[j] < imgs[i] + img)
                 return fail(ISTI_ERR_INVALID_ARG, "isti_unpack_shadows: images overlap");
-        if (n_entries && imgs[i] < e1 && e0 < imgs[i] + img)
-            return fail(ISTI_ERR_INVALID_ARG, "isti_unpack_shadows: an image overlaps the entries");
+        for (const auto &l : lists)
+            if (l[1] > l[0] && imgs[i] < l[1] && l[0] < imgs[i] + img)
+                return fail(ISTI_ERR_INVALID_ARG, "isti_unpack_shadows: an image overlaps the entries");
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream_ptr);
     cudaError_t e = cudaSuccess;
-    for (int i = 0; i < 3 && e == cudaSuccess; i++)
-        e = cudaMemsetAsync(reinterpret_cast<void *>(imgs[i]), 0, img, st);
+    if (!clear_entries)
+        for (int i = 0; i < 3 && e == cudaSuccess; i++)
+            e = cudaMemsetAsync(reinterpret_cast<void *>(imgs[i]), 0, img, st);
+    else if (n_clear)
+    {
+        const unsigned blocks = (unsigned)std::min<size_t>((n_clear + 255) / 256, 152 * 8);
+        isti::clear_shadows_kernel<<<blocks, 256, 0, st>>>(static_cast<uint32_t *>(info_rgba), static_cast<uint32_t *>(a_rgba),
+                                                           static_cast<uint32_t *>(b_rgba), n_pixels, static_cast<const uint4 *>(clear_entries),
+                                                           n_clear);
+        e = cudaGetLastError();
+    }
     if (e == cudaSuccess && n_entries)
     {
         const unsigned blocks = (unsigned)std::min<size_t>((n_entries + 255) / 256, 152 * 8);

@@ -151,7 +151,8 @@ DATASET_SIGNATURES = {
     "isti_depth_to_z": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
     "isti_normalize_proj": (C.c_int, [_f32p, _f32p]),
     "isti_rgb8_to_rgba8": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
-    "isti_unpack_shadows": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "isti_unpack_shadows": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t,
+                                      C.c_void_p]),
     "isti_mat4_mul": (None, [_f32p, _f32p, _f32p]),
     "isti_mat4_inverse": (None, [_f32p, _f32p]),
     "isti_mat4_interpolate": (None, [_f32p, _f32p, C.c_float, _f32p]),

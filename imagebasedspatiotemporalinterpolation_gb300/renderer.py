@@ -379,15 +379,19 @@ def pack_shadow_entries(info, a, b):
     return out
 
 
-def unpack_shadows(info, a, b, entries, n_entries=None, stream=None) -> None:
+def unpack_shadows(info, a, b, entries, n_entries=None, clear_entries=None, n_clear=None, stream=None) -> None:
     """isti_unpack_shadows: device RGBA8 tensors info, a, b ((H, W, 4) uint8, 16-byte aligned)
     <- zero, then the listed pixels of `entries` (a device uint8 tensor of n x 16 bytes, as
-    pack_shadow_entries makes them)."""
+    pack_shadow_entries makes them).  clear_entries: the entries of the previous unpack into
+    the same images, whose pixels alone are then cleared."""
     torch = _torch()
     for t in (info, a, b):
         if t.dtype != torch.uint8 or t.shape[-1] != 4 or not t.is_contiguous() or t.shape != info.shape:
             raise ValueError("unpack_shadows expects three contiguous uint8 (..., 4) tensors of one shape")
     n = entries.numel() // SHADOW_ENTRY_BYTES if n_entries is None else int(n_entries)
+    nc = 0 if clear_entries is None else (clear_entries.numel() // SHADOW_ENTRY_BYTES if n_clear is None else int(n_clear))
     s = (stream or torch.cuda.current_stream()).cuda_stream
     check(native.load().isti_unpack_shadows(_dptr(info), _dptr(a), _dptr(b), C.c_size_t(info.numel() // 4),
-                                            C.c_void_p(_dptr(entries) if n else None), C.c_size_t(n), C.c_void_p(s)))
+                                            C.c_void_p(_dptr(entries) if n else None), C.c_size_t(n),
+                                            C.c_void_p(_dptr(clear_entries) if clear_entries is not None else None), C.c_size_t(nc),
+                                            C.c_void_p(s)))

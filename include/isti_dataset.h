@@ -111,10 +111,14 @@ isti_status isti_rgb8_to_rgba8(void *dst_rgba, const void *src_rgb, size_t n_pix
  * the three RGBA8 images of n_pixels (device, 16-byte aligned, not overlapping the entries)
  * on `stream`: zero everywhere, then each listed pixel's colours with alpha 255.  Entries
  * whose index is not below n_pixels are skipped.  Rendering with the unpacked images gives
- * the same frames as with the dense ones. */
+ * the same frames as with the dense ones.
+ *
+ * clear_entries: NULL, or the entries of the previous unpack into the same three images
+ * (which are then zero everywhere else): only their pixels are cleared instead of the whole
+ * images, which saves 12 bytes of device writes per pixel. */
 #define ISTI_SHADOW_ENTRY_BYTES 16
 isti_status isti_unpack_shadows(void *info_rgba, void *a_rgba, void *b_rgba, size_t n_pixels, const void *entries, size_t n_entries,
-                                void *stream);
+                                const void *clear_entries, size_t n_clear, void *stream);
 
 /* Host matrix helpers of the frame loop (src/main.cu:26-28,161,176), the glm
  * operations the reference applies: out = a * b, out = inverse(m), and

@@ -59,6 +59,22 @@ def test_unpack_equals_dense_where_read(cuda):
 
 
 @pytest.mark.gpu
+def test_unpack_clearing_the_previous_entries_equals_a_fresh_unpack(cuda):
+    import torch
+    from imagebasedspatiotemporalinterpolation_gb300.renderer import unpack_shadows
+    e1 = torch.from_numpy(pack_shadow_entries(*_images(3, 29, 31))).cuda()
+    e2 = torch.from_numpy(pack_shadow_entries(*_images(4, 29, 31))).cuda()
+    imgs = [torch.full((29, 31, 4), 77, dtype=torch.uint8, device="cuda") for _ in range(3)]
+    unpack_shadows(*imgs, e1)                      # whole images cleared
+    unpack_shadows(*imgs, e2, clear_entries=e1)    # only e1's pixels cleared
+    fresh = [torch.full((29, 31, 4), 99, dtype=torch.uint8, device="cuda") for _ in range(3)]
+    unpack_shadows(*fresh, e2)
+    torch.cuda.synchronize()
+    for a, b in zip(imgs, fresh):
+        assert torch.equal(a, b)
+
+
+@pytest.mark.gpu
 def test_frames_from_unpacked_shadows_equal_dense(cuda):
     import torch
     from imagebasedspatiotemporalinterpolation_gb300.renderer import DeviceFrame, DeviceView, Renderer, unpack_shadows
