@@ -21,6 +21,7 @@
 #pragma once
 
 #include "isti.h"
+#include "isti_dataset.h"
 #include "isti_io.h"
 
 #include <cuda_runtime.h>
@@ -440,4 +441,28 @@ private:
     std::vector<isti_view> _curr, _next;
     std::vector<int32_t> _prio;
 };
+
+// Host side of isti_unpack_shadows (include/isti_dataset.h; no counterpart in the reference):
+// the sparse entries of one view's shadow info, colour A and colour B images (host pixels,
+// `ch_*` bytes per pixel, at least 3, R G B first).  One ISTI_SHADOW_ENTRY_BYTES entry per
+// pixel whose info R, G or B is non-zero: index (uint32 little-endian), info RGB, A RGB,
+// B RGB, 3 zero bytes.
+inline std::vector<uint8_t> pack_shadow_entries(const uint8_t *info, int ch_info, const uint8_t *a, int ch_a, const uint8_t *b, int ch_b,
+                                                uint32_t n_pixels)
+{
+    if (!info || !a || !b || ch_info < 3 || ch_a < 3 || ch_b < 3)
+        throw Error(ISTI_ERR_INVALID_ARG, "pack_shadow_entries: three images of at least 3 channels");
+    std::vector<uint8_t> out;
+    for (uint32_t i = 0; i < n_pixels; i++)
+    {
+        const uint8_t *pi = info + (size_t)i * ch_info;
+        if (!(pi[0] | pi[1] | pi[2]))
+            continue;
+        const uint8_t *pa = a + (size_t)i * ch_a, *pb = b + (size_t)i * ch_b;
+        const uint8_t e[ISTI_SHADOW_ENTRY_BYTES] = {(uint8_t)i, (uint8_t)(i >> 8), (uint8_t)(i >> 16), (uint8_t)(i >> 24),
+                                                    pi[0], pi[1], pi[2], pa[0], pa[1], pa[2], pb[0], pb[1], pb[2], 0, 0, 0};
+        out.insert(out.end(), e, e + ISTI_SHADOW_ENTRY_BYTES);
+    }
+    return out;
+}
 } // namespace isti

@@ -102,3 +102,29 @@ def test_frames_from_unpacked_shadows_equal_dense(cuda):
     for k, (x, y) in enumerate(zip(got, want)):
         assert torch.equal(x, y), f"frame {k}: {int((x != y).any(-1).sum())} pixels differ"
     r.close()
+
+
+def test_cpp_header_packs_like_python(tmp_path):
+    """isti::pack_shadow_entries (C++ header) writes the same entries as the Python packer."""
+    import os
+    import shutil
+    import subprocess
+
+    from imagebasedspatiotemporalinterpolation_gb300 import _build
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not found")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = str(tmp_path / "shadow_pack_hpp")
+    res = subprocess.run([gxx, "-std=c++20", "-O2", "-Wall", "-Wextra", "-Werror", "-I", _build.INCLUDE,
+                          "-I", os.path.join(_build._cuda_home(), "include"),
+                          os.path.join(root, "tests", "cpp", "shadow_pack_hpp.cpp"), "-o", exe], capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr
+    info, a, b = _images(5, 41, 23)
+    src = tmp_path / "in.bin"
+    src.write_bytes(np.array([41 * 23], "<u4").tobytes() + info.tobytes() + a.tobytes() + b.tobytes())
+    res = subprocess.run([exe, str(src), str(tmp_path / "out.bin")], capture_output=True, text=True, timeout=60)
+    assert res.returncode == 0, res.stdout + res.stderr
+    want = pack_shadow_entries(info, a, b)
+    assert res.stdout.split() == ["ok", str(len(want))]
+    assert (tmp_path / "out.bin").read_bytes() == want.tobytes()
